@@ -1,0 +1,343 @@
+"""Benchmark: batched NDT scan alignment (20k-point scans against a 5M-point map).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+
+One step = one pass of the hot path over one batch of B synthetic 20k-point scans
+(128-ring ray-cast lidar on a seeded 400x400 m procedural map of 5M points; initial
+guesses from constant-velocity prediction + noise). Prints one JSON line.
+
+- value : aligns/s with the scans already resident in HBM (ndt_align_batch_device),
+          CUDA-event time on the library's stream, L2 flushed (256 MB write) between steps.
+- e2e   : aligns/s through the public C ABI with host buffers (ndt_align_batch): pinned
+          staging, host->device copy of the scans, kernels, device->host copy of results.
+- roofline : the Newton kernel's FP32 work (165 FLOP per point-iteration + 65 per
+          point-voxel pair, the moment formulation) over its CUDA-event time.
+- cpu_baseline : the CPU restatement of the reference's CPU path (NdtOptimizer::align)
+          on all host cores, on a bounded sample of the same scans.
+--impl reference times that CPU path alone (the reference's own implementation is Rust and
+cannot be built here; the restatement stands in for it).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "scan aligns/s (20k pts, 5M-pt map); init-pose est/s, learned vs plain"
+FLOP_PER_POINT_ITER = 165
+FLOP_PER_PAIR = 65
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--map-points", type=int, default=5_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--seed", type=int, default=2)
+    return ap.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def make_workload(args, rank, world):
+    from cuda_ndt_matcher_gb300 import synth
+    n_traj = max(1000, args.batch * world + 8)
+    seq = synth.Sequence(seed=args.seed, n_map=args.map_points, n_scans=n_traj)
+    ks = [2 + rank * args.batch + i for i in range(args.batch)]
+    scans = [seq.scan(k) for k in ks]
+    poses = np.stack([seq.guess(k) for k in ks])
+    truth = np.stack([seq.true_pose(k) for k in ks])
+    return seq, scans, poses, truth
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(grid_args, scans, poses, seconds, semantics="cpu"):
+    """Restated reference CPU path on all host cores over a bounded sample of the scans."""
+    from oracle import oracle as O
+    g = O.Grid(*grid_args)
+    cores = os.cpu_count() or 1
+    done = 0
+    t0 = time.perf_counter()
+    i = 0
+    while time.perf_counter() - t0 < seconds and i < len(scans):
+        j = min(len(scans), i + cores)
+        g.align_batch(scans[i:j], poses[i:j], semantics=semantics, nthreads=cores)
+        done += j - i
+        i = j
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "aligns/s", "cores": cores, "kind": "port",
+            "sample": f"{done} of the bench's 20k-point scans, NdtOptimizer::align restated "
+                      f"(FP64, all neighbours, ND-clamp + SVD step), {cores} threads, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    seq, scans, poses, _ = make_workload(args, 0, 1)
+    from oracle import oracle as O
+    g = O.Grid(seq.map, 2.0)
+    cores = os.cpu_count() or 1
+    per_step = cores
+    times = []
+    for s in range(args.warmup + args.steps):
+        i0 = (s * per_step) % max(1, len(scans) - per_step)
+        t0 = time.perf_counter()
+        g.align_batch(scans[i0:i0 + per_step], poses[i0:i0 + per_step], semantics="cpu",
+                      nthreads=cores)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "aligns/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans",
+                   "batch": per_step, "map_points": args.map_points, "scan_points": 20000},
+        "cpu_baseline": {"value": value, "unit": "aligns/s", "cores": cores, "kind": "port",
+                         "sample": f"{per_step} scans per step, NdtOptimizer::align restated "
+                                   "(the Rust reference cannot be built here)"},
+        "e2e": {"value": value, "unit": "aligns/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from cuda_ndt_matcher_gb300 import capi
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seq, scans, poses, truth = make_workload(args, rank, world)
+    ctx = capi.Context(device=local)
+    t0 = time.perf_counter()
+    ctx.set_target(seq.map)
+    info = ctx.map_info()
+    build_ms = float(info.build_ms)
+
+    # device-resident inputs
+    counts = np.array([len(s) for s in scans], np.uint64)
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
+    allpts = np.concatenate(scans).astype(np.float32)
+    d_pts = torch.from_numpy(allpts).cuda()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    import ctypes as C
+    off_c = np.ascontiguousarray(offsets)
+    pose_c = np.ascontiguousarray(poses, np.float64)
+    B = len(scans)
+    res_arr = (capi.Result * B)()
+
+    def step_device():
+        capi.check(ctx.lib.ndt_align_batch_device(ctx.h, C.c_void_p(d_pts.data_ptr()),
+                                                  off_c.ctypes.data, pose_c.ctypes.data, B,
+                                                  res_arr))
+
+    scan_arr = (capi.Scan * B)()
+    for i, s in enumerate(scans):
+        scan_arr[i].xyz = s.ctypes.data
+        scan_arr[i].num_points = len(s)
+        for k in range(6):
+            scan_arr[i].initial_pose[k] = float(poses[i][k])
+    res_e2e = (capi.Result * B)()
+
+    def step_host():
+        capi.check(ctx.lib.ndt_align_batch(ctx.h, scan_arr, B, res_e2e))
+
+    for _ in range(args.warmup):
+        step_device()
+        step_host()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    # timed region 1: device-resident value (CUDA events on the library stream)
+    ctx.stats_reset()
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = []
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step_device()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    st = ctx.stats()
+    # timed region 2: end to end through the host-buffer C ABI
+    ctx.stats_reset()
+    wall = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        step_host()
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t1
+    st_e2e = ctx.stats()
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([dev_ms, wall], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, wall = float(t[0]), float(t[1])
+
+    aligns = B * args.steps * world
+    value = aligns / (dev_ms / 1000.0)
+    e2e = aligns / wall
+    pk, src = peaks()
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    props = torch.cuda.get_device_properties(local)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    flops = FLOP_PER_POINT_ITER * st["point_iterations"] + FLOP_PER_PAIR * st["correspondences"]
+    kern_s = st["align_kernel_ms"] / 1000.0
+    achieved = flops / kern_s / 1e12 if kern_s > 0 else 0.0
+    launches = st["align_launches"]
+    # accuracy of this run against the true poses (diagnostic)
+    got = np.array([list(r.pose) for r in res_arr])
+    perr = np.linalg.norm(got[:, :2] - truth[:, :2], axis=1)
+    build_bytes = 248 * info.num_points + 64 * info.num_voxels + 16 * info.hash_capacity
+
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        cpu = cpu_baseline((seq.map, 2.0), scans, poses, args.cpu_seconds)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "aligns/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 reductions and 6x6 solve)",
+            "data": "synthetic",
+            "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans, "
+                                   "batched alignment", "batch": B, "scan_points": 20000,
+                       "map_points": args.map_points, "map_voxels": int(info.num_voxels),
+                       "semantics": "graph kernels K1-K5", "l2": "flushed (256 MB write) "
+                       "between steps"},
+            "e2e": {"value": e2e, "unit": "aligns/s",
+                    "h2d_bytes_per_step": int(st_e2e["h2d_bytes"] // max(args.steps, 1)),
+                    "d2h_bytes_per_step": int(st_e2e["d2h_bytes"] // max(args.steps, 1))},
+            "roofline": {"bound": "fp32", "kernel": "k_ndt_align", "achieved": achieved,
+                         "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak if fp32_peak else None,
+                         "traffic": None,
+                         "peak_source": f"derived: SMs x 128 FP32 lanes x 2 x sm_max_mhz "
+                                        f"({src} MEASURED_PEAKS.json clock)",
+                         "flops_per_launch": flops / max(launches, 1),
+                         "avg_launch_ms": st["align_kernel_ms"] / max(launches, 1),
+                         "iterations_per_align": st["iterations"] / max(st["alignments"], 1),
+                         "pairs_per_point_iter": st["correspondences"] /
+                         max(st["point_iterations"], 1)},
+            "build_roofline": {"bound": "hbm", "achieved": build_bytes / (build_ms / 1e3) / 1e9,
+                               "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                               "frac": build_bytes / (build_ms / 1e3) / 1e9 / pk.get("hbm_gbs"),
+                               "build_ms": build_ms, "bytes": int(build_bytes),
+                               "peak_source": src},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(st["align_launches"] + 2 * st["score_launches"]),
+            "accuracy": {"median_xy_err_m": float(np.median(perr)),
+                         "p99_xy_err_m": float(np.percentile(perr, 99))},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,296 @@
+"""ctypes binding of libndt_gb300.so (the C ABI declared in include/ndt_gb300.h).
+
+Loading fails loudly when the library is missing; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NDT_OK = 0
+ERRORS = {
+    -1: "NDT_ERR_INVALID_ARGUMENT", -2: "NDT_ERR_NO_TARGET", -3: "NDT_ERR_EMPTY_INPUT",
+    -4: "NDT_ERR_NO_VOXELS", -5: "NDT_ERR_RANGE", -6: "NDT_ERR_HASH_FULL",
+    -7: "NDT_ERR_PROBE_LIMIT", -8: "NDT_ERR_DEVICE", -9: "NDT_ERR_NO_DEVICE",
+    -10: "NDT_ERR_CAPACITY",
+}
+SEMANTICS_GPU_GRAPH = 0
+SEMANTICS_CPU = 1
+STATUS = {0: "Converged", 1: "MaxIterations", 2: "NoCorrespondences", 3: "SingularHessian"}
+
+# exported symbols, in the order of include/ndt_gb300.h
+EXPORTS = [
+    "ndt_config_default", "ndt_ctx_create", "ndt_ctx_destroy", "ndt_ctx_configure",
+    "ndt_ctx_stream",
+    "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
+    "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
+    "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
+    "ndt_profile_enable", "ndt_last_error_string", "ndt_radix_sort_pairs_u64_u32",
+    "ndt_detect_segments", "ndt_morton_codes",
+]
+
+
+class NdtError(RuntimeError):
+    def __init__(self, code, msg):
+        self.code = code
+        super().__init__(f"{ERRORS.get(code, 'cudaError %d' % code)}: {msg}")
+
+
+class Config(C.Structure):
+    _fields_ = [("resolution", C.c_float), ("max_iterations", C.c_int32),
+                ("trans_epsilon", C.c_double), ("step_size", C.c_double),
+                ("outlier_ratio", C.c_double), ("min_points_per_voxel", C.c_int32),
+                ("eigenvalue_ratio", C.c_float), ("max_neighbors", C.c_int32),
+                ("semantics", C.c_int32), ("min_correspondences", C.c_int32),
+                ("device", C.c_int32), ("cluster_size", C.c_int32),
+                ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
+
+
+class Result(C.Structure):
+    _fields_ = [("pose", C.c_double * 6), ("score", C.c_double),
+                ("transform_probability", C.c_double), ("nvtl", C.c_double),
+                ("hessian", C.c_double * 36), ("converged", C.c_int32),
+                ("iterations", C.c_int32), ("num_correspondences", C.c_int32),
+                ("oscillation_count", C.c_int32), ("status", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class Scan(C.Structure):
+    _fields_ = [("xyz", C.c_void_p), ("num_points", C.c_uint64),
+                ("initial_pose", C.c_double * 6)]
+
+
+class MapInfo(C.Structure):
+    _fields_ = [("num_points", C.c_uint64), ("num_segments", C.c_uint64),
+                ("num_voxels", C.c_uint64), ("hash_capacity", C.c_uint64),
+                ("max_probe", C.c_uint32), ("key_bits", C.c_uint32 * 3),
+                ("min_coord", C.c_int32 * 3), ("max_coord", C.c_int32 * 3),
+                ("build_ms", C.c_float), ("reserved", C.c_float)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("align_launches", C.c_uint64), ("alignments", C.c_uint64),
+                ("iterations", C.c_uint64), ("point_iterations", C.c_uint64),
+                ("correspondences", C.c_uint64), ("align_kernel_ms", C.c_double),
+                ("score_launches", C.c_uint64), ("score_kernel_ms", C.c_double),
+                ("build_launches", C.c_uint64), ("build_ms", C.c_double),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.CUDA_LIB
+
+
+def load(build_if_missing=True):
+    """Load libndt_gb300.so (built in-tree). Raises if it cannot be built or loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.CUDA_LIB
+    if build_if_missing:
+        _build.build_cuda()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libndt_gb300.so not found at {path}; run __graft_entry__.build()")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    sig = {
+        "ndt_config_default": (C.c_int, [C.POINTER(Config)]),
+        "ndt_ctx_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+        "ndt_ctx_destroy": (C.c_int, [P]),
+        "ndt_ctx_configure": (C.c_int, [P, C.POINTER(Config)]),
+        "ndt_ctx_stream": (C.c_void_p, [P]),
+        "ndt_set_target": (C.c_int, [P, P, C.c_uint64]),
+        "ndt_set_target_device": (C.c_int, [P, P, C.c_uint64]),
+        "ndt_map_info_get": (C.c_int, [P, C.POINTER(MapInfo)]),
+        "ndt_map_voxels": (C.c_int, [P, P, P, P, P, P, C.c_uint64]),
+        "ndt_align": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(Result)]),
+        "ndt_align_multi_pose": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
+        "ndt_align_batch": (C.c_int, [P, P, C.c_uint64, P]),
+        "ndt_align_batch_device": (C.c_int, [P, P, P, P, C.c_uint64, P]),
+        "ndt_eval_batch": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P, P]),
+        "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
+        "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
+        "ndt_stats_reset": (C.c_int, [P]),
+        "ndt_profile_enable": (C.c_int, [P, C.c_int]),
+        "ndt_last_error_string": (C.c_char_p, []),
+        "ndt_radix_sort_pairs_u64_u32": (C.c_int, [P, P, C.c_uint64, C.c_int32, C.c_int32, P,
+                                                   C.POINTER(C.c_uint64), P]),
+        "ndt_detect_segments": (C.c_int, [P, C.c_uint64, P, P, P, P, C.POINTER(C.c_uint64), P]),
+        "ndt_morton_codes": (C.c_int, [P, C.c_uint64, C.c_float, P, P, P, P,
+                                       C.POINTER(C.c_uint64), P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != NDT_OK:
+        msg = _lib.ndt_last_error_string()
+        raise NdtError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def default_config(**overrides):
+    cfg = Config()
+    load().ndt_config_default(C.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def as_xyz(points):
+    a = np.ascontiguousarray(np.asarray(points, dtype=np.float32).reshape(-1, 3))
+    return a
+
+
+def result_dict(r: Result):
+    return {
+        "pose": np.array(r.pose[:], dtype=np.float64),
+        "score": r.score,
+        "transform_probability": r.transform_probability,
+        "nvtl": r.nvtl,
+        "hessian": np.array(r.hessian[:], dtype=np.float64).reshape(6, 6),
+        "converged": bool(r.converged),
+        "iterations": r.iterations,
+        "num_correspondences": r.num_correspondences,
+        "oscillation_count": r.oscillation_count,
+        "status": r.status,
+    }
+
+
+class Context:
+    """Thin owner of an ndt_ctx*: every method is one C-ABI call."""
+
+    def __init__(self, **cfg):
+        self.lib = load()
+        self.cfg = default_config(**cfg)
+        h = C.c_void_p()
+        check(self.lib.ndt_ctx_create(C.byref(self.cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ndt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def configure(self, **overrides):
+        for k, v in overrides.items():
+            setattr(self.cfg, k, v)
+        check(self.lib.ndt_ctx_configure(self.h, C.byref(self.cfg)))
+
+    @property
+    def stream(self):
+        return self.lib.ndt_ctx_stream(self.h)
+
+    def set_target(self, points):
+        p = as_xyz(points)
+        check(self.lib.ndt_set_target(self.h, p.ctypes.data, len(p)))
+
+    def set_target_device(self, ptr, n):
+        check(self.lib.ndt_set_target_device(self.h, ptr, n))
+
+    def map_info(self):
+        mi = MapInfo()
+        check(self.lib.ndt_map_info_get(self.h, C.byref(mi)))
+        return mi
+
+    def map_voxels(self):
+        v = int(self.map_info().num_voxels)
+        coords = np.zeros((v, 3), np.int32)
+        means = np.zeros((v, 3), np.float32)
+        covs = np.zeros((v, 9), np.float32)
+        icovs = np.zeros((v, 9), np.float32)
+        counts = np.zeros(v, np.uint32)
+        check(self.lib.ndt_map_voxels(self.h, coords.ctypes.data, means.ctypes.data,
+                                      covs.ctypes.data, icovs.ctypes.data, counts.ctypes.data,
+                                      v))
+        return coords, means, covs, icovs, counts
+
+    def align(self, points, pose):
+        p = as_xyz(points)
+        pose = np.ascontiguousarray(pose, np.float64)
+        r = Result()
+        check(self.lib.ndt_align(self.h, p.ctypes.data, len(p), pose.ctypes.data, C.byref(r)))
+        return result_dict(r)
+
+    def align_multi_pose(self, points, poses):
+        p = as_xyz(points)
+        poses = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 6))
+        res = (Result * len(poses))()
+        check(self.lib.ndt_align_multi_pose(self.h, p.ctypes.data, len(p), poses.ctypes.data,
+                                            len(poses), res))
+        return [result_dict(r) for r in res]
+
+    def align_batch(self, scans, poses):
+        scans = [as_xyz(s) for s in scans]
+        m = len(scans)
+        arr = (Scan * m)()
+        for i, (s, pose) in enumerate(zip(scans, poses)):
+            arr[i].xyz = s.ctypes.data
+            arr[i].num_points = len(s)
+            for k in range(6):
+                arr[i].initial_pose[k] = float(pose[k])
+        res = (Result * m)()
+        check(self.lib.ndt_align_batch(self.h, arr, m, res))
+        return [result_dict(r) for r in res]
+
+    def align_batch_raw(self, scan_array, results):
+        """Hot-path form: prebuilt (Scan * m) and (Result * m) arrays, no conversion."""
+        check(self.lib.ndt_align_batch(self.h, scan_array, len(scan_array), results))
+
+    def align_batch_device(self, d_xyz, offsets, poses):
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        poses = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 6))
+        m = len(poses)
+        res = (Result * m)()
+        check(self.lib.ndt_align_batch_device(self.h, d_xyz, offsets.ctypes.data,
+                                              poses.ctypes.data, m, res))
+        return [result_dict(r) for r in res]
+
+    def eval_batch(self, points, T34):
+        p = as_xyz(points)
+        T = np.ascontiguousarray(np.asarray(T34, np.float64).reshape(-1, 12))
+        m = len(T)
+        nvtl = np.zeros(m)
+        tp = np.zeros(m)
+        check(self.lib.ndt_eval_batch(self.h, p.ctypes.data, len(p), T.ctypes.data, m,
+                                      nvtl.ctypes.data, tp.ctypes.data))
+        return nvtl, tp
+
+    def neighbors(self, q, max_nb=8):
+        q = as_xyz(q)
+        idx = np.zeros((len(q), max_nb), np.int32)
+        cnt = np.zeros(len(q), np.int32)
+        check(self.lib.ndt_neighbors_query(self.h, q.ctypes.data, len(q), max_nb,
+                                           idx.ctypes.data, cnt.ctypes.data))
+        return idx, cnt
+
+    def stats(self):
+        s = Stats()
+        check(self.lib.ndt_stats_get(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def stats_reset(self):
+        check(self.lib.ndt_stats_reset(self.h))

@@ -1,0 +1,706 @@
+// ndt_api.cu — the C ABI of libndt_gb300.so (declared in include/ndt_gb300.h).
+//
+// A context owns one CUDA stream, the device voxel map, grow-only device buffers and pinned
+// host staging buffers. An alignment call packs the host scans into pinned memory, copies
+// them with one cudaMemcpyAsync, launches the Newton kernel (one cluster per alignment,
+// longest scans first) and the NVTL kernel on the final poses, copies the per-alignment
+// records back and synchronises once.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ndt_internal.h"
+
+namespace ndtgb {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& m) { g_err = m; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return (int)e;
+}
+
+int dev_reserve(DevBuf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.p) return 0;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t nb = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaMalloc(&b.p, nb);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    b.bytes = nb;
+    return 0;
+}
+
+void dev_free(DevBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+int pin_reserve(PinBuf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.p) return 0;
+    if (b.p) cudaFreeHost(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t nb = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaMallocHost(&b.p, nb);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    b.bytes = nb;
+    return 0;
+}
+
+void pin_free(PinBuf& b) {
+    if (b.p) cudaFreeHost(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+static void gauss_params(double res, double outlier, double* d1, double* d2) {
+    // GaussianParams::new (src/ndt_cuda/src/derivatives/types.rs:61-75)
+    double c1 = 10.0 * (1.0 - outlier);
+    double c2 = outlier / (res * res * res);
+    double d3 = -std::log(c2);
+    double g1 = -std::log(c1 + c2) - d3;
+    double nom = -std::log(c1 * std::exp(-0.5) + c2) - d3;
+    *d1 = g1;
+    *d2 = -2.0 * std::log(nom / g1);
+}
+
+}  // namespace ndtgb
+
+using namespace ndtgb;
+
+struct ndt_ctx {
+    ndt_config cfg{};
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    Map map;
+    BuildScratch bs;
+    DevBuf d_in, d_jobs, d_aout, d_sjobs, d_sout, d_part, d_status, d_q, d_qidx, d_qcnt;
+    PinBuf h_pts, h_jobs, h_aout, h_sjobs, h_sout, h_misc;
+    double d1 = 0, d2 = 0;
+    ndt_stats stats{};
+    bool profile = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+};
+
+static int check_status(ndt_ctx* c, uint32_t st) {
+    if (st == 0) return 0;
+    uint32_t zero = 0;
+    cudaMemcpyAsync(c->d_status.p, &zero, 4, cudaMemcpyHostToDevice, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (st & ST_HASH_FULL) {
+        set_error("hash insert found no free slot");
+        return NDT_ERR_HASH_FULL;
+    }
+    if (st & ST_PROBE_LIMIT) {
+        set_error("hash probe exceeded its bound");
+        return NDT_ERR_PROBE_LIMIT;
+    }
+    set_error("device reported status " + std::to_string(st));
+    return NDT_ERR_DEVICE;
+}
+
+extern "C" {
+
+const char* ndt_last_error_string(void) { return g_err.c_str(); }
+
+int ndt_config_default(ndt_config* cfg) {
+    if (!cfg) return NDT_ERR_INVALID_ARGUMENT;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->resolution = 2.0f;
+    cfg->max_iterations = 30;
+    cfg->trans_epsilon = 0.01;
+    cfg->step_size = 0.1;
+    cfg->outlier_ratio = 0.55;
+    cfg->min_points_per_voxel = 6;
+    cfg->eigenvalue_ratio = 0.01f;
+    cfg->max_neighbors = MAX_NB_GPU;
+    cfg->semantics = NDT_SEMANTICS_GPU_GRAPH;
+    cfg->min_correspondences = 10;
+    cfg->device = 0;
+    cfg->cluster_size = 0;
+    cfg->threads_per_cta = 0;
+    cfg->hash_capacity_factor = 2;
+    return NDT_OK;
+}
+
+int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
+    if (!out) return NDT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    ndt_config c;
+    if (cfg)
+        c = *cfg;
+    else
+        ndt_config_default(&c);
+    if (!(c.resolution > 0.f) || c.max_iterations < 1 || c.max_neighbors < 1 ||
+        c.max_neighbors > MAX_NB_ALL || !(c.step_size > 0.0) || !(c.outlier_ratio > 0.0) ||
+        !(c.outlier_ratio < 1.0)) {
+        set_error("invalid configuration");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= c.device) {
+        set_error("no CUDA device available");
+        return NDT_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, c.device)) != cudaSuccess) return cuda_fail(e, "device");
+    if (!(prop.major == 10 && prop.minor == 3)) {
+        set_error("libndt_gb300 is built for sm_103a; device " + std::string(prop.name) +
+                  " has compute capability " + std::to_string(prop.major) + "." +
+                  std::to_string(prop.minor));
+        return NDT_ERR_NO_DEVICE;
+    }
+    if ((e = cudaSetDevice(c.device)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    ndt_ctx* x = new ndt_ctx();
+    x->cfg = c;
+    x->device = c.device;
+    x->num_sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete x;
+        return cuda_fail(e, "stream");
+    }
+    cudaEventCreate(&x->ev0);
+    cudaEventCreate(&x->ev1);
+    cudaEventCreate(&x->ev2);
+    cudaEventCreate(&x->ev3);
+    int rc = dev_reserve(x->d_status, 16);
+    if (rc) {
+        delete x;
+        return rc;
+    }
+    cudaMemsetAsync(x->d_status.p, 0, 16, x->stream);
+    gauss_params((double)c.resolution, c.outlier_ratio, &x->d1, &x->d2);
+    *out = x;
+    return NDT_OK;
+}
+
+int ndt_ctx_destroy(ndt_ctx* c) {
+    if (!c) return NDT_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (DevBuf* b : {&c->map.slots, &c->map.slot_icov, &c->map.slot_vidx, &c->map.vox_coord,
+                      &c->map.vox_mean, &c->map.vox_cov, &c->map.vox_icov, &c->map.vox_count,
+                      &c->bs.keys_a, &c->bs.keys_b, &c->bs.vals_a, &c->bs.vals_b, &c->bs.tmp,
+                      &c->bs.seg_ids, &c->bs.seg_starts, &c->bs.seg_valid, &c->bs.seg_rank,
+                      &c->bs.seg_rec, &c->bs.small, &c->d_in, &c->d_jobs, &c->d_aout,
+                      &c->d_sjobs, &c->d_sout, &c->d_part, &c->d_status, &c->d_q, &c->d_qidx,
+                      &c->d_qcnt})
+        dev_free(*b);
+    for (PinBuf* b : {&c->h_pts, &c->h_jobs, &c->h_aout, &c->h_sjobs, &c->h_sout, &c->h_misc})
+        pin_free(*b);
+    for (cudaEvent_t ev : {c->ev0, c->ev1, c->ev2, c->ev3})
+        if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return NDT_OK;
+}
+
+void* ndt_ctx_stream(ndt_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int ndt_ctx_configure(ndt_ctx* c, const ndt_config* cfg) {
+    if (!c || !cfg) return NDT_ERR_INVALID_ARGUMENT;
+    const ndt_config& n = *cfg;
+    if (!(n.resolution > 0.f) || n.max_iterations < 1 || n.max_neighbors < 1 ||
+        n.max_neighbors > MAX_NB_ALL || !(n.step_size > 0.0) || !(n.outlier_ratio > 0.0) ||
+        !(n.outlier_ratio < 1.0) || n.device != c->cfg.device ||
+        (n.semantics != NDT_SEMANTICS_GPU_GRAPH && n.semantics != NDT_SEMANTICS_CPU)) {
+        set_error("invalid configuration");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    if (c->map.valid && n.resolution != c->map.view.res) {
+        set_error("resolution changes need a new set_target");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    c->cfg = n;
+    gauss_params((double)n.resolution, n.outlier_ratio, &c->d1, &c->d2);
+    return NDT_OK;
+}
+
+int ndt_profile_enable(ndt_ctx* c, int enable) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    c->profile = enable != 0;
+    return NDT_OK;
+}
+
+int ndt_stats_get(ndt_ctx* c, ndt_stats* out) {
+    if (!c || !out) return NDT_ERR_INVALID_ARGUMENT;
+    *out = c->stats;
+    return NDT_OK;
+}
+
+int ndt_stats_reset(ndt_ctx* c) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    std::memset(&c->stats, 0, sizeof c->stats);
+    return NDT_OK;
+}
+
+static int set_target_dev(ndt_ctx* c, const float* d_xyz, uint64_t n) {
+    c->map.valid = false;
+    float ms = 0.f;
+    int rc = build_map(c->map, c->bs, d_xyz, (size_t)n, c->cfg, (uint32_t*)c->d_status.p,
+                       c->stream, &ms);
+    if (rc) return rc;
+    uint32_t st = 0;
+    cudaMemcpyAsync(&st, c->d_status.p, 4, cudaMemcpyDeviceToHost, c->stream);
+    if ((rc = cuda_fail(cudaStreamSynchronize(c->stream), "set_target"))) return rc;
+    if ((rc = check_status(c, st))) {
+        c->map.valid = false;
+        return rc;
+    }
+    c->stats.build_launches++;
+    c->stats.build_ms += ms;
+    return NDT_OK;
+}
+
+int ndt_set_target(ndt_ctx* c, const float* xyz, uint64_t n) {
+    if (!c || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    if (n == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    cudaSetDevice(c->device);
+    int rc = dev_reserve(c->d_in, n * 12);
+    if (rc) return rc;
+    rc = cuda_fail(cudaMemcpyAsync(c->d_in.p, xyz, n * 12, cudaMemcpyHostToDevice, c->stream),
+                   "target upload");
+    if (rc) return rc;
+    c->stats.h2d_bytes += n * 12;
+    return set_target_dev(c, (const float*)c->d_in.p, n);
+}
+
+int ndt_set_target_device(ndt_ctx* c, const float* d_xyz, uint64_t n) {
+    if (!c || (!d_xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    if (n == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    cudaSetDevice(c->device);
+    return set_target_dev(c, d_xyz, n);
+}
+
+int ndt_map_info_get(ndt_ctx* c, ndt_map_info* out) {
+    if (!c || !out) return NDT_ERR_INVALID_ARGUMENT;
+    if (!c->map.valid) {
+        set_error("No target set. Call set_target() first.");
+        return NDT_ERR_NO_TARGET;
+    }
+    *out = c->map.info;
+    return NDT_OK;
+}
+
+int ndt_map_voxels(ndt_ctx* c, int32_t* coords, float* means, float* covs, float* icovs,
+                   uint32_t* counts, uint64_t capacity) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    if (!c->map.valid) {
+        set_error("No target set. Call set_target() first.");
+        return NDT_ERR_NO_TARGET;
+    }
+    uint64_t V = c->map.info.num_voxels;
+    if (capacity < V) {
+        set_error("output capacity below the number of voxels");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    if (coords) cudaMemcpyAsync(coords, c->map.vox_coord.p, V * 12, cudaMemcpyDeviceToHost, s);
+    if (covs) cudaMemcpyAsync(covs, c->map.vox_cov.p, V * 36, cudaMemcpyDeviceToHost, s);
+    if (icovs) cudaMemcpyAsync(icovs, c->map.vox_icov.p, V * 36, cudaMemcpyDeviceToHost, s);
+    if (counts) cudaMemcpyAsync(counts, c->map.vox_count.p, V * 4, cudaMemcpyDeviceToHost, s);
+    std::vector<float> m4;
+    if (means) {
+        m4.resize(V * 4);
+        cudaMemcpyAsync(m4.data(), c->map.vox_mean.p, V * 16, cudaMemcpyDeviceToHost, s);
+    }
+    int rc = cuda_fail(cudaStreamSynchronize(s), "map readback");
+    if (rc) return rc;
+    if (means)
+        for (uint64_t v = 0; v < V; ++v) {
+            means[3 * v] = m4[4 * v];
+            means[3 * v + 1] = m4[4 * v + 1];
+            means[3 * v + 2] = m4[4 * v + 2];
+        }
+    return NDT_OK;
+}
+
+}  // extern "C"
+
+// Launch shape: enough CTAs to fill the GPU twice over, at least ~1k points per CTA.
+static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
+    LaunchShape sh;
+    sh.threads = c->cfg.threads_per_cta > 0 ? c->cfg.threads_per_cta : 256;
+    if (c->cfg.cluster_size > 0) {
+        sh.cluster = c->cfg.cluster_size;
+        return sh;
+    }
+    int K = 1;
+    while (K < 8 && (uint64_t)jobs * K < 2ull * (uint64_t)c->num_sms &&
+           max_n / (uint32_t)(2 * K) >= (uint32_t)sh.threads * 4)
+        K *= 2;
+    sh.cluster = K;
+    return sh;
+}
+
+// Core: align jobs whose points are already at d_pts (device, concatenated).
+static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
+                     const std::vector<uint64_t>& n_by_slot, ndt_result* out) {
+    uint32_t nj = (uint32_t)jobs.size();
+    if (nj == 0) return NDT_OK;
+    std::stable_sort(jobs.begin(), jobs.end(),
+                     [](const AlignJob& a, const AlignJob& b) { return a.n > b.n; });
+    uint32_t max_n = jobs.front().n;
+    int rc;
+    size_t jb = nj * sizeof(AlignJob), ob = nj * sizeof(AlignOut), sjb = nj * sizeof(ScoreJob),
+           sob = nj * sizeof(ScoreOut);
+    if ((rc = dev_reserve(c->d_jobs, jb)) || (rc = dev_reserve(c->d_aout, ob)) ||
+        (rc = dev_reserve(c->d_sjobs, sjb)) || (rc = dev_reserve(c->d_sout, sob)) ||
+        (rc = dev_reserve(c->d_part, score_part_bytes(nj, max_n))) ||
+        (rc = pin_reserve(c->h_jobs, jb + sjb)) || (rc = pin_reserve(c->h_aout, ob + sob + 16)))
+        return rc;
+    AlignJob* hj = (AlignJob*)c->h_jobs.p;
+    ScoreJob* hs = (ScoreJob*)((char*)c->h_jobs.p + jb);
+    for (uint32_t j = 0; j < nj; ++j) {
+        hj[j] = jobs[j];
+        ScoreJob s{};
+        s.offset = jobs[j].offset;
+        s.n = jobs[j].n;
+        s.pose_src = 1;
+        s.out_index = j;
+        hs[j] = s;
+    }
+    cudaStream_t st = c->stream;
+    cudaMemcpyAsync(c->d_jobs.p, hj, jb + 0, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
+    c->stats.h2d_bytes += jb + sjb;
+    AlignParams p{};
+    p.map = c->map.view;
+    p.pts = d_pts;
+    p.jobs = (const AlignJob*)c->d_jobs.p;
+    p.out = (AlignOut*)c->d_aout.p;
+    p.num_jobs = nj;
+    p.max_iter = c->cfg.max_iterations;
+    bool cpu = c->cfg.semantics == NDT_SEMANTICS_CPU;
+    p.semantics = c->cfg.semantics;
+    p.max_nb = cpu ? MAX_NB_ALL : c->cfg.max_neighbors;
+    p.min_corr = c->cfg.min_correspondences;
+    p.d1 = c->d1;
+    p.d2 = c->d2;
+    p.d1f = (float)c->d1;
+    p.d2f = (float)c->d2;
+    p.step_size = c->cfg.step_size;
+    if (cpu) {
+        p.eps = c->cfg.trans_epsilon;
+    } else {  // K5: step_len < sqrtf(epsilon_sq), epsilon_sq = (f32 eps)^2
+        float ef = (float)c->cfg.trans_epsilon;
+        p.eps = (double)sqrtf(ef * ef);
+    }
+    p.status = (uint32_t*)c->d_status.p;
+    LaunchShape shape = choose_shape(c, nj, max_n);
+    cudaEventRecord(c->ev0, st);
+    if ((rc = launch_align(p, shape, st))) return rc;
+    cudaEventRecord(c->ev1, st);
+    if ((rc = launch_score(c->map.view, d_pts, (const ScoreJob*)c->d_sjobs.p, nj, max_n,
+                           (const AlignOut*)c->d_aout.p, c->d_part.p, (ScoreOut*)c->d_sout.p,
+                           (float)c->d1, (float)c->d2, st)))
+        return rc;
+    cudaEventRecord(c->ev2, st);
+    AlignOut* ho = (AlignOut*)c->h_aout.p;
+    ScoreOut* hso = (ScoreOut*)((char*)c->h_aout.p + ob);
+    uint32_t* hst = (uint32_t*)((char*)c->h_aout.p + ob + sob);
+    cudaMemcpyAsync(ho, c->d_aout.p, ob, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hso, c->d_sout.p, sob, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hst, c->d_status.p, 4, cudaMemcpyDeviceToHost, st);
+    c->stats.d2h_bytes += ob + sob + 4;
+    if ((rc = cuda_fail(cudaStreamSynchronize(st), "align"))) return rc;
+    if ((rc = check_status(c, *hst))) return rc;
+    float ams = 0.f, sms = 0.f;
+    cudaEventElapsedTime(&ams, c->ev0, c->ev1);
+    cudaEventElapsedTime(&sms, c->ev1, c->ev2);
+    c->stats.align_launches++;
+    c->stats.align_kernel_ms += ams;
+    c->stats.score_launches++;
+    c->stats.score_kernel_ms += sms;
+    for (uint32_t j = 0; j < nj; ++j) {
+        const AlignOut& o = ho[j];
+        const ScoreOut& so = hso[j];
+        ndt_result& r = out[jobs[j].slot];
+        std::memset(&r, 0, sizeof r);
+        for (int i = 0; i < 6; ++i) r.pose[i] = o.pose[i];
+        r.score = o.score;
+        for (int i = 0; i < 36; ++i) r.hessian[i] = o.hessian[i];
+        r.converged = o.converged;
+        r.iterations = o.iterations;
+        r.num_correspondences = o.ncorr;
+        r.oscillation_count = o.osc;
+        r.status = o.status;
+        uint64_t nsrc = n_by_slot[jobs[j].slot];
+        bool nocorr_early = cpu && o.status == NDT_STATUS_NO_CORRESPONDENCES;
+        r.transform_probability = (nsrc && !nocorr_early) ? o.score / (double)nsrc : 0.0;
+        r.nvtl = (!nocorr_early && so.nvtl_count) ? so.nvtl_sum / (double)so.nvtl_count : 0.0;
+        c->stats.alignments++;
+        c->stats.iterations += (uint64_t)std::max(o.iterations, 0);
+        c->stats.point_iterations += o.point_iters;
+        c->stats.correspondences += o.corr_total;
+    }
+    return NDT_OK;
+}
+
+static int need_target(ndt_ctx* c) {
+    if (!c->map.valid) {
+        set_error("No target set. Call set_target() first.");
+        return NDT_ERR_NO_TARGET;
+    }
+    return 0;
+}
+
+extern "C" {
+
+int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* out) {
+    if (!c || (!scans && m) || (!out && m)) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (m == 0) return NDT_OK;
+    if (m > 0xFFFFFFull) {
+        set_error("too many scans in one batch");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    uint64_t total = 0;
+    for (uint64_t i = 0; i < m; ++i) {
+        if (scans[i].num_points && !scans[i].xyz) return NDT_ERR_INVALID_ARGUMENT;
+        if (scans[i].num_points > 0xFFFFFFF0ull) {
+            set_error("scan exceeds 2^32 points");
+            return NDT_ERR_CAPACITY;
+        }
+        total += scans[i].num_points;
+    }
+    if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
+        return rc;
+    std::vector<AlignJob> jobs(m);
+    std::vector<uint64_t> ns(m);
+    uint64_t off = 0;
+    char* hp = (char*)c->h_pts.p;
+    for (uint64_t i = 0; i < m; ++i) {
+        std::memcpy(hp + off * 12, scans[i].xyz, scans[i].num_points * 12);
+        jobs[i].offset = off;
+        jobs[i].n = (uint32_t)scans[i].num_points;
+        jobs[i].slot = (uint32_t)i;
+        for (int k = 0; k < 6; ++k) jobs[i].pose[k] = scans[i].initial_pose[k];
+        ns[i] = scans[i].num_points;
+        off += scans[i].num_points;
+    }
+    if (total)
+        cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
+    c->stats.h2d_bytes += total * 12;
+    return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
+}
+
+int ndt_align(ndt_ctx* c, const float* xyz, uint64_t n, const double pose_in[6], ndt_result* out) {
+    if (!c || !pose_in || !out || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (n == 0) {
+        set_error("Source point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    ndt_scan s;
+    s.xyz = xyz;
+    s.num_points = n;
+    for (int k = 0; k < 6; ++k) s.initial_pose[k] = pose_in[k];
+    return ndt_align_batch(c, &s, 1, out);
+}
+
+int ndt_align_multi_pose(ndt_ctx* c, const float* xyz, uint64_t n, const double* poses,
+                         uint64_t m, ndt_result* out) {
+    if (!c || (!poses && m) || (!out && m) || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (n == 0) {
+        set_error("Source point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    if (m == 0) return NDT_OK;
+    if (n > 0xFFFFFFF0ull || m > 0xFFFFFFull) {
+        set_error("scan or pose count too large");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    if ((rc = pin_reserve(c->h_pts, n * 12)) || (rc = dev_reserve(c->d_in, n * 12))) return rc;
+    std::memcpy(c->h_pts.p, xyz, n * 12);
+    cudaMemcpyAsync(c->d_in.p, c->h_pts.p, n * 12, cudaMemcpyHostToDevice, c->stream);
+    c->stats.h2d_bytes += n * 12;
+    std::vector<AlignJob> jobs(m);
+    std::vector<uint64_t> ns(m, n);
+    for (uint64_t i = 0; i < m; ++i) {
+        jobs[i].offset = 0;
+        jobs[i].n = (uint32_t)n;
+        jobs[i].slot = (uint32_t)i;
+        for (int k = 0; k < 6; ++k) jobs[i].pose[k] = poses[6 * i + k];
+    }
+    return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
+}
+
+int ndt_align_batch_device(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets,
+                           const double* poses, uint64_t m, ndt_result* out) {
+    if (!c || (m && (!d_xyz || !offsets || !poses || !out))) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (m == 0) return NDT_OK;
+    if (m > 0xFFFFFFull) {
+        set_error("too many scans in one batch");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    std::vector<AlignJob> jobs(m);
+    std::vector<uint64_t> ns(m);
+    for (uint64_t i = 0; i < m; ++i) {
+        if (offsets[i + 1] < offsets[i] || offsets[i + 1] - offsets[i] > 0xFFFFFFF0ull)
+            return NDT_ERR_INVALID_ARGUMENT;
+        jobs[i].offset = offsets[i];
+        jobs[i].n = (uint32_t)(offsets[i + 1] - offsets[i]);
+        jobs[i].slot = (uint32_t)i;
+        for (int k = 0; k < 6; ++k) jobs[i].pose[k] = poses[6 * i + k];
+        ns[i] = jobs[i].n;
+    }
+    return run_align(c, d_xyz, jobs, ns, out);
+}
+
+int ndt_eval_batch(ndt_ctx* c, const float* xyz, uint64_t n, const double* T34, uint64_t m,
+                   double* nvtl, double* tp) {
+    if (!c || (!T34 && m) || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (m == 0) return NDT_OK;
+    if (n > 0xFFFFFFF0ull || m > 0xFFFFFFull) {
+        set_error("scan or pose count too large");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    size_t sjb = m * sizeof(ScoreJob), sob = m * sizeof(ScoreOut);
+    if ((rc = pin_reserve(c->h_pts, n * 12 + 16)) || (rc = dev_reserve(c->d_in, n * 12 + 16)) ||
+        (rc = dev_reserve(c->d_sjobs, sjb)) || (rc = dev_reserve(c->d_sout, sob)) ||
+        (rc = dev_reserve(c->d_part, score_part_bytes((uint32_t)m, (uint32_t)n))) ||
+        (rc = pin_reserve(c->h_sjobs, sjb)) || (rc = pin_reserve(c->h_sout, sob)))
+        return rc;
+    if (n) std::memcpy(c->h_pts.p, xyz, n * 12);
+    ScoreJob* hs = (ScoreJob*)c->h_sjobs.p;
+    for (uint64_t j = 0; j < m; ++j) {
+        ScoreJob s{};
+        s.offset = 0;
+        s.n = (uint32_t)n;
+        s.pose_src = 0;
+        s.out_index = (uint32_t)j;
+        for (int k = 0; k < 12; ++k) s.T[k] = T34[12 * j + k];
+        hs[j] = s;
+    }
+    cudaStream_t st = c->stream;
+    if (n) cudaMemcpyAsync(c->d_in.p, c->h_pts.p, n * 12, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
+    cudaEventRecord(c->ev0, st);
+    if ((rc = launch_score(c->map.view, (const float*)c->d_in.p, (const ScoreJob*)c->d_sjobs.p,
+                           (uint32_t)m, (uint32_t)n, nullptr, c->d_part.p, (ScoreOut*)c->d_sout.p,
+                           (float)c->d1, (float)c->d2, st)))
+        return rc;
+    cudaEventRecord(c->ev1, st);
+    cudaMemcpyAsync(c->h_sout.p, c->d_sout.p, sob, cudaMemcpyDeviceToHost, st);
+    if ((rc = cuda_fail(cudaStreamSynchronize(st), "eval"))) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.score_launches++;
+    c->stats.score_kernel_ms += ms;
+    c->stats.h2d_bytes += n * 12 + sjb;
+    c->stats.d2h_bytes += sob;
+    const ScoreOut* so = (const ScoreOut*)c->h_sout.p;
+    for (uint64_t j = 0; j < m; ++j) {
+        if (nvtl) nvtl[j] = so[j].nvtl_count ? so[j].nvtl_sum / (double)so[j].nvtl_count : 0.0;
+        if (tp) tp[j] = so[j].ncorr ? so[j].score_sum / (double)so[j].ncorr : 0.0;
+    }
+    return NDT_OK;
+}
+
+int ndt_neighbors_query(ndt_ctx* c, const float* xyz, uint64_t n, int32_t max_nb, int32_t* idx,
+                        int32_t* counts) {
+    if (!c || (n && (!xyz || !idx || !counts)) || max_nb < 1 || max_nb > MAX_NB_ALL)
+        return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (n == 0) return NDT_OK;
+    cudaSetDevice(c->device);
+    if ((rc = dev_reserve(c->d_q, n * 12)) || (rc = dev_reserve(c->d_qidx, n * 4 * max_nb)) ||
+        (rc = dev_reserve(c->d_qcnt, n * 4)))
+        return rc;
+    cudaStream_t st = c->stream;
+    cudaMemcpyAsync(c->d_q.p, xyz, n * 12, cudaMemcpyHostToDevice, st);
+    if ((rc = launch_query(c->map.view, (const float*)c->d_q.p, n, max_nb, (int32_t*)c->d_qidx.p,
+                           (int32_t*)c->d_qcnt.p, st)))
+        return rc;
+    cudaMemcpyAsync(idx, c->d_qidx.p, n * 4 * max_nb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(counts, c->d_qcnt.p, n * 4, cudaMemcpyDeviceToHost, st);
+    return cuda_fail(cudaStreamSynchronize(st), "neighbour query");
+}
+
+int ndt_radix_sort_pairs_u64_u32(uint64_t* d_keys, uint32_t* d_values, uint64_t n,
+                                 int32_t begin_bit, int32_t end_bit, void* d_temp,
+                                 uint64_t* temp_bytes, void* stream) {
+    if (!temp_bytes || begin_bit < 0 || end_bit > 64 || begin_bit > end_bit)
+        return NDT_ERR_INVALID_ARGUMENT;
+    size_t need = radix_sort_temp_bytes((size_t)n);
+    if (!d_temp) {
+        *temp_bytes = need;
+        return NDT_OK;
+    }
+    if (*temp_bytes < need || (n && (!d_keys || !d_values))) return NDT_ERR_INVALID_ARGUMENT;
+    return radix_sort_pairs(d_keys, d_values, (size_t)n, begin_bit, end_bit, d_temp,
+                            (size_t)*temp_bytes, (cudaStream_t)stream);
+}
+
+int ndt_detect_segments(const uint64_t* d_sorted, uint64_t n, uint32_t* d_segment_ids,
+                        uint32_t* d_segment_starts, uint32_t* d_num_segments, void* d_temp,
+                        uint64_t* temp_bytes, void* stream) {
+    if (!temp_bytes) return NDT_ERR_INVALID_ARGUMENT;
+    size_t need = detect_segments_temp_bytes((size_t)n);
+    if (!d_temp) {
+        *temp_bytes = need;
+        return NDT_OK;
+    }
+    if (*temp_bytes < need || !d_num_segments || (n && (!d_sorted || !d_segment_starts)))
+        return NDT_ERR_INVALID_ARGUMENT;
+    return detect_segments(d_sorted, (size_t)n, d_segment_ids, d_segment_starts, d_num_segments,
+                           d_temp, (size_t)*temp_bytes, (cudaStream_t)stream);
+}
+
+int ndt_morton_codes(const float* d_xyz, uint64_t n, float res, uint64_t* d_codes,
+                     uint32_t* d_indices, int32_t* d_min_cell, void* d_temp,
+                     uint64_t* temp_bytes, void* stream) {
+    if (!temp_bytes || !(res > 0.f)) return NDT_ERR_INVALID_ARGUMENT;
+    if (!d_temp) {
+        *temp_bytes = 256;
+        return NDT_OK;
+    }
+    if (*temp_bytes < 256 || (n && (!d_xyz || !d_codes || !d_indices)))
+        return NDT_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = morton_codes(d_xyz, (size_t)n, res, d_codes, d_indices, (int32_t*)d_temp, s);
+    if (rc) return rc;
+    if (d_min_cell)
+        cudaMemcpyAsync(d_min_cell, d_temp, 12, cudaMemcpyDeviceToDevice, s);
+    return cuda_fail(cudaGetLastError(), "morton codes");
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// ndt_common.cuh — device-side definitions shared by the NDT kernels (sm_103a).
+//
+// Voxel map layout in HBM (built by voxel_build.cu, read by ndt_align.cu / ndt_score.cu):
+//   slots[cap]      uint4 {key32, mean.x, mean.y, mean.z}: open-addressing hash, 16 B per
+//                   slot, key32 = EMPTY_KEY when free. The home slot is the reference's
+//                   MurmurHash3 finaliser of the reference's 21-bit-per-axis packed cell key
+//                   (src/cuda_ffi/csrc/voxel_hash.cu:33-58), masked by the power-of-two
+//                   capacity; the stored key is the cell relative to the map's minimum cell
+//                   (key_bits per axis, <= 31 bits in total), so one 16-byte load both tests
+//                   the key and yields the centroid for the radius check.
+//   slot_icov[cap]  2 x float4 {c00, c01, c02, c11}, {c12, c22, 0, 0}: inverse covariance of
+//                   the voxel in that slot (one 32-byte sector per accepted neighbour).
+//   slot_vidx[cap]  int32 voxel index (ascending coordinate-Morton order), for the query API.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ndtgb {
+
+constexpr uint32_t EMPTY_KEY = 0xFFFFFFFFu;
+constexpr int MAX_NB_GPU = 8;    // graph-kernel truncation (ndt_graph_common.cuh:21)
+constexpr int MAX_NB_ALL = 27;   // one voxel per cell at most
+
+// status word bits written by kernels (atomicOr), mapped to NDT_ERR_* on the host
+constexpr uint32_t ST_HASH_FULL = 1u << 0;
+constexpr uint32_t ST_PROBE_LIMIT = 1u << 1;
+constexpr uint32_t ST_BAD_INPUT = 1u << 2;
+
+struct MapView {
+    const uint4* slots;
+    const float4* slot_icov;
+    const int32_t* slot_vidx;
+    uint32_t mask;        // capacity - 1
+    uint32_t max_probe;   // longest insert displacement; queries scan max_probe + 1 slots
+    int32_t min_cell[3];
+    uint32_t bits[3];     // local key bits per axis
+    float res;
+    float inv_res;        // 1.0f / res, as the reference query computes it
+    float r2;             // res * res (f32)
+    uint32_t num_voxels;
+};
+
+// Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).
+__host__ __device__ __forceinline__ uint64_t pack21(int32_t gx, int32_t gy, int32_t gz) {
+    uint64_t ux = (uint64_t)(int64_t)(gx + (1 << 20));
+    uint64_t uy = (uint64_t)(int64_t)(gy + (1 << 20));
+    uint64_t uz = (uint64_t)(int64_t)(gz + (1 << 20));
+    return (ux << 42) | (uy << 21) | uz;
+}
+
+__host__ __device__ __forceinline__ uint64_t fmix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// local key of a cell, or EMPTY_KEY when the cell lies outside the map's bounding box
+__device__ __forceinline__ uint32_t local_key(const MapView& m, int32_t gx, int32_t gy,
+                                              int32_t gz) {
+    uint32_t lx = (uint32_t)(gx - m.min_cell[0]);
+    uint32_t ly = (uint32_t)(gy - m.min_cell[1]);
+    uint32_t lz = (uint32_t)(gz - m.min_cell[2]);
+    if ((lx >> m.bits[0]) | (ly >> m.bits[1]) | (lz >> m.bits[2])) return EMPTY_KEY;
+    return lx | (ly << m.bits[0]) | (lz << (m.bits[0] + m.bits[1]));
+}
+
+// Bounded linear probe: returns the slot holding `key` or -1. The bound max_probe + 1 is
+// exact (no stored key sits further than max_probe from its home), so the loop both matches
+// "probe to empty or match" and cannot spin.
+__device__ __forceinline__ int32_t probe(const MapView& m, uint32_t key, uint32_t home,
+                                         uint4* out) {
+    uint32_t s = home;
+    for (uint32_t j = 0; j <= m.max_probe; ++j) {
+        uint4 v = __ldg(m.slots + s);
+        if (v.x == key) {
+            *out = v;
+            return (int32_t)s;
+        }
+        if (v.x == EMPTY_KEY) return -1;
+        s = (s + 1) & m.mask;
+    }
+    return -1;
+}
+
+// Offsets in the reference's fixed order (ndt_graph_kernels.cu:29-39): dx outer, dz inner.
+__host__ __device__ __forceinline__ void offset27(int n, int& dx, int& dy, int& dz) {
+    dx = n / 9 - 1;
+    dy = (n / 3) % 3 - 1;
+    dz = n % 3 - 1;
+}
+
+// Morton spreading (src/ndt_cuda/src/voxel_grid/gpu/morton.rs:284-305)
+__host__ __device__ __forceinline__ uint64_t spread21(uint64_t v) {
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+__host__ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return (spread21(x) << 2) | (spread21(y) << 1) | spread21(z);
+}
+
+__device__ __forceinline__ float dist2_rn(float ax, float ay, float az, float bx, float by,
+                                          float bz) {
+    // unfused, left to right: the reference's f32 expression dx*dx + dy*dy + dz*dz
+    float ex = __fsub_rn(ax, bx), ey = __fsub_rn(ay, by), ez = __fsub_rn(az, bz);
+    float d = __fmul_rn(ex, ex);
+    d = __fadd_rn(d, __fmul_rn(ey, ey));
+    d = __fadd_rn(d, __fmul_rn(ez, ez));
+    return d;
+}
+
+// f32 -> int32 with Rust `as i32` semantics (saturating, NaN -> 0)
+__device__ __forceinline__ int32_t sat_i32(float v) {
+    if (v != v) return 0;
+    if (v >= 2147483648.0f) return INT32_MAX;
+    if (v < -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+
+}  // namespace ndtgb

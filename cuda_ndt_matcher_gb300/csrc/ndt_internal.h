@@ -1,0 +1,131 @@
+// ndt_internal.h — host-side structures shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ndt_common.cuh"
+#include "ndt_gb300.h"
+
+namespace ndtgb {
+
+// Grow-only device allocation owned by a context.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+int dev_reserve(DevBuf& b, size_t bytes);
+void dev_free(DevBuf& b);
+
+struct PinBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+int pin_reserve(PinBuf& b, size_t bytes);
+void pin_free(PinBuf& b);
+
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+// Device-resident voxel map.
+struct Map {
+    DevBuf slots, slot_icov, slot_vidx;
+    DevBuf vox_coord, vox_mean, vox_cov, vox_icov, vox_count;
+    MapView view{};
+    ndt_map_info info{};
+    bool valid = false;
+};
+
+// Scratch used while building a map (kept for the next rebuild).
+struct BuildScratch {
+    DevBuf keys_a, keys_b, vals_a, vals_b, tmp;
+    DevBuf seg_ids, seg_starts, seg_valid, seg_rank, seg_rec, small;
+};
+
+// Temporary-storage sizing of the sort / scan primitives (two-phase convention).
+size_t radix_sort_temp_bytes(size_t n);
+size_t scan_temp_bytes(size_t n);
+int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
+                     void* temp, size_t temp_bytes, cudaStream_t s);
+int detect_segments(const uint64_t* sorted, size_t n, uint32_t* seg_ids, uint32_t* seg_starts,
+                    uint32_t* num_segments, void* temp, size_t temp_bytes, cudaStream_t s);
+size_t detect_segments_temp_bytes(size_t n);
+int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_t* idx,
+                 int32_t* d_minmax /* 6 ints + count */, cudaStream_t s);
+
+int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+              uint32_t* d_status, cudaStream_t s, float* build_ms);
+
+// One alignment job of a launch.
+struct AlignJob {
+    uint64_t offset;   // first point (index into the concatenated xyz array)
+    uint32_t n;        // points
+    uint32_t slot;     // index of the caller's result
+    double pose[6];    // initial pose
+};
+
+struct AlignOut {
+    double pose[6];
+    double score;
+    double hessian[36];
+    int32_t iterations;
+    int32_t converged;
+    int32_t ncorr;
+    int32_t osc;
+    int32_t status;
+    int32_t pad;
+    uint64_t point_iters;
+    uint64_t corr_total;
+};
+
+struct AlignParams {
+    MapView map;
+    const float* pts;
+    const AlignJob* jobs;
+    AlignOut* out;
+    uint32_t num_jobs;
+    int32_t max_iter;
+    int32_t max_nb;
+    int32_t semantics;
+    int32_t min_corr;
+    int32_t cluster;
+    float d1f, d2f;
+    double d1, d2;
+    double step_size;
+    double eps;
+    uint32_t* status;
+};
+
+struct LaunchShape {
+    int cluster;
+    int threads;
+};
+
+int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s);
+
+// Per-pose scoring (NVTL + score/correspondences over all neighbours within one resolution).
+struct ScoreJob {
+    uint64_t offset;
+    uint32_t n;
+    uint32_t pose_src;   // 0: T34 given; 1: take pose from AlignOut[pose_index] (zyx quirk)
+    uint32_t out_index;
+    uint32_t pad;
+    double T[12];
+};
+struct ScoreOut {
+    double nvtl_sum;
+    double score_sum;
+    uint64_t nvtl_count;
+    uint64_t ncorr;
+};
+size_t score_part_bytes(uint32_t num_jobs, uint32_t max_n);
+int launch_score(const MapView& map, const float* pts, const ScoreJob* jobs, uint32_t num_jobs,
+                 uint32_t max_n, const AlignOut* align_out, void* part, ScoreOut* out, float d1,
+                 float d2, cudaStream_t s);
+int launch_query(const MapView& map, const float* q, size_t n, int max_nb, int32_t* idx,
+                 int32_t* cnt, cudaStream_t s);
+
+}  // namespace ndtgb

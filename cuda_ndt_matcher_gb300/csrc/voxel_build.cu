@@ -1,0 +1,725 @@
+// voxel_build.cu — GPU voxel-map build for sm_103a (the `set_target` hot path).
+//
+// Pipeline (one CUDA stream, no host work between kernels except the two size reads that
+// size the allocations):
+//   1. cells + bounds      : cell = floor(p / res) per finite point (f32 IEEE division, the
+//                            membership rule of VoxelCoord::from_point,
+//                            src/ndt_cuda/src/voxel_grid/types.rs:206-212); min/max cell.
+//   2. Morton keys         : key = morton(cell - min cell), 21 bits per axis
+//                            (src/ndt_cuda/src/voxel_grid/gpu/morton.rs:45-95 layout); the
+//                            non-finite points get key ~0 and sort last.
+//   3. LSD radix sort      : stable, 8-bit digits, only the significant key bits
+//                            (replaces cub::DeviceRadixSort, src/cuda_ffi/csrc/radix_sort.cu).
+//   4. segments            : boundary flags + exclusive scan -> segment id / start
+//                            (src/cuda_ffi/csrc/segment_detect.cu:27-146).
+//   5. voxel statistics    : one thread per segment, FP64 two-pass centred moments over the
+//                            segment's points in input order, cyclic-Jacobi eigen
+//                            regularisation to the min-ratio, FP64 inverse, f32 outputs
+//                            (Voxel::from_statistics / regularize_covariance,
+//                            src/ndt_cuda/src/voxel_grid/types.rs:54-190).
+//   6. compaction          : valid voxels keep their Morton order.
+//   7. hash insert         : bounded linear probing with atomicCAS, displacement recorded
+//                            (voxel_hash_build_kernel, src/cuda_ffi/csrc/voxel_hash.cu:69-114).
+// This translation unit is compiled with -fmad=false: every FP64/FP32 operation is one IEEE
+// rounding, so the statistics match a CPU evaluation of the same operation sequence bit for
+// bit.
+#include <algorithm>
+#include <cstdio>
+
+#include "ndt_internal.h"
+
+namespace ndtgb {
+
+constexpr int BT = 256;        // threads per block for tile kernels
+constexpr int ITEMS = 16;      // items per thread
+constexpr int TILE = BT * ITEMS;
+
+static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+static inline uint32_t ntiles(size_t n) { return (uint32_t)((n + TILE - 1) / TILE); }
+
+// ---------------------------------------------------------------------------------------
+// Block-wide exclusive scan of one value per thread (256 threads).
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* ws,
+                                                         uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (BT / 32) ? ws[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < BT / 32) ws[lane] = w;
+    }
+    __syncthreads();
+    uint32_t pre = warp ? ws[warp - 1] : 0u;
+    *total = ws[BT / 32 - 1];
+    __syncthreads();
+    return pre + x - v;
+}
+
+__global__ void __launch_bounds__(BT) k_tile_reduce(const uint32_t* __restrict__ in, size_t n,
+                                                    uint32_t* __restrict__ bsum) {
+    __shared__ uint32_t ws[BT / 32];
+    size_t base = (size_t)blockIdx.x * TILE;
+    uint32_t s = 0;
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+        size_t i = base + (size_t)r * BT + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    uint32_t tot;
+    block_exclusive_scan(s, ws, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(BT) k_scan_bsums(uint32_t* __restrict__ bsum, uint32_t nb) {
+    __shared__ uint32_t ws[BT / 32];
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nb; base += TILE) {
+        uint32_t v[ITEMS];
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            uint32_t i = base + threadIdx.x * ITEMS + k;
+            v[k] = i < nb ? bsum[i] : 0u;
+            s += v[k];
+        }
+        uint32_t tot;
+        uint32_t run = carry + block_exclusive_scan(s, ws, &tot);
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            uint32_t i = base + threadIdx.x * ITEMS + k;
+            if (i < nb) bsum[i] = run;
+            run += v[k];
+        }
+        carry += tot;
+        __syncthreads();
+    }
+}
+
+// exclusive scan of a tile; element order: thread t holds items t*ITEMS .. t*ITEMS+15
+__global__ void __launch_bounds__(BT) k_tile_scan(const uint32_t* __restrict__ in,
+                                                  uint32_t* __restrict__ out, size_t n,
+                                                  const uint32_t* __restrict__ bsum) {
+    __shared__ uint32_t ws[BT / 32];
+    size_t base = (size_t)blockIdx.x * TILE + (size_t)threadIdx.x * ITEMS;
+    uint32_t v[ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t run = bsum[blockIdx.x] + block_exclusive_scan(s, ws, &tot);
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+size_t scan_temp_bytes(size_t n) { return align_up((size_t)ntiles(n) * 4 + 4, 256); }
+
+// exclusive scan in -> out (may alias); temp >= scan_temp_bytes(n)
+static int exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, void* temp,
+                          cudaStream_t s) {
+    if (n == 0) return 0;
+    uint32_t nb = ntiles(n);
+    uint32_t* bsum = (uint32_t*)temp;
+    k_tile_reduce<<<nb, BT, 0, s>>>(in, n, bsum);
+    k_scan_bsums<<<1, BT, 0, s>>>(bsum, nb);
+    k_tile_scan<<<nb, BT, 0, s>>>(in, out, n, bsum);
+    return cuda_fail(cudaGetLastError(), "scan launch");
+}
+
+// ---------------------------------------------------------------------------------------
+// Stable LSD radix sort of (u64 key, u32 value), 8-bit digits.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(BT) k_radix_hist(const uint64_t* __restrict__ keys, size_t n,
+                                                   int shift, uint32_t dmask,
+                                                   uint32_t* __restrict__ hist, uint32_t nb) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * TILE;
+#pragma unroll 4
+    for (int r = 0; r < ITEMS; ++r) {
+        size_t i = base + (size_t)r * BT + threadIdx.x;
+        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & dmask], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+// Each block re-reads its tile in rounds of 256 consecutive keys; a key's destination is
+// base[digit] (scanned histogram) + keys of the same digit in earlier warps of the round +
+// its rank among same-digit lanes of its warp, so the pass is stable.
+__global__ void __launch_bounds__(BT) k_radix_scatter(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+    uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, size_t n, int shift,
+    uint32_t dmask, const uint32_t* __restrict__ offs, uint32_t nb) {
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t cnt[BT / 32][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    base[threadIdx.x] = offs[(size_t)threadIdx.x * nb + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < BT / 32; ++w) cnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    size_t tbase = (size_t)blockIdx.x * TILE;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int r = 0; r < ITEMS; ++r) {
+        size_t i = tbase + (size_t)r * BT + threadIdx.x;
+        bool valid = i < n;
+        uint64_t key = valid ? kin[i] : 0ull;
+        uint32_t val = valid ? vin[i] : 0u;
+        uint32_t d = valid ? ((uint32_t)(key >> shift) & dmask) : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t rank = __popc(peers & lt);
+        int leader = __ffs(peers) - 1;
+        if (valid && lane == leader) cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pre = 0;
+            for (int w = 0; w < warp; ++w) pre += cnt[w][d];
+            uint32_t pos = base[d] + pre + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+#pragma unroll
+        for (int w = 0; w < BT / 32; ++w) {
+            add += cnt[w][threadIdx.x];
+            cnt[w][threadIdx.x] = 0;
+        }
+        base[threadIdx.x] += add;
+        __syncthreads();
+    }
+}
+
+size_t radix_sort_temp_bytes(size_t n) {
+    size_t nb = ntiles(n);
+    return align_up(n * 8, 256) + align_up(n * 4, 256) + align_up(256 * nb * 4, 256) +
+           scan_temp_bytes(256 * nb);
+}
+
+int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
+                     void* temp, size_t temp_bytes, cudaStream_t s) {
+    if (n <= 1 || end_bit <= begin_bit) return 0;
+    if (temp_bytes < radix_sort_temp_bytes(n)) {
+        set_error("radix sort: temporary storage too small");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    uint32_t nb = ntiles(n);
+    char* t = (char*)temp;
+    uint64_t* kalt = (uint64_t*)t;
+    t += align_up(n * 8, 256);
+    uint32_t* valt = (uint32_t*)t;
+    t += align_up(n * 4, 256);
+    uint32_t* hist = (uint32_t*)t;
+    t += align_up(256 * (size_t)nb * 4, 256);
+    void* stemp = t;
+    uint64_t* kin = keys;
+    uint32_t* vin = vals;
+    uint64_t* kout = kalt;
+    uint32_t* vout = valt;
+    int passes = 0;
+    for (int shift = begin_bit; shift < end_bit; shift += 8, ++passes) {
+        int width = std::min(8, end_bit - shift);
+        uint32_t dmask = (1u << width) - 1u;
+        k_radix_hist<<<nb, BT, 0, s>>>(kin, n, shift, dmask, hist, nb);
+        int rc = exclusive_scan(hist, hist, 256 * (size_t)nb, stemp, s);
+        if (rc) return rc;
+        k_radix_scatter<<<nb, BT, 0, s>>>(kin, vin, kout, vout, n, shift, dmask, hist, nb);
+        int e = cuda_fail(cudaGetLastError(), "radix scatter launch");
+        if (e) return e;
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    if (passes & 1) {
+        cudaMemcpyAsync(keys, kin, n * 8, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(vals, vin, n * 4, cudaMemcpyDeviceToDevice, s);
+    }
+    return cuda_fail(cudaGetLastError(), "radix sort");
+}
+
+// ---------------------------------------------------------------------------------------
+// Segments of sorted keys.
+// ---------------------------------------------------------------------------------------
+__global__ void k_seg_flags(const uint64_t* __restrict__ keys, size_t n,
+                            uint32_t* __restrict__ flags) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flags[i] = (i > 0 && keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_seg_finish(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ ex,
+                             size_t n, uint32_t* __restrict__ seg_ids,
+                             uint32_t* __restrict__ starts, uint32_t* __restrict__ num) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t f = flags[i];
+    uint32_t sid = ex[i] + f;
+    if (seg_ids) seg_ids[i] = sid;
+    if (i == 0 || f) starts[sid] = (uint32_t)i;
+    if (i == n - 1) *num = sid + 1;
+}
+
+size_t detect_segments_temp_bytes(size_t n) {
+    return 2 * align_up(n * 4 + 4, 256) + scan_temp_bytes(n);
+}
+
+int detect_segments(const uint64_t* sorted, size_t n, uint32_t* seg_ids, uint32_t* seg_starts,
+                    uint32_t* num_segments, void* temp, size_t temp_bytes, cudaStream_t s) {
+    cudaMemsetAsync(num_segments, 0, 4, s);
+    if (n == 0) return cuda_fail(cudaGetLastError(), "segments");
+    if (temp_bytes < detect_segments_temp_bytes(n)) {
+        set_error("detect segments: temporary storage too small");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    char* t = (char*)temp;
+    uint32_t* flags = (uint32_t*)t;
+    t += align_up(n * 4 + 4, 256);
+    uint32_t* ex = (uint32_t*)t;
+    t += align_up(n * 4 + 4, 256);
+    unsigned g = (unsigned)((n + BT - 1) / BT);
+    k_seg_flags<<<g, BT, 0, s>>>(sorted, n, flags);
+    int rc = exclusive_scan(flags, ex, n, t, s);
+    if (rc) return rc;
+    k_seg_finish<<<g, BT, 0, s>>>(flags, ex, n, seg_ids, seg_starts, num_segments);
+    return cuda_fail(cudaGetLastError(), "segments");
+}
+
+// ---------------------------------------------------------------------------------------
+// Cells, bounds and Morton keys.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+    return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+__device__ __forceinline__ void cell_of(const float* p, float res, int32_t* c) {
+    c[0] = sat_i32(floorf(p[0] / res));
+    c[1] = sat_i32(floorf(p[1] / res));
+    c[2] = sat_i32(floorf(p[2] / res));
+}
+
+// mm: [0..2] min cell, [3..5] max cell, [6] finite count
+__global__ void __launch_bounds__(BT) k_cells_minmax(const float* __restrict__ pts, size_t n,
+                                                     float res, int32_t* __restrict__ mm) {
+    int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    uint32_t cnt = 0;
+    for (size_t i = (size_t)blockIdx.x * BT + threadIdx.x; i < n; i += (size_t)gridDim.x * BT) {
+        float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        if (!finite3(p[0], p[1], p[2])) continue;
+        int32_t c[3];
+        cell_of(p, res, c);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], c[a]);
+            mx[a] = max(mx[a], c[a]);
+        }
+        cnt++;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&mm[a], mn[a]);
+            atomicMax(&mm[3 + a], mx[a]);
+        }
+        atomicAdd(&mm[6], (int32_t)cnt);
+    }
+}
+
+__global__ void k_minmax_init(int32_t* mm) {
+    if (threadIdx.x < 3) mm[threadIdx.x] = INT32_MAX;
+    else if (threadIdx.x < 6) mm[threadIdx.x] = INT32_MIN;
+    else if (threadIdx.x == 6) mm[6] = 0;
+}
+
+__global__ void __launch_bounds__(BT) k_morton(const float* __restrict__ pts, size_t n, float res,
+                                               const int32_t* __restrict__ mm,
+                                               uint64_t* __restrict__ codes,
+                                               uint32_t* __restrict__ idx) {
+    size_t i = (size_t)blockIdx.x * BT + threadIdx.x;
+    if (i >= n) return;
+    float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+    uint64_t code = ~0ull;
+    if (finite3(p[0], p[1], p[2])) {
+        int32_t c[3];
+        cell_of(p, res, c);
+        uint32_t q[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int64_t d = (int64_t)c[a] - (int64_t)mm[a];
+            q[a] = d > 0x1FFFFF ? 0x1FFFFFu : (uint32_t)d;
+        }
+        code = morton3(q[0], q[1], q[2]);
+    }
+    codes[i] = code;
+    idx[i] = (uint32_t)i;
+}
+
+int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_t* idx,
+                 int32_t* mm, cudaStream_t s) {
+    k_minmax_init<<<1, 32, 0, s>>>(mm);
+    if (n) {
+        unsigned g = (unsigned)std::min<size_t>((n + BT - 1) / BT, 152 * 8);
+        k_cells_minmax<<<g, BT, 0, s>>>(pts, n, res, mm);
+        k_morton<<<(unsigned)((n + BT - 1) / BT), BT, 0, s>>>(pts, n, res, mm, codes, idx);
+    }
+    return cuda_fail(cudaGetLastError(), "morton codes");
+}
+
+// ---------------------------------------------------------------------------------------
+// Voxel statistics (one thread per segment) and regularisation.
+// ---------------------------------------------------------------------------------------
+struct SegRec {
+    float mean[3];
+    float cov[9];
+    float icov[6];  // c00, c01, c02, c11, c12, c22
+    int32_t coord[3];
+    uint32_t count;
+};
+
+// Cyclic Jacobi for a symmetric 3x3 in FP64 (same operation sequence as the CPU oracle).
+__device__ void jacobi3(double* a, double* v) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) v[i * 3 + j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        double off = 0.0, dg = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            dg += a[i * 3 + i] * a[i * 3 + i];
+            for (int j = i + 1; j < 3; ++j) off += a[i * 3 + j] * a[i * 3 + j];
+        }
+        if (off <= 1e-40 * dg) break;
+        for (int p = 0; p < 2; ++p) {
+            for (int q = p + 1; q < 3; ++q) {
+                double apq = a[p * 3 + q];
+                if (apq == 0.0) continue;
+                double theta = (a[q * 3 + q] - a[p * 3 + p]) / (2.0 * apq);
+                double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+                if (theta < 0.0) t = -t;
+                double c = 1.0 / sqrt(t * t + 1.0);
+                double s = t * c;
+                a[p * 3 + p] = a[p * 3 + p] - t * apq;
+                a[q * 3 + q] = a[q * 3 + q] + t * apq;
+                a[p * 3 + q] = 0.0;
+                a[q * 3 + p] = 0.0;
+                int r = 3 - p - q;
+                double arp = a[r * 3 + p], arq = a[r * 3 + q];
+                double np = c * arp - s * arq;
+                double nq = s * arp + c * arq;
+                a[r * 3 + p] = np;
+                a[p * 3 + r] = np;
+                a[r * 3 + q] = nq;
+                a[q * 3 + r] = nq;
+                for (int k = 0; k < 3; ++k) {
+                    double vrp = v[k * 3 + p], vrq = v[k * 3 + q];
+                    v[k * 3 + p] = c * vrp - s * vrq;
+                    v[k * 3 + q] = s * vrp + c * vrq;
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_voxel_stats(
+    const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
+    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ num_seg, uint32_t nf,
+    float res, int min_points, float ratio, SegRec* __restrict__ rec,
+    uint32_t* __restrict__ valid) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t S = *num_seg;
+    if (s >= nf) return;
+    if (s >= S) {
+        valid[s] = 0;
+        return;
+    }
+    uint32_t b = starts[s];
+    uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+    uint32_t cnt = e - b;
+    uint32_t ok = 0;
+    SegRec r;
+    {
+        const float* p0 = pts + 3 * (size_t)sidx[b];
+        cell_of(p0, res, r.coord);
+    }
+    r.count = cnt;
+    if ((int)cnt >= min_points) {
+        double sum[3] = {0.0, 0.0, 0.0};
+        for (uint32_t k = b; k < e; ++k) {
+            const float* p = pts + 3 * (size_t)sidx[k];
+            sum[0] += (double)p[0];
+            sum[1] += (double)p[1];
+            sum[2] += (double)p[2];
+        }
+        double nn = (double)cnt;
+        double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
+        double sq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint32_t k = b; k < e; ++k) {
+            const float* p = pts + 3 * (size_t)sidx[k];
+            double d[3] = {(double)p[0] - mean[0], (double)p[1] - mean[1],
+                           (double)p[2] - mean[2]};
+            for (int rr = 0; rr < 3; ++rr)
+                for (int cc = 0; cc < 3; ++cc) sq[rr * 3 + cc] += d[rr] * d[cc];
+        }
+        double cov[9];
+        for (int q = 0; q < 9; ++q) cov[q] = sq[q] / (nn - 1.0);
+        double a[9], V[9], ev[3];
+        for (int q = 0; q < 9; ++q) a[q] = cov[q];
+        jacobi3(a, V);
+        for (int i = 0; i < 3; ++i) ev[i] = a[i * 3 + i];
+        double mx = 0.0;
+        for (int i = 0; i < 3; ++i) mx = fmax(mx, ev[i]);
+        if (mx > 0.0) {
+            double thr = mx * (double)ratio;
+            int needs = 0;
+            double cl[3];
+            for (int i = 0; i < 3; ++i) {
+                cl[i] = ev[i] < thr ? thr : ev[i];
+                if (ev[i] < thr) needs = 1;
+            }
+            double rc[9], ic[9];
+            for (int rr = 0; rr < 3; ++rr) {
+                for (int cc = rr; cc < 3; ++cc) {
+                    double sr = 0.0, si = 0.0;
+                    for (int k = 0; k < 3; ++k) {
+                        sr += V[rr * 3 + k] * cl[k] * V[cc * 3 + k];
+                        si += V[rr * 3 + k] * (1.0 / cl[k]) * V[cc * 3 + k];
+                    }
+                    rc[rr * 3 + cc] = rc[cc * 3 + rr] = sr;
+                    ic[rr * 3 + cc] = ic[cc * 3 + rr] = si;
+                }
+            }
+            for (int q = 0; q < 9; ++q) r.cov[q] = (float)(needs ? rc[q] : cov[q]);
+            r.icov[0] = (float)ic[0];
+            r.icov[1] = (float)ic[1];
+            r.icov[2] = (float)ic[2];
+            r.icov[3] = (float)ic[4];
+            r.icov[4] = (float)ic[5];
+            r.icov[5] = (float)ic[8];
+            for (int q = 0; q < 3; ++q) r.mean[q] = (float)mean[q];
+            ok = 1;
+        }
+    }
+    if (ok) rec[s] = r;
+    valid[s] = ok;
+}
+
+__global__ void k_voxel_compact(const SegRec* __restrict__ rec, const uint32_t* __restrict__ valid,
+                                const uint32_t* __restrict__ rank,
+                                const uint32_t* __restrict__ num_seg, int32_t* __restrict__ coord,
+                                float4* __restrict__ mean4, float* __restrict__ cov,
+                                float* __restrict__ icov, uint32_t* __restrict__ count) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *num_seg || !valid[s]) return;
+    uint32_t v = rank[s];
+    const SegRec& r = rec[s];
+    coord[3 * v] = r.coord[0];
+    coord[3 * v + 1] = r.coord[1];
+    coord[3 * v + 2] = r.coord[2];
+    mean4[v] = make_float4(r.mean[0], r.mean[1], r.mean[2], __uint_as_float(r.count));
+    for (int q = 0; q < 9; ++q) cov[9 * (size_t)v + q] = r.cov[q];
+    const float* c = r.icov;
+    float full[9] = {c[0], c[1], c[2], c[1], c[3], c[4], c[2], c[4], c[5]};
+    for (int q = 0; q < 9; ++q) icov[9 * (size_t)v + q] = full[q];
+    count[v] = r.count;
+}
+
+__global__ void k_hash_insert(const int32_t* __restrict__ coord, const float4* __restrict__ mean4,
+                              const float* __restrict__ icov, uint32_t nv, MapView m,
+                              uint4* __restrict__ slots, float4* __restrict__ slot_icov,
+                              int32_t* __restrict__ slot_vidx, uint32_t* __restrict__ max_probe,
+                              uint32_t* __restrict__ status) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    int32_t gx = coord[3 * v], gy = coord[3 * v + 1], gz = coord[3 * v + 2];
+    uint32_t key = local_key(m, gx, gy, gz);
+    uint32_t s = (uint32_t)fmix64(pack21(gx, gy, gz)) & m.mask;
+    for (uint32_t j = 0; j <= m.mask; ++j) {
+        uint32_t old = atomicCAS(&slots[s].x, EMPTY_KEY, key);
+        if (old == EMPTY_KEY) {
+            float4 mu = mean4[v];
+            slots[s].y = __float_as_uint(mu.x);
+            slots[s].z = __float_as_uint(mu.y);
+            slots[s].w = __float_as_uint(mu.z);
+            const float* c = icov + 9 * (size_t)v;
+            slot_icov[2 * (size_t)s] = make_float4(c[0], c[1], c[2], c[4]);
+            slot_icov[2 * (size_t)s + 1] = make_float4(c[5], c[8], 0.f, 0.f);
+            slot_vidx[s] = (int32_t)v;
+            atomicMax(max_probe, j);
+            return;
+        }
+        s = (s + 1) & m.mask;
+    }
+    atomicOr(status, ST_HASH_FULL);
+}
+
+static uint32_t bit_width(uint32_t x) {
+    uint32_t b = 0;
+    while (b < 32 && (x >> b)) ++b;
+    return b;
+}
+
+int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+              uint32_t* d_status, cudaStream_t s, float* build_ms) {
+    if (n == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    if (n >= 0xFFFFFFF0ull) {
+        set_error("target point cloud exceeds 2^32 points");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    int rc = 0;
+    if ((rc = dev_reserve(sc.keys_a, n * 8)) || (rc = dev_reserve(sc.vals_a, n * 4)) ||
+        (rc = dev_reserve(sc.small, 256)) || (rc = dev_reserve(sc.seg_starts, n * 4 + 4)) ||
+        (rc = dev_reserve(sc.seg_valid, n * 4 + 4)) || (rc = dev_reserve(sc.seg_rank, n * 4 + 4)) ||
+        (rc = dev_reserve(sc.seg_rec, n * sizeof(SegRec))))
+        return rc;
+    size_t tmp = std::max(radix_sort_temp_bytes(n), detect_segments_temp_bytes(n));
+    tmp = std::max(tmp, scan_temp_bytes(n));
+    if ((rc = dev_reserve(sc.tmp, tmp))) return rc;
+    uint64_t* keys = (uint64_t*)sc.keys_a.p;
+    uint32_t* vals = (uint32_t*)sc.vals_a.p;
+    int32_t* mm = (int32_t*)sc.small.p;
+    uint32_t* nseg = (uint32_t*)((char*)sc.small.p + 64);
+    uint32_t* mprobe = (uint32_t*)((char*)sc.small.p + 128);
+
+    if ((rc = morton_codes(d_pts, n, cfg.resolution, keys, vals, mm, s))) return rc;
+    int32_t hmm[7];
+    cudaMemcpyAsync(hmm, mm, sizeof hmm, cudaMemcpyDeviceToHost, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "map bounds"))) return rc;
+    size_t nf = (size_t)(uint32_t)hmm[6];
+    if (nf == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    uint32_t bits[3];
+    for (int a = 0; a < 3; ++a) {
+        int64_t range = (int64_t)hmm[3 + a] - (int64_t)hmm[a];
+        if (range > 0x1FFFFF) {
+            set_error("map extent exceeds 2^21 voxels along an axis");
+            return NDT_ERR_RANGE;
+        }
+        bits[a] = std::max<uint32_t>(1, bit_width((uint32_t)range));
+    }
+    if (bits[0] + bits[1] + bits[2] > 31) {
+        set_error("map bounding box exceeds 2^31 voxel cells (tile the map)");
+        return NDT_ERR_RANGE;
+    }
+    uint32_t lv = std::max(bits[0], std::max(bits[1], bits[2]));
+    int end_bit = std::min(64, (int)(3 * lv + 1));
+    if ((rc = radix_sort_pairs(keys, vals, n, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s))) return rc;
+    if ((rc = detect_segments(keys, nf, nullptr, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p,
+                              sc.tmp.bytes, s)))
+        return rc;
+    unsigned g = (unsigned)((nf + 127) / 128);
+    k_voxel_stats<<<g, 128, 0, s>>>(d_pts, vals, (uint32_t*)sc.seg_starts.p, nseg, (uint32_t)nf,
+                                    cfg.resolution, cfg.min_points_per_voxel,
+                                    cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
+                                    (uint32_t*)sc.seg_valid.p);
+    if ((rc = exclusive_scan((uint32_t*)sc.seg_valid.p, (uint32_t*)sc.seg_rank.p, nf, sc.tmp.p,
+                             s)))
+        return rc;
+    uint32_t hs[3];
+    cudaMemcpyAsync(&hs[0], nseg, 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hs[1], (uint32_t*)sc.seg_rank.p + (nf - 1), 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hs[2], (uint32_t*)sc.seg_valid.p + (nf - 1), 4, cudaMemcpyDeviceToHost, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "voxel statistics"))) return rc;
+    uint32_t S = hs[0];
+    uint32_t V = hs[1] + hs[2];
+    if (V == 0) {
+        set_error("No voxels created from target points (too sparse?)");
+        return NDT_ERR_NO_VOXELS;
+    }
+    uint64_t factor = (uint64_t)std::max(2, cfg.hash_capacity_factor);
+    uint64_t cap = 1;
+    while (cap < factor * V) cap *= 2;
+    if (cap > (1ull << 31)) {
+        set_error("hash capacity exceeds 2^31 slots");
+        return NDT_ERR_CAPACITY;
+    }
+    if ((rc = dev_reserve(map.vox_coord, (size_t)V * 12)) ||
+        (rc = dev_reserve(map.vox_mean, (size_t)V * 16)) ||
+        (rc = dev_reserve(map.vox_cov, (size_t)V * 36)) ||
+        (rc = dev_reserve(map.vox_icov, (size_t)V * 36)) ||
+        (rc = dev_reserve(map.vox_count, (size_t)V * 4)) ||
+        (rc = dev_reserve(map.slots, cap * 16)) || (rc = dev_reserve(map.slot_icov, cap * 32)) ||
+        (rc = dev_reserve(map.slot_vidx, cap * 4)))
+        return rc;
+    k_voxel_compact<<<g, 128, 0, s>>>((SegRec*)sc.seg_rec.p, (uint32_t*)sc.seg_valid.p,
+                                      (uint32_t*)sc.seg_rank.p, nseg, (int32_t*)map.vox_coord.p,
+                                      (float4*)map.vox_mean.p, (float*)map.vox_cov.p,
+                                      (float*)map.vox_icov.p, (uint32_t*)map.vox_count.p);
+    cudaMemsetAsync(map.slots.p, 0xFF, cap * 16, s);
+    cudaMemsetAsync(mprobe, 0, 4, s);
+    MapView v{};
+    v.slots = (const uint4*)map.slots.p;
+    v.slot_icov = (const float4*)map.slot_icov.p;
+    v.slot_vidx = (const int32_t*)map.slot_vidx.p;
+    v.mask = (uint32_t)(cap - 1);
+    v.max_probe = 0;
+    for (int a = 0; a < 3; ++a) {
+        v.min_cell[a] = hmm[a];
+        v.bits[a] = bits[a];
+    }
+    v.res = cfg.resolution;
+    v.inv_res = 1.0f / cfg.resolution;
+    v.r2 = cfg.resolution * cfg.resolution;
+    v.num_voxels = V;
+    k_hash_insert<<<(V + 127) / 128, 128, 0, s>>>(
+        (int32_t*)map.vox_coord.p, (float4*)map.vox_mean.p, (float*)map.vox_icov.p, V, v,
+        (uint4*)map.slots.p, (float4*)map.slot_icov.p, (int32_t*)map.slot_vidx.p, mprobe,
+        d_status);
+    cudaEventRecord(e1, s);
+    uint32_t hprobe = 0;
+    cudaMemcpyAsync(&hprobe, mprobe, 4, cudaMemcpyDeviceToHost, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "hash insert"))) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (build_ms) *build_ms = ms;
+    v.max_probe = hprobe;
+    map.view = v;
+    ndt_map_info& info = map.info;
+    info.num_points = nf;
+    info.num_segments = S;
+    info.num_voxels = V;
+    info.hash_capacity = cap;
+    info.max_probe = hprobe;
+    for (int a = 0; a < 3; ++a) {
+        info.key_bits[a] = bits[a];
+        info.min_coord[a] = hmm[a];
+        info.max_coord[a] = hmm[3 + a];
+    }
+    info.build_ms = ms;
+    map.valid = true;
+    return 0;
+}
+
+}  // namespace ndtgb

@@ -1,0 +1,209 @@
+/*
+ * ndt_gb300.h — C ABI of the GB300-native NDT scan-matching library (libndt_gb300.so).
+ *
+ * Drop-in boundary for the hot path of cuda_ndt_matcher: the `ndt_cuda` crate's
+ * NdtScanMatcher (src/ndt_cuda/src/ndt.rs:255-1321) calls these functions in place of its
+ * CubeCL pipelines and the `cuda_ffi` kernels (src/cuda_ffi/csrc/). Conventions:
+ *   - every function returns int: 0 = NDT_OK, negative = NDT_ERR_*, positive = a
+ *     cudaError_t passed through from the CUDA runtime (the reference's `CudaError` codes,
+ *     src/cuda_ffi/src/radix_sort.rs:59-95);
+ *   - no exceptions cross the ABI; ndt_last_error_string() describes the last failure of
+ *     the calling thread;
+ *   - the caller owns host arrays; a context owns every device buffer and its CUDA stream,
+ *     grows capacities monotonically and allocates nothing on the alignment path once
+ *     warmed up;
+ *   - a context is single-threaded (the reference serialises a matcher behind a Mutex,
+ *     src/cuda_ndt_matcher/src/main.rs:951); several contexts may share one device.
+ *
+ * Poses are 6-vectors [x, y, z, roll, pitch, yaw] with R = Rx(roll)*Ry(pitch)*Rz(yaw), the
+ * convention of the reference's derivative kernels
+ * (src/cuda_ffi/csrc/persistent_ndt_device.cuh:38-71). Converting an Isometry3 with
+ * nalgebra's euler angles (src/ndt_cuda/src/optimization/types.rs:156-174) is the host
+ * binding's job, as in the reference.
+ */
+#ifndef NDT_GB300_H
+#define NDT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NDT_OK 0
+#define NDT_ERR_INVALID_ARGUMENT (-1)
+#define NDT_ERR_NO_TARGET (-2)      /* "No target set. Call set_target() first." */
+#define NDT_ERR_EMPTY_INPUT (-3)    /* "Target/Source point cloud is empty" */
+#define NDT_ERR_NO_VOXELS (-4)      /* "No voxels created from target points (too sparse?)" */
+#define NDT_ERR_RANGE (-5)          /* map extent exceeds the voxel key range */
+#define NDT_ERR_HASH_FULL (-6)      /* device: hash insert found no free slot */
+#define NDT_ERR_PROBE_LIMIT (-7)    /* device: a probe sequence exceeded its bound */
+#define NDT_ERR_DEVICE (-8)         /* device: other status reported by a kernel */
+#define NDT_ERR_NO_DEVICE (-9)      /* no CUDA device with compute capability 10.3 */
+#define NDT_ERR_CAPACITY (-10)      /* a size exceeds a fixed limit of the entry point */
+
+#define NDT_SEMANTICS_GPU_GRAPH 0   /* align_gpu: graph kernels K1-K5 */
+#define NDT_SEMANTICS_CPU 1         /* align with use_gpu = false: NdtOptimizer::align */
+
+#define NDT_STATUS_CONVERGED 0
+#define NDT_STATUS_MAX_ITERATIONS 1
+#define NDT_STATUS_NO_CORRESPONDENCES 2
+#define NDT_STATUS_SINGULAR_HESSIAN 3
+
+/* NdtScanMatcherConfig (src/ndt_cuda/src/ndt.rs:41-107) plus device tuning knobs. */
+typedef struct ndt_config {
+    float resolution;              /* 2.0 m */
+    int32_t max_iterations;        /* 30 */
+    double trans_epsilon;          /* 0.01 */
+    double step_size;              /* 0.1, maximum step length */
+    double outlier_ratio;          /* 0.55 */
+    int32_t min_points_per_voxel;  /* 6 */
+    float eigenvalue_ratio;        /* 0.01 (VoxelGridConfig::eigenvalue_ratio_threshold) */
+    int32_t max_neighbors;         /* 8: graph-kernel truncation (ndt_graph_common.cuh:21) */
+    int32_t semantics;             /* NDT_SEMANTICS_* */
+    int32_t min_correspondences;   /* 10 (OptimizationConfig, solver.rs:58); CPU semantics */
+    int32_t device;                /* CUDA device ordinal */
+    int32_t cluster_size;          /* CTAs per alignment; 0 = autotuned */
+    int32_t threads_per_cta;       /* 0 = autotuned */
+    int32_t hash_capacity_factor;  /* capacity = next pow2 >= factor * V; 2 = reference */
+    int32_t reserved[3];
+} ndt_config;
+
+/* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
+typedef struct ndt_result {
+    double pose[6];
+    double score;
+    double transform_probability;  /* score / num source points (solver.rs:707-713) */
+    double nvtl;                   /* compute_nvtl_simple at the final pose (scoring/nvtl.rs:211) */
+    double hessian[36];            /* row-major */
+    int32_t converged;
+    int32_t iterations;
+    int32_t num_correspondences;
+    int32_t oscillation_count;
+    int32_t status;                /* NDT_STATUS_* */
+    int32_t reserved;
+} ndt_result;
+
+/* One scan of a batch (align_parallel_scans, src/ndt_cuda/src/ndt.rs:1224). */
+typedef struct ndt_scan {
+    const float* xyz;              /* host, num_points * 3 floats */
+    uint64_t num_points;
+    double initial_pose[6];
+} ndt_scan;
+
+typedef struct ndt_map_info {
+    uint64_t num_points;           /* finite input points */
+    uint64_t num_segments;         /* occupied cells */
+    uint64_t num_voxels;           /* valid voxels (count >= min points, regularisable) */
+    uint64_t hash_capacity;
+    uint32_t max_probe;            /* longest insert probe sequence (slots) */
+    uint32_t key_bits[3];          /* local key bits per axis */
+    int32_t min_coord[3];
+    int32_t max_coord[3];
+    float build_ms;                /* device time of the last set_target build */
+    float reserved;
+} ndt_map_info;
+
+/* Counters accumulated by a context since creation or the last ndt_stats_reset. */
+typedef struct ndt_stats {
+    uint64_t align_launches;       /* Newton kernel launches */
+    uint64_t alignments;
+    uint64_t iterations;           /* sum of Newton iterations */
+    uint64_t point_iterations;     /* sum over iterations of scan points processed */
+    uint64_t correspondences;      /* sum over iterations of point-voxel pairs */
+    double align_kernel_ms;        /* CUDA-event time of the Newton kernel launches */
+    uint64_t score_launches;
+    double score_kernel_ms;
+    uint64_t build_launches;
+    double build_ms;
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+} ndt_stats;
+
+typedef struct ndt_ctx ndt_ctx;
+
+/* Defaults of NdtScanMatcherConfig::default() (src/ndt_cuda/src/ndt.rs:90-107). */
+int ndt_config_default(ndt_config* cfg);
+
+/* NdtScanMatcher::with_config (src/ndt_cuda/src/ndt.rs:279-331). */
+int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out);
+int ndt_ctx_destroy(ndt_ctx* ctx);
+/* Replaces the alignment parameters of a live context (iterations, epsilon, step size,
+ * outlier ratio, neighbour cap, semantics, launch shape) without touching the map. The
+ * map parameters (resolution, min points, eigenvalue ratio, hash factor) take effect at the
+ * next ndt_set_target. */
+int ndt_ctx_configure(ndt_ctx* ctx, const ndt_config* cfg);
+/* the context's CUDA stream (a cudaStream_t), for callers that order their own work on it */
+void* ndt_ctx_stream(ndt_ctx* ctx);
+
+/* NdtScanMatcher::set_target (src/ndt_cuda/src/ndt.rs:361-407): builds the voxel map
+ * (Morton keys, LSD radix sort, segments, FP64 moments, eigen regularisation, hash insert)
+ * on the device. `xyz` is host memory; the _device variant takes a device pointer. */
+int ndt_set_target(ndt_ctx* ctx, const float* xyz, uint64_t num_points);
+int ndt_set_target_device(ndt_ctx* ctx, const float* d_xyz, uint64_t num_points);
+int ndt_map_info_get(ndt_ctx* ctx, ndt_map_info* out);
+/* VoxelGrid accessors (means_flat / inv_covariances_flat, voxel_grid/mod.rs:428-453):
+ * valid voxels in ascending coordinate-Morton order; any output pointer may be NULL. */
+int ndt_map_voxels(ndt_ctx* ctx, int32_t* coords, float* means, float* covs, float* icovs,
+                   uint32_t* counts, uint64_t capacity);
+
+/* NdtScanMatcher::align / align_gpu (src/ndt_cuda/src/ndt.rs:421-510). */
+int ndt_align(ndt_ctx* ctx, const float* xyz, uint64_t num_points, const double pose_in[6],
+              ndt_result* out);
+/* NdtScanMatcher::align_batch_gpu (src/ndt_cuda/src/ndt.rs:959): one scan, many poses. */
+int ndt_align_multi_pose(ndt_ctx* ctx, const float* xyz, uint64_t num_points,
+                         const double* poses_in, uint64_t num_poses, ndt_result* out);
+/* NdtScanMatcher::align_parallel_scans (src/ndt_cuda/src/ndt.rs:1224-1321): uneven scans
+ * aligned in one launch (one thread-block cluster per alignment). */
+int ndt_align_batch(ndt_ctx* ctx, const ndt_scan* scans, uint64_t num_scans, ndt_result* out);
+/* Same, with the scans already resident on the device, concatenated: scan i is
+ * d_xyz[3*offsets[i] .. 3*offsets[i+1]); offsets and poses are host arrays. */
+int ndt_align_batch_device(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
+                           const double* poses_in, uint64_t num_scans, ndt_result* out);
+
+/* evaluate_nvtl / evaluate_transform_probability / evaluate_nvtl_batch
+ * (src/ndt_cuda/src/ndt.rs:681-890): per pose, NVTL (mean over points with a neighbour of
+ * the best voxel score) and score / correspondences over all voxels within one resolution.
+ * T34 = num_poses row-major 3x4 world transforms (host). nvtl / tp may be NULL. */
+int ndt_eval_batch(ndt_ctx* ctx, const float* xyz, uint64_t num_points, const double* T34,
+                   uint64_t num_poses, double* nvtl, double* transform_probability);
+
+/* 27-cell hash neighbour query (graph_hash_query_inline, ndt_graph_kernels.cu:47-104;
+ * voxel_hash_query_kernel, voxel_hash.cu:136-210) for host query points; idx is
+ * num_points * max_neighbors voxel indices (Morton order), -1 padded. */
+int ndt_neighbors_query(ndt_ctx* ctx, const float* xyz, uint64_t num_points,
+                        int32_t max_neighbors, int32_t* idx, int32_t* counts);
+
+int ndt_stats_get(ndt_ctx* ctx, ndt_stats* out);
+int ndt_stats_reset(ndt_ctx* ctx);
+/* Enables CUDA-event timing of every kernel launch (read back through ndt_stats). */
+int ndt_profile_enable(ndt_ctx* ctx, int enable);
+
+const char* ndt_last_error_string(void);
+
+/* ---- build-stage primitives on caller device memory (the cuda_ffi roles) ------------ */
+/* Temporary storage follows the two-phase convention of the reference's CUB wrappers:
+ * call with d_temp == NULL to read the required *temp_bytes. `stream` is a cudaStream_t. */
+
+/* cub_radix_sort_pairs_u64_u32 (src/cuda_ffi/csrc/radix_sort.cu:62-86): stable ascending
+ * LSD sort of (u64 key, u32 value) pairs on bits [begin_bit, end_bit), in place. */
+int ndt_radix_sort_pairs_u64_u32(uint64_t* d_keys, uint32_t* d_values, uint64_t n,
+                                 int32_t begin_bit, int32_t end_bit, void* d_temp,
+                                 uint64_t* temp_bytes, void* stream);
+/* detect_boundaries_kernel + InclusiveSum + Flagged (src/cuda_ffi/csrc/segment_detect.cu:
+ * 27-146): segment id per element and start index per segment of sorted keys. */
+int ndt_detect_segments(const uint64_t* d_sorted, uint64_t n, uint32_t* d_segment_ids,
+                        uint32_t* d_segment_starts, uint32_t* d_num_segments, void* d_temp,
+                        uint64_t* temp_bytes, void* stream);
+/* compute_morton_codes_kernel (src/ndt_cuda/src/voxel_grid/gpu/morton.rs:45-95) with this
+ * library's membership rule: key = morton(floor(p / res) - min cell), idx = identity.
+ * min_cell (3 x int32, device) receives the per-axis minimum cell. */
+int ndt_morton_codes(const float* d_xyz, uint64_t n, float resolution, uint64_t* d_codes,
+                     uint32_t* d_indices, int32_t* d_min_cell, void* d_temp,
+                     uint64_t* temp_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NDT_GB300_H */

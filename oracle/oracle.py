@@ -1,0 +1,304 @@
+"""ctypes wrapper over the oracle library (test infrastructure only).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs as the checker
+and as the timed CPU baseline. The GPU product never imports this module.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class OrResult(C.Structure):
+    _fields_ = [("pose", C.c_double * 6), ("score", C.c_double),
+                ("transform_probability", C.c_double), ("nvtl", C.c_double),
+                ("hessian", C.c_double * 36), ("converged", C.c_int32),
+                ("iterations", C.c_int32), ("num_correspondences", C.c_int32),
+                ("oscillation_count", C.c_int32), ("status", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self):
+        return {
+            "pose": np.array(self.pose[:], dtype=np.float64),
+            "score": self.score,
+            "transform_probability": self.transform_probability,
+            "nvtl": self.nvtl,
+            "hessian": np.array(self.hessian[:], dtype=np.float64).reshape(6, 6),
+            "converged": bool(self.converged),
+            "iterations": self.iterations,
+            "num_correspondences": self.num_correspondences,
+            "oscillation_count": self.oscillation_count,
+            "status": self.status,
+        }
+
+
+class OrConfig(C.Structure):
+    _fields_ = [("resolution", C.c_double), ("max_iterations", C.c_int32),
+                ("max_neighbors", C.c_int32), ("trans_epsilon", C.c_double),
+                ("step_size", C.c_double), ("outlier_ratio", C.c_double),
+                ("min_correspondences", C.c_int32), ("pad", C.c_int32)]
+
+
+def config(resolution=2.0, max_iterations=30, max_neighbors=8, trans_epsilon=0.01,
+           step_size=0.1, outlier_ratio=0.55, min_correspondences=10):
+    return OrConfig(resolution, max_iterations, max_neighbors, trans_epsilon, step_size,
+                    outlier_ratio, min_correspondences, 0)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+        u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+        sig = {
+            "or_gauss_params": (None, [C.c_double, C.c_double, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
+            "or_voxel_coord": (None, [f32p, C.c_float, i32p]),
+            "or_morton_encode": (C.c_uint64, [C.c_uint32, C.c_uint32, C.c_uint32]),
+            "or_morton_decode": (None, [C.c_uint64, C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+            "or_morton_codes_ref": (None, [f32p, C.c_size_t, C.c_float, u64p, f32p]),
+            "or_morton_codes_coord": (C.c_int, [f32p, C.c_size_t, C.c_float, u64p, i32p]),
+            "or_radix_sort_pairs": (None, [u64p, u32p, C.c_size_t]),
+            "or_detect_segments": (C.c_size_t, [u64p, C.c_size_t, u32p, u32p]),
+            "or_grid_build": (P, [f32p, C.c_size_t, C.c_float, C.c_int, C.c_float, C.c_int]),
+            "or_grid_free": (None, [P]),
+            "or_grid_size": (C.c_size_t, [P]),
+            "or_grid_copy": (None, [P, i32p, f32p, f32p, f32p, u32p, f32p]),
+            "or_grid_hash_capacity": (C.c_uint32, [P]),
+            "or_pack_key": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32]),
+            "or_hash_slot": (C.c_uint32, [C.c_int64, C.c_uint32]),
+            "or_grid_lookup": (C.c_int32, [P, C.c_int32, C.c_int32, C.c_int32]),
+            "or_query_gpu_sem": (None, [P, f32p, C.c_size_t, C.c_int, i32p, i32p]),
+            "or_radius_search": (C.c_int, [P, f32p, C.c_float, i32p, C.c_int]),
+            "or_derivatives_cpu": (None, [P, f32p, C.c_size_t, f64p, C.c_double, C.c_double,
+                                          C.POINTER(C.c_double), f64p, f64p,
+                                          C.POINTER(C.c_int32)]),
+            "or_derivatives_gpu_sem": (None, [P, f32p, C.c_size_t, f64p, C.c_double,
+                                              C.c_double, C.c_int, C.POINTER(C.c_double),
+                                              f64p, f64p, C.POINTER(C.c_int32)]),
+            "or_newton_step_nd": (C.c_int, [f64p, f64p, C.c_double, C.c_double, f64p]),
+            "or_jacobi_svd_solve": (C.c_int, [f64p, f64p, f64p]),
+            "or_align_cpu": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
+                                    C.POINTER(OrResult)]),
+            "or_align_gpu_sem": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
+                                        C.POINTER(OrResult)]),
+            "or_align_batch": (None, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), f64p,
+                                      C.c_size_t, C.POINTER(OrConfig), C.c_int, C.c_int,
+                                      C.POINTER(OrResult)]),
+            "or_nvtl": (C.c_double, [P, f32p, C.c_size_t, f64p, C.c_double, C.c_double,
+                                     C.c_double]),
+            "or_score_gpu_sem": (None, [P, f32p, C.c_size_t, f64p, C.c_double, C.c_double,
+                                        C.c_int, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int32)]),
+            "or_pose_to_T34_xyz": (None, [f64p, f64p]),
+            "or_pose_to_T34_zyx": (None, [f64p, f64p]),
+            "or_eigen_sym3": (None, [f64p, f64p, f64p]),
+            "or_eigen_sym6": (None, [f64p, f64p, f64p]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, 3))
+
+
+def gauss_params(resolution=2.0, outlier_ratio=0.55):
+    d1, d2 = C.c_double(), C.c_double()
+    lib().or_gauss_params(resolution, outlier_ratio, C.byref(d1), C.byref(d2))
+    return d1.value, d2.value
+
+
+def voxel_coord(p, res):
+    out = np.zeros(3, np.int32)
+    lib().or_voxel_coord(np.ascontiguousarray(p, np.float32), res, out)
+    return out
+
+
+def morton_encode(x, y, z):
+    return int(lib().or_morton_encode(x, y, z))
+
+
+def morton_decode(code):
+    x, y, z = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    lib().or_morton_decode(code, C.byref(x), C.byref(y), C.byref(z))
+    return x.value, y.value, z.value
+
+
+def morton_codes_ref(pts, res):
+    pts = _f32(pts)
+    codes = np.zeros(len(pts), np.uint64)
+    gmin = np.zeros(3, np.float32)
+    lib().or_morton_codes_ref(pts, len(pts), res, codes, gmin)
+    return codes, gmin
+
+
+def morton_codes_coord(pts, res):
+    pts = _f32(pts)
+    codes = np.zeros(len(pts), np.uint64)
+    mn = np.zeros(3, np.int32)
+    ok = lib().or_morton_codes_coord(pts, len(pts), res, codes, mn)
+    return codes, mn, bool(ok)
+
+
+def radix_sort_pairs(keys, vals):
+    k = np.ascontiguousarray(keys, np.uint64).copy()
+    v = np.ascontiguousarray(vals, np.uint32).copy()
+    lib().or_radix_sort_pairs(k, v, len(k))
+    return k, v
+
+
+def detect_segments(sorted_codes):
+    s = np.ascontiguousarray(sorted_codes, np.uint64)
+    ids = np.zeros(max(len(s), 1), np.uint32)
+    starts = np.zeros(max(len(s), 1), np.uint32)
+    n = lib().or_detect_segments(s, len(s), ids, starts)
+    return ids[:len(s)], starts[:n], int(n)
+
+
+class Grid:
+    """Oracle voxel grid (Morton-ordered valid voxels + reference-semantics hash)."""
+
+    def __init__(self, pts, res=2.0, min_points=6, ratio=0.01, centered=True):
+        self.pts = _f32(pts)
+        self.res = float(res)
+        self.h = lib().or_grid_build(self.pts, len(self.pts), res, min_points, ratio,
+                                     1 if centered else 0)
+        if not self.h:
+            raise ValueError("voxel coordinate range exceeds 21 bits per axis")
+        n = lib().or_grid_size(self.h)
+        self.n = int(n)
+        self.coords = np.zeros((max(n, 1), 3), np.int32)
+        self.means = np.zeros((max(n, 1), 3), np.float32)
+        self.covs = np.zeros((max(n, 1), 9), np.float32)
+        self.icovs = np.zeros((max(n, 1), 9), np.float32)
+        self.counts = np.zeros(max(n, 1), np.uint32)
+        self.paxes = np.zeros((max(n, 1), 3), np.float32)
+        lib().or_grid_copy(self.h, self.coords, self.means, self.covs, self.icovs,
+                           self.counts, self.paxes)
+        for a in ("coords", "means", "covs", "icovs", "counts", "paxes"):
+            setattr(self, a, getattr(self, a)[:n])
+        self.capacity = int(lib().or_grid_hash_capacity(self.h))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_grid_free(self.h)
+            self.h = None
+
+    def lookup(self, gx, gy, gz):
+        return int(lib().or_grid_lookup(self.h, gx, gy, gz))
+
+    def query_gpu_sem(self, q, max_nb=8):
+        q = _f32(q)
+        idx = np.zeros((len(q), max_nb), np.int32)
+        cnt = np.zeros(len(q), np.int32)
+        lib().or_query_gpu_sem(self.h, q, len(q), max_nb, idx, cnt)
+        return idx, cnt
+
+    def radius_search(self, q, radius):
+        out = np.zeros(64, np.int32)
+        k = lib().or_radius_search(self.h, np.ascontiguousarray(q, np.float32), radius, out, 64)
+        return out[:min(k, 64)]
+
+    def derivatives(self, src, pose, semantics="gpu", max_nb=8, resolution=None,
+                    outlier_ratio=0.55):
+        d1, d2 = gauss_params(resolution or self.res, outlier_ratio)
+        src = _f32(src)
+        pose = np.ascontiguousarray(pose, np.float64)
+        sc = C.c_double()
+        nc = C.c_int32()
+        g = np.zeros(6)
+        H = np.zeros(36)
+        if semantics == "gpu":
+            lib().or_derivatives_gpu_sem(self.h, src, len(src), pose, d1, d2, max_nb,
+                                         C.byref(sc), g, H, C.byref(nc))
+        else:
+            lib().or_derivatives_cpu(self.h, src, len(src), pose, d1, d2, C.byref(sc), g, H,
+                                     C.byref(nc))
+        return sc.value, g, H.reshape(6, 6), nc.value
+
+    def align(self, src, pose, semantics="gpu", **cfg):
+        c = config(resolution=self.res, **cfg)
+        r = OrResult()
+        src = _f32(src)
+        pose = np.ascontiguousarray(pose, np.float64)
+        fn = lib().or_align_gpu_sem if semantics == "gpu" else lib().or_align_cpu
+        fn(self.h, src, len(src), pose, C.byref(c), C.byref(r))
+        return r.as_dict()
+
+    def align_batch(self, scans, poses, semantics="gpu", nthreads=0, **cfg):
+        c = config(resolution=self.res, **cfg)
+        scans = [_f32(s) for s in scans]
+        m = len(scans)
+        ptrs = (C.c_void_p * m)(*[s.ctypes.data for s in scans])
+        ns = (C.c_size_t * m)(*[len(s) for s in scans])
+        poses = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(m, 6))
+        res = (OrResult * m)()
+        lib().or_align_batch(self.h, ptrs, ns, poses, m, C.byref(c),
+                             0 if semantics == "gpu" else 1, nthreads, res)
+        return [r.as_dict() for r in res]
+
+    def nvtl(self, src, T34, outlier_ratio=0.55):
+        d1, d2 = gauss_params(self.res, outlier_ratio)
+        src = _f32(src)
+        return lib().or_nvtl(self.h, src, len(src), np.ascontiguousarray(T34, np.float64).ravel(),
+                             self.res, d1, d2)
+
+    def score_gpu_sem(self, src, T34, max_nb=8, outlier_ratio=0.55):
+        d1, d2 = gauss_params(self.res, outlier_ratio)
+        src = _f32(src)
+        sc = C.c_double()
+        nc = C.c_int32()
+        lib().or_score_gpu_sem(self.h, src, len(src),
+                               np.ascontiguousarray(T34, np.float64).ravel(), d1, d2, max_nb,
+                               C.byref(sc), C.byref(nc))
+        return sc.value, nc.value
+
+
+def pose_T34_xyz(pose):
+    T = np.zeros(12)
+    lib().or_pose_to_T34_xyz(np.ascontiguousarray(pose, np.float64), T)
+    return T.reshape(3, 4)
+
+
+def pose_T34_zyx(pose):
+    T = np.zeros(12)
+    lib().or_pose_to_T34_zyx(np.ascontiguousarray(pose, np.float64), T)
+    return T.reshape(3, 4)
+
+
+def newton_step_nd(g, H, min_eig=-1e-3, tol=1e-10):
+    x = np.zeros(6)
+    ok = lib().or_newton_step_nd(np.ascontiguousarray(g, np.float64),
+                                 np.ascontiguousarray(H, np.float64).ravel(), min_eig, tol, x)
+    return x if ok else None
+
+
+def jacobi_svd_solve(H, g):
+    x = np.zeros(6)
+    ok = lib().or_jacobi_svd_solve(np.ascontiguousarray(H, np.float64).ravel(),
+                                   np.ascontiguousarray(g, np.float64), x)
+    return x, bool(ok)
+
+
+def eigen_sym(a):
+    a = np.ascontiguousarray(a, np.float64)
+    n = a.shape[0]
+    ev = np.zeros(n)
+    V = np.zeros(n * n)
+    (lib().or_eigen_sym3 if n == 3 else lib().or_eigen_sym6)(a.ravel(), ev, V)
+    return ev, V.reshape(n, n)

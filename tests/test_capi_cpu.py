@@ -1,0 +1,81 @@
+"""The C-ABI library builds, loads and exports every symbol include/ndt_gb300.h declares;
+host-side logic that needs no GPU. No compute calls are made here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cuda_ndt_matcher_gb300 import capi, matcher
+from tests.conftest import has_gpu
+
+HDR = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "ndt_gb300.h")
+
+
+def declared_functions():
+    src = open(HDR).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return re.findall(r"^\s*(?:int|void\*|const char\*)\s+(ndt_\w+)\s*\(", src, flags=re.M)
+
+
+def test_header_and_binding_agree():
+    decl = declared_functions()
+    assert len(decl) >= 20
+    assert sorted(decl) == sorted(capi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = capi.load()
+    missing = [f for f in declared_functions() if not hasattr(L, f)]
+    assert not missing
+    out = os.popen(f"nm -D --defined-only {capi.lib_path()}").read()
+    for f in declared_functions():
+        assert re.search(rf"\bT {f}\b", out), f
+
+
+def test_struct_layouts():
+    assert C.sizeof(capi.Result) == 6 * 8 + 3 * 8 + 36 * 8 + 6 * 4
+    assert C.sizeof(capi.Config) == 80
+    assert C.sizeof(capi.Scan) == 8 + 8 + 48
+
+
+def test_config_defaults_mirror_reference():
+    """NdtScanMatcherConfig::default (src/ndt_cuda/src/ndt.rs:90-107) and the graph kernel's
+    neighbour cap (src/cuda_ffi/csrc/ndt_graph_common.cuh:21)."""
+    cfg = capi.default_config()
+    assert cfg.resolution == 2.0 and cfg.max_iterations == 30
+    assert cfg.trans_epsilon == 0.01 and cfg.step_size == 0.1 and cfg.outlier_ratio == 0.55
+    assert cfg.min_points_per_voxel == 6 and abs(cfg.eigenvalue_ratio - 0.01) < 1e-9
+    assert cfg.max_neighbors == 8 and cfg.min_correspondences == 10
+    assert cfg.hash_capacity_factor == 2
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device error path")
+def test_context_fails_loudly_without_device():
+    with pytest.raises(capi.NdtError) as e:
+        capi.Context()
+    assert e.value.code == -9
+
+
+def test_pose_isometry_round_trip():
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        p = np.concatenate([rng.uniform(-100, 100, 3), rng.uniform(-1.2, 1.2, 3)])
+        T = matcher.pose_vector_to_isometry(p)
+        assert np.allclose(T[:3, :3] @ T[:3, :3].T, np.eye(3), atol=1e-12)
+        q = matcher.isometry_to_pose_vector(T)
+        assert np.allclose(q, p, atol=1e-9)
+
+
+def test_isometry_matches_oracle_zyx(oracle):
+    p = np.array([1.0, 2.0, 3.0, 0.1, -0.2, 0.3])
+    assert np.allclose(matcher.pose_vector_to_isometry(p)[:3], oracle.pose_T34_zyx(p))
+
+
+def test_builder_mirrors_reference_names():
+    b = matcher.NdtScanMatcher.builder().resolution(1.0).max_iterations(10) \
+        .transformation_epsilon(0.02).step_size(0.2).outlier_ratio(0.5).use_gpu(True)
+    c = b.config
+    assert (c.resolution, c.max_iterations, c.trans_epsilon, c.step_size, c.outlier_ratio,
+            c.use_gpu) == (1.0, 10, 0.02, 0.2, 0.5, True)

@@ -1,0 +1,163 @@
+"""GPU Newton alignment vs the FP64 oracle through the C ABI.
+
+Tolerances (stated by the target): final pose within 1e-4 m and 1e-5 rad, score and NVTL
+within 1e-5 relative, identical iteration counts and convergence flags. The GPU computes
+per-point terms in FP32 (compensated warp sums, FP64 cluster reduction and solve); the
+oracle is FP64 throughout, so these bounds are the FP32-vs-FP64 error budget."""
+import numpy as np
+import pytest
+
+from cuda_ndt_matcher_gb300 import NdtScanMatcher, capi, matcher, synth
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 1e-4
+ROT_TOL = 1e-5
+REL_TOL = 1e-5
+
+
+def assert_parity(got, want, what=""):
+    dp = np.abs(got["pose"][:3] - want["pose"][:3]).max()
+    dr = np.abs(got["pose"][3:] - want["pose"][3:]).max()
+    assert got["iterations"] == want["iterations"], (what, got["iterations"], want["iterations"])
+    assert got["converged"] == want["converged"], what
+    assert got["status"] == want["status"], what
+    assert dp <= POS_TOL, (what, dp)
+    assert dr <= ROT_TOL, (what, dr)
+    for k in ("score", "nvtl", "transform_probability"):
+        ref = abs(want[k]) if want[k] != 0 else 1.0
+        assert abs(got[k] - want[k]) <= REL_TOL * ref, (what, k, got[k], want[k])
+    # correspondence counts come from f32 (GPU) vs f64 (oracle) radius tests
+    assert abs(got["num_correspondences"] - want["num_correspondences"]) <= \
+        max(2, 1e-3 * want["num_correspondences"]), what
+    hs = np.abs(want["hessian"]).max()
+    assert np.abs(got["hessian"] - want["hessian"]).max() <= 1e-4 * max(hs, 1.0), what
+
+
+@pytest.mark.parametrize("semantics", [0, 1])
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_single_alignment_parity(gpu, oracle, single_cases, semantics, cluster):
+    sem_name = "gpu" if semantics == 0 else "cpu"
+    for i, case in enumerate(single_cases):
+        ctx = capi.Context(semantics=semantics, cluster_size=cluster)
+        ctx.set_target(case.map_points)
+        got = ctx.align(case.scan, case.guess)
+        g = oracle.Grid(case.map_points, 2.0)
+        want = g.align(case.scan, case.guess, semantics=sem_name)
+        assert_parity(got, want, f"case {i} {sem_name} K={cluster}")
+
+
+def test_deterministic(gpu, single_cases):
+    case = single_cases[0]
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    a = ctx.align(case.scan, case.guess)
+    b = ctx.align(case.scan, case.guess)
+    assert np.array_equal(a["pose"], b["pose"]) and a["score"] == b["score"]
+    assert np.array_equal(a["hessian"], b["hessian"])
+
+
+def test_batch_uneven_matches_single(gpu, oracle):
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=40, scan_points=0)
+    rng = np.random.default_rng(1)
+    ks = [3, 7, 11, 19, 23, 31]
+    scans = []
+    for k in ks:
+        s = seq.scan(k)
+        m = int(rng.integers(2000, min(len(s), 40_000) + 1))
+        scans.append(s[np.sort(rng.choice(len(s), m, replace=False))])
+    poses = [seq.guess(k) for k in ks]
+    ctx = capi.Context()
+    ctx.set_target(seq.map)
+    batch = ctx.align_batch(scans, poses)
+    g = oracle.Grid(seq.map, 2.0)
+    for j, (s, p) in enumerate(zip(scans, poses)):
+        want = g.align(s, p, semantics="gpu")
+        assert_parity(batch[j], want, f"batch scan {j} ({len(s)} pts)")
+
+
+def test_multi_pose(gpu, oracle, single_cases):
+    case = single_cases[1]
+    rng = np.random.default_rng(5)
+    poses = []
+    for _ in range(12):
+        p = case.true_pose.copy()
+        p[:2] += rng.uniform(-1.0, 1.0, 2)
+        p[5] += rng.uniform(-0.1, 0.1)
+        poses.append(p)
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    res = ctx.align_multi_pose(case.scan, poses)
+    g = oracle.Grid(case.map_points, 2.0)
+    for p, r in zip(poses, res):
+        assert_parity(r, g.align(case.scan, p, semantics="gpu"), "multi-pose")
+
+
+def test_eval_batch_matches_oracle(gpu, oracle, single_cases):
+    case = single_cases[2]
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    g = oracle.Grid(case.map_points, 2.0)
+    Ts = []
+    rng = np.random.default_rng(9)
+    for _ in range(16):
+        p = case.true_pose.copy()
+        p[:2] += rng.uniform(-0.5, 0.5, 2)
+        p[3:] += rng.uniform(-0.02, 0.02, 3)
+        Ts.append(oracle.pose_T34_zyx(p))
+    nvtl, tp = ctx.eval_batch(case.scan, Ts)
+    for T, a in zip(Ts, nvtl):
+        want = g.nvtl(case.scan, T)
+        assert abs(a - want) <= REL_TOL * abs(want)
+    # transform probability: score / correspondences over every voxel within one resolution
+    d1, d2 = oracle.gauss_params(2.0, 0.55)
+    for T, t in zip(Ts, tp):
+        q = (case.scan.astype(np.float64) @ T[:, :3].T) + T[:, 3]
+        tot, cnt = 0.0, 0
+        for qq in q:
+            for v in g.radius_search(qq.astype(np.float32), 2.0):
+                x = qq - g.means[v].astype(np.float64)
+                C_ = g.icovs[v].reshape(3, 3).astype(np.float64)
+                tot += -d1 * np.exp(-d2 * (x @ C_ @ x) / 2)
+                cnt += 1
+        assert abs(t - tot / cnt) <= REL_TOL * abs(tot / cnt)
+
+
+def test_errors(gpu, single_cases):
+    ctx = capi.Context()
+    with pytest.raises(capi.NdtError) as e:
+        ctx.align(single_cases[0].scan, np.zeros(6))
+    assert e.value.code == -2
+    ctx.set_target(single_cases[0].map_points)
+    with pytest.raises(capi.NdtError) as e:
+        ctx.align(np.zeros((0, 3), np.float32), np.zeros(6))
+    assert e.value.code == -3
+    # far away from the map: no correspondences
+    r = ctx.align(single_cases[0].scan, [5000, 5000, 0, 0, 0, 0])
+    assert r["num_correspondences"] == 0 and not r["converged"] and r["status"] == 2
+    ctx.configure(semantics=1)
+    r = ctx.align(single_cases[0].scan, [5000, 5000, 0, 0, 0, 0])
+    assert r["iterations"] == 0 and r["status"] == 2 and r["nvtl"] == 0.0
+
+
+def test_reference_scenarios(gpu):
+    """Ports of src/ndt_cuda/src/ndt.rs:1490-1600 through the NdtScanMatcher mirror."""
+    m = NdtScanMatcher.builder().resolution(2.0).max_iterations(30) \
+        .transformation_epsilon(0.01).use_gpu(True).build()
+    m.set_target(synth.half_cubic_pcd() + np.array([100, 100, 0], np.float32))
+    scan = synth.voxelize_pcd(synth.half_cubic_pcd(), 1.0)
+    good = m.align(scan, matcher.translation(100, 100, 0))
+    t = good.pose[:3, 3]
+    assert abs(t[0] - 100) < 2 and abs(t[1] - 100) < 2 and abs(t[2]) < 2
+    assert good.score > 0 and good.nvtl > 0 and good.num_correspondences > 0
+    bad = m.align(scan, matcher.translation(-100, -100, 0))
+    assert good.score > bad.score or good.nvtl > bad.nvtl
+    # small offset (ndt.rs:1595-1633)
+    m2 = NdtScanMatcher.builder().resolution(2.0).use_gpu(False).build()
+    mp = synth.half_cubic_pcd()
+    m2.set_target(mp)
+    r = m2.align(synth.voxelize_pcd(mp, 1.0), matcher.translation(0.5, 0.3, 0.1))
+    assert np.linalg.norm(r.pose[:3, 3]) < 1.0
+    assert m2.evaluate_nvtl(synth.voxelize_pcd(mp, 1.0), np.eye(4)) > 0
+    res = m.align_parallel_scans([(scan, matcher.translation(100, 100, 0))] * 3)
+    assert len(res) == 3 and all(abs(x.pose[0, 3] - 100) < 2 for x in res)
