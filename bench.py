@@ -127,6 +127,12 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def phase_shares(st):
+    keys = ["cycles_points", "cycles_cluster_wait", "cycles_control", "cycles_broadcast"]
+    tot = sum(st[k] for k in keys) or 1
+    return {k.replace("cycles_", ""): round(st[k] / tot, 4) for k in keys}
+
+
 def cpu_baseline(grid_args, scans, poses, seconds, semantics="cpu"):
     """Restated reference CPU path on all host cores over a bounded sample of the scans."""
     from oracle import oracle as O
@@ -313,7 +319,10 @@ def run_ours(args):
                          "avg_launch_ms": st["align_kernel_ms"] / max(launches, 1),
                          "iterations_per_align": st["iterations"] / max(st["alignments"], 1),
                          "pairs_per_point_iter": st["correspondences"] /
-                         max(st["point_iterations"], 1)},
+                         max(st["point_iterations"], 1),
+                         "phase_cycles_share": phase_shares(st),
+                         "eigen_solves_per_align": st["eigen_solves"] /
+                         max(st["alignments"], 1)},
             "build_roofline": {"bound": "hbm", "achieved": build_bytes / (build_ms / 1e3) / 1e9,
                                "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                                "frac": build_bytes / (build_ms / 1e3) / 1e9 / pk.get("hbm_gbs"),

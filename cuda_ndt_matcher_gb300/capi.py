@@ -27,7 +27,8 @@ EXPORTS = [
     "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
     "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
-    "ndt_profile_enable", "ndt_last_error_string", "ndt_radix_sort_pairs_u64_u32",
+    "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
+    "ndt_radix_sort_pairs_u64_u32",
     "ndt_detect_segments", "ndt_morton_codes",
 ]
 
@@ -77,7 +78,10 @@ class Stats(C.Structure):
                 ("correspondences", C.c_uint64), ("align_kernel_ms", C.c_double),
                 ("score_launches", C.c_uint64), ("score_kernel_ms", C.c_double),
                 ("build_launches", C.c_uint64), ("build_ms", C.c_double),
-                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("cycles_points", C.c_uint64), ("cycles_cluster_wait", C.c_uint64),
+                ("cycles_control", C.c_uint64), ("cycles_broadcast", C.c_uint64),
+                ("eigen_solves", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -121,6 +125,8 @@ def load(build_if_missing=True):
         "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
         "ndt_stats_reset": (C.c_int, [P]),
         "ndt_profile_enable": (C.c_int, [P, C.c_int]),
+        "ndt_debug_trace": (C.c_int, [P, C.c_int]),
+        "ndt_debug_read": (C.c_int, [P, C.c_uint64, P, C.c_int32, C.POINTER(C.c_int32)]),
         "ndt_last_error_string": (C.c_char_p, []),
         "ndt_radix_sort_pairs_u64_u32": (C.c_int, [P, P, C.c_uint64, C.c_int32, C.c_int32, P,
                                                    C.POINTER(C.c_uint64), P]),
@@ -286,6 +292,15 @@ class Context:
         check(self.lib.ndt_neighbors_query(self.h, q.ctypes.data, len(q), max_nb,
                                            idx.ctypes.data, cnt.ctypes.data))
         return idx, cnt
+
+    def trace(self, enable=True):
+        check(self.lib.ndt_debug_trace(self.h, 1 if enable else 0))
+
+    def read_trace(self, index):
+        out = np.zeros((self.cfg.max_iterations, 48))
+        n = C.c_int32()
+        check(self.lib.ndt_debug_read(self.h, index, out.ctypes.data, len(out), C.byref(n)))
+        return out[:n.value]
 
     def stats(self):
         s = Stats()

@@ -3,14 +3,16 @@
 // One thread-block cluster owns one alignment for all of its iterations (graph kernels
 // K1-K5 of src/cuda_ffi/csrc/ndt_graph_kernels.cu fused into one launch; many alignments
 // of uneven size share the launch, one cluster each). Per iteration:
-//   1. every thread transforms its points (f32), finds the voxels of the 27 surrounding cells
-//      through the hash (graph_hash_query_inline semantics: fixed offset order, one voxel per
-//      cell, dist^2 <= res^2, at most max_nb), and aggregates per point
+//   1. every thread transforms its points with a compensated f32 transform (R and t as
+//      hi + lo f32 pairs, TwoProd/TwoSum, so x = (q_hi - mean) + q_lo keeps f32 precision of
+//      x itself), finds the voxels of the 27 surrounding cells through the hash
+//      (graph_hash_query_inline semantics: fixed offset order, one voxel per cell,
+//      dist^2 <= res^2 in f32, at most max_nb), and aggregates per point
 //        S = sum -d1 e,  G = sum w c,  M = sum w (C - d2 c c^T)    (w = d1 d2 e, c = C x)
-//      which it folds into 73 FP32 moment accumulators
-//        score, G, G p^T, M, M (x) p, M (x) p p^T                   (FP32 per-point terms)
-//      — the Hessian/gradient of Magnusson eqs. 6.12-6.13 factor through the pose-constant
-//      angular derivative matrices, so the 6x6 contraction happens once per iteration;
+//      (Magnusson eqs. 6.9-6.13: per-pair work is only this aggregation); the point Jacobian
+//      J_k = A_k p (A_k = dR/dtheta_k, pose constant) is contracted with M and G once per
+//      point into 34 FP32 accumulators: score, G, G p^T, M, M J, J^T M J. The second
+//      derivative term G . (d2R/dtheta_k dtheta_l) p is recovered from G p^T at the end;
 //   2. warp reduction with two-sum compensation, CTA reduction in FP64, cluster reduction in
 //      FP64 over distributed shared memory (fixed order: deterministic);
 //   3. rank 0 forms g and H in FP64, solves (Jacobi |lambda| pseudo-inverse of
@@ -29,21 +31,30 @@ namespace cg = cooperative_groups;
 
 namespace ndtgb {
 
-constexpr int NACC = 73;          // float moment accumulators
+constexpr int NACC = 34;          // f32 per-thread accumulators
 constexpr int NRED = NACC + 1;    // + correspondence count
 constexpr int MAX_WARPS = 16;
+constexpr int NFR = 52;           // per-iteration frame: R,t hi (12), R,t lo (12), A_k (27)
 
-// accumulator offsets
-constexpr int A_SC = 0, A_G = 1, A_GP = 4, A_M = 13, A_MP = 19, A_MPP = 37;
+// accumulator offsets: score, G[3], G p^T [3x3], M[6 sym], (M J_k)[a][k] [3x3], J^T M J [6]
+constexpr int A_SC = 0, A_G = 1, A_GP = 4, A_M = 13, A_HTR = 19, A_HRR = 28;
+
+struct SolveScratch {
+    double A[36], V[36], cs[6], x[6];
+    int ok, path;  // path: 0 Cholesky, 1 eigen
+};
 
 struct AlignShared {
+    SolveScratch solve;
+    unsigned long long cyc[4];  // rank 0: points+CTA reduce, cluster wait, control, broadcast
+    int n_eigen;
     double warp_part[MAX_WARPS][NRED];
     double part[NRED];
     double tot[NRED];
     double pose[6];
     double H[36];
     double g[6];
-    float Rt[12];
+    float fr[NFR];
     int done;
     // rank-0 controller state
     double best_pose[6];
@@ -131,32 +142,149 @@ __device__ void angular_mats(const double* pose, bool small, double A[3][9], dou
     }
 }
 
-// R = Rx(roll) Ry(pitch) Rz(yaw) and t, rounded to f32 for the per-point transform.
-__device__ void pose_to_Rt(const double* pose, float* Rt) {
+// Per-iteration frame for the per-point work: R = Rx(roll) Ry(pitch) Rz(yaw) and t as
+// hi/lo f32 pairs (hi = fl(v), lo = fl(v - hi)), and the angular Jacobian matrices A_k in f32.
+__device__ __noinline__ void make_frame(const double* pose, bool small, float* fr) {
     double sr, cr, sp, cp, sy, cy;
     sincos(pose[3], &sr, &cr);
     sincos(pose[4], &sp, &cp);
     sincos(pose[5], &sy, &cy);
-    Rt[0] = (float)(cp * cy);
-    Rt[1] = (float)(-cp * sy);
-    Rt[2] = (float)sp;
-    Rt[3] = (float)(sr * sp * cy + cr * sy);
-    Rt[4] = (float)(cr * cy - sr * sp * sy);
-    Rt[5] = (float)(-sr * cp);
-    Rt[6] = (float)(sr * sy - cr * sp * cy);
-    Rt[7] = (float)(cr * sp * sy + sr * cy);
-    Rt[8] = (float)(cr * cp);
-    Rt[9] = (float)pose[0];
-    Rt[10] = (float)pose[1];
-    Rt[11] = (float)pose[2];
+    double v[12] = {cp * cy, -cp * sy, sp,
+                    sr * sp * cy + cr * sy, cr * cy - sr * sp * sy, -sr * cp,
+                    sr * sy - cr * sp * cy, cr * sp * sy + sr * cy, cr * cp,
+                    pose[0], pose[1], pose[2]};
+    for (int i = 0; i < 12; ++i) {
+        float h = (float)v[i];
+        fr[i] = h;
+        fr[12 + i] = (float)(v[i] - (double)h);
+    }
+    double A[3][9], B[6][9];
+    angular_mats(pose, small, A, B);
+    for (int k = 0; k < 3; ++k)
+        for (int q = 0; q < 9; ++q) fr[24 + 9 * k + q] = (float)A[k][q];
 }
 
 // ------------------------------------------------------------------------------------
-// 6x6 solvers (FP64, one thread)
+// 6x6 solvers (FP64)
 // ------------------------------------------------------------------------------------
-// Cholesky of a symmetric matrix; false if a pivot is not positive or the pivot ratio
-// falls below 1e-6 (then the caller takes the eigen path).
-__device__ bool chol6(const double* M, double* L) {
+// Round-robin schedule of the 15 index pairs of a 6x6 matrix in 5 rounds of 3 disjoint
+// pairs (circle method), so the three rotations of a round commute and run in parallel.
+__constant__ int8_t RR_PAIRS[5][3][2] = {
+    {{0, 1}, {2, 5}, {3, 4}}, {{0, 2}, {1, 3}, {4, 5}}, {{0, 3}, {2, 4}, {1, 5}},
+    {{0, 4}, {3, 5}, {1, 2}}, {{0, 5}, {1, 4}, {2, 3}}};
+
+// Warp-parallel Jacobi eigen-decomposition of the symmetric 6x6 in `A` (FP64, shared memory):
+// A becomes diagonal, V accumulates the rotations. Rotation angles and stopping rules follow
+// the reference's jacobi_svd_6x6.cuh:135-210 (tau formula, skip |a_pq| < 1e-15, stop when
+// 2 sum(offdiag^2) < 1e-28 sum(diag^2), <= 30 sweeps); the sweep order is parallel
+// round-robin instead of cyclic-by-row, which changes results only by FP64 rounding. Every
+// FP64 instruction does the work of up to 32 lanes (the FP64 pipe is narrow on this GPU).
+__device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int lane) {
+    if (lane < 36 - 32) V[32 + lane] = ((32 + lane) % 7 == 0) ? 1.0 : 0.0;
+    V[lane] = (lane % 7 == 0) ? 1.0 : 0.0;
+    __syncwarp();
+    int sweeps = 0;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        // convergence test (lane i < 6 owns diagonal i; lanes < 15 own one off-diagonal pair)
+        double dg = lane < 6 ? A[lane * 7] * A[lane * 7] : 0.0;
+        double off = 0.0;
+        if (lane < 15) {
+            int p = RR_PAIRS[lane / 3][lane % 3][0], q = RR_PAIRS[lane / 3][lane % 3][1];
+            off = A[p * 6 + q] * A[p * 6 + q];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dg += __shfl_xor_sync(0xffffffffu, dg, o);
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+        }
+        if (2.0 * off < 1e-28 * dg) break;
+        sweeps++;
+        for (int r = 0; r < 5; ++r) {
+            if (lane < 3) {
+                int p = RR_PAIRS[r][lane][0], q = RR_PAIRS[r][lane][1];
+                double apq = A[p * 6 + q];
+                double c = 1.0, sn = 0.0;
+                if (fabs(apq) >= 1e-15) {
+                    double tau = (A[q * 6 + q] - A[p * 6 + p]) / (2.0 * apq);
+                    double t = tau >= 0.0 ? 1.0 / (tau + sqrt(tau * tau + 1.0))
+                                          : -1.0 / (-tau + sqrt(tau * tau + 1.0));
+                    c = 1.0 / sqrt(t * t + 1.0);
+                    sn = t * c;
+                }
+                cs[2 * lane] = c;
+                cs[2 * lane + 1] = sn;
+            }
+            __syncwarp();
+            // rotation of index i: partner j and coefficients (own, partner) of row i of J^T
+            // (p: c, -s; q: s, c)
+            double nA0 = 0.0, nV0 = 0.0, nV1 = 0.0;
+            int ai = 0, aj = 0;
+            if (lane < 21) {  // upper-triangle entry (ai <= aj)
+                int t = lane;
+                ai = 0;
+                while (t >= 6 - ai) {
+                    t -= 6 - ai;
+                    ++ai;
+                }
+                aj = ai + t;
+            }
+            auto coef = [&](int i, int& partner, double& cown, double& cpart) {
+                for (int k = 0; k < 3; ++k) {
+                    int p = RR_PAIRS[r][k][0], q = RR_PAIRS[r][k][1];
+                    if (i == p) {
+                        partner = q;
+                        cown = cs[2 * k];
+                        cpart = -cs[2 * k + 1];
+                    } else if (i == q) {
+                        partner = p;
+                        cown = cs[2 * k];
+                        cpart = cs[2 * k + 1];
+                    }
+                }
+            };
+            if (lane < 21) {
+                int pi, pj;
+                double ci, si, cj, sj;
+                coef(ai, pi, ci, si);
+                coef(aj, pj, cj, sj);
+                if (pi == aj) {  // rotated pair itself: zeroed by construction
+                    nA0 = 0.0;
+                } else {
+                    double a_ij = A[ai * 6 + aj], a_ipj = A[pi * 6 + aj];
+                    double a_ijp = A[ai * 6 + pj], a_ipjp = A[pi * 6 + pj];
+                    nA0 = ci * (cj * a_ij + sj * a_ijp) + si * (cj * a_ipj + sj * a_ipjp);
+                }
+            }
+            // V' = V J: column j mixes with its partner
+            {
+                int vi = lane / 6, vj = lane % 6, pj;
+                double cj, sj;
+                coef(vj, pj, cj, sj);
+                nV0 = cj * V[vi * 6 + vj] + sj * V[vi * 6 + pj];
+                if (lane < 4) {
+                    int e = 32 + lane;
+                    int wi = e / 6, wj = e % 6, pw;
+                    double cw, sw;
+                    coef(wj, pw, cw, sw);
+                    nV1 = cw * V[wi * 6 + wj] + sw * V[wi * 6 + pw];
+                }
+            }
+            __syncwarp();
+            if (lane < 21) {
+                A[ai * 6 + aj] = nA0;
+                A[aj * 6 + ai] = nA0;
+            }
+            V[lane] = nV0;
+            if (lane < 4) V[32 + lane] = nV1;
+            __syncwarp();
+        }
+    }
+    return sweeps;
+}
+
+// Cholesky of a symmetric matrix (one lane); false if a pivot is not positive or the pivot
+// ratio falls below 1e-6 (then the caller takes the eigen path).
+__device__ __noinline__ bool chol6(const double* M, double* L) {
     double dmin = 1e300, dmax = 0.0;
     for (int i = 0; i < 6; ++i) {
         for (int j = 0; j <= i; ++j) {
@@ -189,120 +317,83 @@ __device__ void chol6_solve(const double* L, const double* b, double* x) {
     }
 }
 
-// Cyclic Jacobi eigen-decomposition with the reference's stopping rules
-// (jacobi_svd_6x6.cuh:135-210): A becomes diagonal, V accumulates the rotations.
-__device__ void jacobi6(double* A, double* V) {
-    for (int i = 0; i < 36; ++i) V[i] = (i % 7 == 0) ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 30; ++sweep) {
-        double off = 0.0, dg = 0.0;
-        for (int i = 0; i < 6; ++i) {
-            dg += A[i * 6 + i] * A[i * 6 + i];
-            for (int j = i + 1; j < 6; ++j) off += A[i * 6 + j] * A[i * 6 + j];
-        }
-        off *= 2.0;
-        if (off < 1e-28 * dg) break;
-        for (int p = 0; p < 5; ++p) {
-            for (int q = p + 1; q < 6; ++q) {
-                double apq = A[p * 6 + q];
-                if (fabs(apq) < 1e-15) continue;
-                double app = A[p * 6 + p], aqq = A[q * 6 + q];
-                double tau = (aqq - app) / (2.0 * apq);
-                double t = tau >= 0.0 ? 1.0 / (tau + sqrt(tau * tau + 1.0))
-                                      : -1.0 / (-tau + sqrt(tau * tau + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                double c2 = c * c, s2 = s * s, cs = c * s;
-                A[p * 6 + p] = c2 * app + s2 * aqq - 2.0 * cs * apq;
-                A[q * 6 + q] = s2 * app + c2 * aqq + 2.0 * cs * apq;
-                A[p * 6 + q] = 0.0;
-                A[q * 6 + p] = 0.0;
-                for (int k = 0; k < 6; ++k) {
-                    if (k == p || k == q) continue;
-                    double apk = A[p * 6 + k], aqk = A[q * 6 + k];
-                    double np = c * apk - s * aqk, nq = s * apk + c * aqk;
-                    A[p * 6 + k] = np;
-                    A[k * 6 + p] = np;
-                    A[q * 6 + k] = nq;
-                    A[k * 6 + q] = nq;
-                }
-                for (int i = 0; i < 6; ++i) {
-                    double vip = V[i * 6 + p], viq = V[i * 6 + q];
-                    V[i * 6 + p] = c * vip - s * viq;
-                    V[i * 6 + q] = s * vip + c * viq;
-                }
+// Newton step for both semantics; all 32 lanes of one warp call it, result in S.x / S.ok.
+//  graph (K3): x = V diag(1/|lambda|) V^T (-g), |lambda| > max(1e-10 max|lambda|, 1e-15)
+//              (jacobi_svd_solve_6x6_f64); definite H: x = (sH)^-1 (-g), s = sign
+//  cpu       : newton_step_negative_definite(g, H, -1e-3, 1e-10) (newton.rs:160-176)
+template <bool CPU_SEM>
+__device__ __noinline__ void solve_warp(const double* H, const double* g, SolveScratch& S,
+                                        int lane) {
+    if (lane == 0) {
+        double M[36], L[36];
+        S.ok = 0;
+        S.path = 1;
+        for (int sgn = 1; sgn >= -1; sgn -= 2) {
+            if (CPU_SEM && sgn == 1) continue;  // only the negative-definite fast path
+            for (int i = 0; i < 36; ++i) M[i] = sgn * H[i];
+            if (chol6(M, L)) {
+                double b[6];
+                for (int i = 0; i < 6; ++i) b[i] = CPU_SEM ? g[i] : -g[i];
+                chol6_solve(L, b, S.x);
+                S.ok = 1;
+                S.path = 0;
+                break;
             }
         }
     }
-}
-
-// x = V f(lambda) V^T (-g) with f(l) = 1/|l| (graph semantics) or 1/l (CPU semantics)
-__device__ int eig_apply(const double* A, const double* V, const double* g, bool use_abs,
-                         double thr, double* x) {
-    double z[6];
-    int nz = 0;
-    for (int i = 0; i < 6; ++i) {
-        double y = 0.0;
-        for (int j = 0; j < 6; ++j) y += V[j * 6 + i] * (-g[j]);
-        double l = A[i * 6 + i];
-        double al = fabs(l);
-        if (al > thr) {
-            z[i] = y / (use_abs ? al : l);
-            nz++;
+    __syncwarp();
+    if (S.path == 0) return;
+    S.A[lane] = H[lane];
+    if (lane < 4) S.A[32 + lane] = H[32 + lane];
+    __syncwarp();
+    jacobi6_warp(S.A, S.V, S.cs, lane);
+    if (lane == 0) {
+        double lam[6];
+        for (int i = 0; i < 6; ++i) lam[i] = S.A[i * 7];
+        double thr;
+        bool use_abs;
+        if (!CPU_SEM) {
+            double mx = 0.0;
+            for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(lam[i]));
+            thr = fmax(1e-10 * mx, 1e-15);
+            use_abs = true;
         } else {
-            z[i] = 0.0;
+            bool nd = true;
+            for (int i = 0; i < 6; ++i)
+                if (!(lam[i] < 0.0)) nd = false;
+            if (!nd)
+                for (int i = 0; i < 6; ++i)
+                    if (lam[i] > -1e-3) lam[i] = -1e-3;
+            double mx = 0.0;
+            for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(lam[i]));
+            thr = 1e-10;
+            use_abs = false;
+            if (mx < 1e-10) {
+                S.ok = 0;
+                return;
+            }
         }
-    }
-    for (int i = 0; i < 6; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < 6; ++j) s += V[i * 6 + j] * z[j];
-        x[i] = s;
-    }
-    return nz;
-}
-
-// Graph semantics (K3): pseudo-inverse with |lambda|, relative cut 1e-10 (min 1e-15).
-__device__ bool solve_graph(const double* H, const double* g, double* x) {
-    double M[36], L[36];
-    // definite and well conditioned: the pseudo-inverse is (sH)^-1 (-g), s = sign
-    for (int sgn = 1; sgn >= -1; sgn -= 2) {
-        for (int i = 0; i < 36; ++i) M[i] = sgn * H[i];
-        if (chol6(M, L)) {
-            double b[6];
-            for (int i = 0; i < 6; ++i) b[i] = -g[i];
-            chol6_solve(L, b, x);
-            return true;
+        double z[6];
+        int nz = 0;
+        for (int i = 0; i < 6; ++i) {
+            double y = 0.0;
+            for (int j = 0; j < 6; ++j) y += S.V[j * 6 + i] * (-g[j]);
+            double al = fabs(lam[i]);
+            if (al > thr) {
+                z[i] = y / (use_abs ? al : lam[i]);
+                nz++;
+            } else {
+                z[i] = 0.0;
+            }
         }
+        for (int i = 0; i < 6; ++i) {
+            double s = 0.0;
+            for (int j = 0; j < 6; ++j) s += S.V[i * 6 + j] * z[j];
+            S.x[i] = s;
+        }
+        S.ok = CPU_SEM ? 1 : (nz > 0);
     }
-    double A[36], V[36];
-    for (int i = 0; i < 36; ++i) A[i] = H[i];
-    jacobi6(A, V);
-    double mx = 0.0;
-    for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(A[i * 6 + i]));
-    double thr = fmax(1e-10 * mx, 1e-15);
-    return eig_apply(A, V, g, true, thr, x) > 0;
-}
-
-// CPU semantics: newton_step_negative_definite(g, H, -1e-3, 1e-10).
-__device__ bool solve_cpu(const double* H, const double* g, double* x) {
-    double M[36], L[36];
-    for (int i = 0; i < 36; ++i) M[i] = -H[i];
-    if (chol6(M, L)) {  // H negative definite: x = H^-1 (-g) = (-H)^-1 g
-        chol6_solve(L, g, x);
-        return true;
-    }
-    double A[36], V[36];
-    for (int i = 0; i < 36; ++i) A[i] = H[i];
-    jacobi6(A, V);
-    bool nd = true;
-    for (int i = 0; i < 6; ++i)
-        if (!(A[i * 6 + i] < 0.0)) nd = false;
-    if (!nd)
-        for (int i = 0; i < 6; ++i)
-            if (A[i * 6 + i] > -1e-3) A[i * 6 + i] = -1e-3;
-    double mx = 0.0;
-    for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(A[i * 6 + i]));
-    if (mx < 1e-10) return false;
-    eig_apply(A, V, g, false, 1e-10, x);
-    return true;
+    __syncwarp();
 }
 
 // ------------------------------------------------------------------------------------
@@ -310,48 +401,102 @@ __device__ bool solve_cpu(const double* H, const double* g, double* x) {
 // ------------------------------------------------------------------------------------
 template <bool CPU_SEM>
 __device__ __forceinline__ void point_terms(const MapView& m, float px, float py, float pz,
-                                            const float* Rt, int max_nb, float d1f, float d2f,
-                                            float* acc, int& ncorr) {
-    float qx = fmaf(Rt[0], px, fmaf(Rt[1], py, fmaf(Rt[2], pz, Rt[9])));
-    float qy = fmaf(Rt[3], px, fmaf(Rt[4], py, fmaf(Rt[5], pz, Rt[10])));
-    float qz = fmaf(Rt[6], px, fmaf(Rt[7], py, fmaf(Rt[8], pz, Rt[11])));
-    int32_t gx = (int32_t)floorf(__fmul_rn(qx, m.inv_res));
-    int32_t gy = (int32_t)floorf(__fmul_rn(qy, m.inv_res));
-    int32_t gz = (int32_t)floorf(__fmul_rn(qz, m.inv_res));
+                                            const float* fr, int max_nb, float d1f, float d2f,
+                                            float* acc, int& ncorr, uint32_t* nbl,
+                                            int nbl_stride) {
+    const float pv[3] = {px, py, pz};
+    float qh[3], ql[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float hi = fr[9 + i], lo = fr[21 + i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float r = fr[3 * i + j];
+            float ph = r * pv[j];
+            float pl = fmaf(r, pv[j], -ph);      // exact product error
+            float s = hi + ph;                   // TwoSum(hi, ph)
+            float bb = s - hi;
+            float e = (hi - (s - bb)) + (ph - bb);
+            hi = s;
+            lo += e + pl + fr[12 + 3 * i + j] * pv[j];
+        }
+        float s = hi + lo;                       // FastTwoSum renormalisation
+        ql[i] = lo - (s - hi);
+        qh[i] = s;
+    }
+    int32_t gc[3];
+    cell_of_sum(m, qh, ql, gc);
+    // ---- search: the 27 cells in the reference's order (dx outer, dy, dz inner); the slots
+    // of the accepted voxels (centroid within one resolution, at most max_nb) are listed in
+    // shared memory, so the search runs with all lanes busy and the pair work below runs once
+    // per listed voxel rather than once per cell
+    int cnt = 0;
+    const uint32_t bxy = m.bits[0] + m.bits[1];
+    const uint32_t lz0 = (uint32_t)(gc[2] - m.min_cell[2]);
+#pragma unroll 1
+    for (int c9 = 0; c9 < 9; ++c9) {
+        if (cnt >= max_nb) break;
+        const int dx = c9 / 3 - 1, dy = c9 % 3 - 1;
+        const uint32_t lx = (uint32_t)(gc[0] + dx - m.min_cell[0]);
+        const uint32_t ly = (uint32_t)(gc[1] + dy - m.min_cell[1]);
+        if ((lx >> m.bits[0]) | (ly >> m.bits[1])) continue;
+        const uint32_t kxy = lx | (ly << m.bits[0]);
+        uint4 sv[3];
+        uint32_t key[3], home[3];
+        bool inb[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {  // the column's three home slots, loaded together
+            const uint32_t lz = lz0 + (uint32_t)(k - 1);
+            inb[k] = (lz >> m.bits[2]) == 0u;
+            key[k] = kxy | (lz << bxy);
+            home[k] = mix32(key[k]) & m.mask;
+            sv[k] = inb[k] ? __ldg(m.slots + home[k]) : make_uint4(EMPTY_KEY, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (cnt >= max_nb) break;
+            if (!inb[k]) continue;
+            uint4 v = sv[k];
+            int32_t s = (int32_t)home[k];
+            if (v.x != key[k]) {
+                if (v.x == EMPTY_KEY) continue;
+                s = probe_next(m, key[k], home[k], &v);
+                if (s < 0) continue;
+            }
+            const float e0 = (qh[0] - __uint_as_float(v.y)) + ql[0];
+            const float e1 = (qh[1] - __uint_as_float(v.z)) + ql[1];
+            const float e2 = (qh[2] - __uint_as_float(v.w)) + ql[2];
+            if (fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2) continue;
+            nbl[cnt * nbl_stride] = (uint32_t)s;
+            cnt++;
+        }
+    }
+    if (cnt == 0) return;
+    // ---- pairs: S, G, M aggregated over the listed voxels
     float S = 0.f, G0 = 0.f, G1 = 0.f, G2 = 0.f;
     float M0 = 0.f, M1 = 0.f, M2 = 0.f, M3 = 0.f, M4 = 0.f, M5 = 0.f;
-    int cnt = 0;
     const float d1d2 = d1f * d2f;
 #pragma unroll 1
-    for (int c = 0; c < 27; ++c) {
-        if (cnt >= max_nb) break;
-        int dx, dy, dz;
-        offset27(c, dx, dy, dz);
-        int32_t cx = gx + dx, cy = gy + dy, cz = gz + dz;
-        uint32_t key = local_key(m, cx, cy, cz);
-        if (key == EMPTY_KEY) continue;
-        uint32_t home = (uint32_t)fmix64(pack21(cx, cy, cz)) & m.mask;
-        uint4 sv;
-        int32_t s = probe(m, key, home, &sv);
-        if (s < 0) continue;
-        float mx = __uint_as_float(sv.y), my = __uint_as_float(sv.z), mz = __uint_as_float(sv.w);
-        if (dist2_rn(qx, qy, qz, mx, my, mz) > m.r2) continue;
-        cnt++;
-        float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
-        float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
+    for (int j = 0; j < cnt; ++j) {
+        const uint32_t s = nbl[j * nbl_stride];
+        const uint4 v = __ldg(m.slots + s);
+        const float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
+        const float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
+        const float x0 = (qh[0] - __uint_as_float(v.y)) + ql[0];
+        const float x1 = (qh[1] - __uint_as_float(v.z)) + ql[1];
+        const float x2 = (qh[2] - __uint_as_float(v.w)) + ql[2];
         // C = [[ca.x ca.y ca.z] [ca.y ca.w cb.x] [ca.z cb.x cb.y]]
-        float x0 = qx - mx, x1 = qy - my, x2 = qz - mz;
-        float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
-        float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
-        float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
-        float sq = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
-        float e = expf(-0.5f * d2f * sq);
+        const float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
+        const float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
+        const float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
+        const float sq = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
+        const float e = expf(-0.5f * d2f * sq);
         if (CPU_SEM) {
-            float wn = d2f * e;  // compute_derivative_single: zero unless d2*e in [0, 1]
+            const float wn = d2f * e;  // compute_derivative_single: zero unless d2*e in [0,1]
             if (!(wn >= 0.f && wn <= 1.f)) continue;
         }
-        float w = d1d2 * e;
-        float wd = w * d2f;
+        const float w = d1d2 * e;
+        const float wd = w * d2f;
         S = fmaf(-d1f, e, S);
         G0 = fmaf(w, c0, G0);
         G1 = fmaf(w, c1, G1);
@@ -365,38 +510,51 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
     }
     if (cnt == 0) return;
     ncorr += cnt;
-    const float p[3] = {px, py, pz};
     const float G[3] = {G0, G1, G2};
-    const float M[6] = {M0, M1, M2, M3, M4, M5};
-    const float pp[6] = {px * px, px * py, px * pz, py * py, py * pz, pz * pz};
+    const float Ms[3][3] = {{M0, M1, M2}, {M1, M3, M4}, {M2, M4, M5}};
     acc[A_SC] += S;
+    // J_k = A_k p, MJ_k = M J_k
+    float J[3][3], MJ[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            J[k][a] = fmaf(fr[24 + 9 * k + 3 * a], pv[0],
+                           fmaf(fr[25 + 9 * k + 3 * a], pv[1], fr[26 + 9 * k + 3 * a] * pv[2]));
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            MJ[k][a] = fmaf(Ms[a][0], J[k][0], fmaf(Ms[a][1], J[k][1], Ms[a][2] * J[k][2]));
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         acc[A_G + a] += G[a];
 #pragma unroll
-        for (int b = 0; b < 3; ++b) acc[A_GP + 3 * a + b] = fmaf(G[a], p[b], acc[A_GP + 3 * a + b]);
+        for (int b = 0; b < 3; ++b) acc[A_GP + 3 * a + b] = fmaf(G[a], pv[b], acc[A_GP + 3 * a + b]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc[A_HTR + 3 * a + k] += MJ[k][a];
     }
+    acc[A_M + 0] += M0;
+    acc[A_M + 1] += M1;
+    acc[A_M + 2] += M2;
+    acc[A_M + 3] += M3;
+    acc[A_M + 4] += M4;
+    acc[A_M + 5] += M5;
+    int kl = 0;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        acc[A_M + k] += M[k];
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) acc[A_MP + 3 * k + c] = fmaf(M[k], p[c], acc[A_MP + 3 * k + c]);
-#pragma unroll
-        for (int j = 0; j < 6; ++j)
-            acc[A_MPP + 6 * k + j] = fmaf(M[k], pp[j], acc[A_MPP + 6 * k + j]);
-    }
+        for (int l = k; l < 3; ++l, ++kl)
+            acc[A_HRR + kl] = fmaf(J[k][0], MJ[l][0],
+                                   fmaf(J[k][1], MJ[l][1], fmaf(J[k][2], MJ[l][2], acc[A_HRR + kl])));
 }
 
-// g (6) and H (6x6) from the reduced moments (FP64), lanes of one warp share the work.
-__device__ void finalize_gH(const double* tot, const double* pose, bool small, double* g,
+// g (6) and H (6x6) in FP64 from the reduced accumulators; lanes of one warp share the work.
+__device__ __noinline__ void finalize_gH(const double* tot, const double* pose, bool small, double* g,
                             double* H, int lane) {
     double A[3][9], B[6][9];
     angular_mats(pose, small, A, B);
     const double* GP = tot + A_GP;
-    const double* MT = tot + A_M;
-    const double* MP = tot + A_MP;
-    const double* MPP = tot + A_MPP;
-    // lanes 0..5: gradient; lanes 0..20: one upper-triangle Hessian entry each
     if (lane < 6) {
         double v;
         if (lane < 3) {
@@ -414,29 +572,15 @@ __device__ void finalize_gH(const double* tot, const double* pose, bool small, d
             ++i;
         }
         j += i;
-        double v = 0.0;
+        double v;
         if (j < 3) {
-            v = MT[sym3(i, j)];
+            v = tot[A_M + sym3(i, j)];
         } else if (i < 3) {
-            const double* Ak = A[j - 3];
-            for (int b = 0; b < 3; ++b)
-                for (int c = 0; c < 3; ++c) v += Ak[b * 3 + c] * MP[3 * sym3(i, b) + c];
+            v = tot[A_HTR + 3 * i + (j - 3)];
         } else {
             int k = i - 3, l = j - 3;
-            const double* Ak = A[k];
-            const double* Al = A[l];
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) {
-                    int ab = sym3(a, b);
-                    for (int c = 0; c < 3; ++c) {
-                        double akac = Ak[a * 3 + c];
-                        if (akac == 0.0) continue;
-                        for (int d = 0; d < 3; ++d)
-                            v += akac * Al[b * 3 + d] * MPP[6 * ab + sym3(c, d)];
-                    }
-                }
-            // pair index of (k, l), k <= l: rr rp ry pp py yy
-            int kl = (k == 0) ? l : (k == 1 ? 2 + l : 5);
+            int kl = (k == 0) ? l : (k == 1 ? 2 + l : 5);  // rr rp ry pp py yy
+            v = tot[A_HRR + kl];
             for (int q = 0; q < 9; ++q) v += B[kl][q] * GP[q];
         }
         H[i * 6 + j] = v;
@@ -481,14 +625,15 @@ __device__ void write_out(AlignOut& o, const double* pose, double score, const d
 
 // One step of the controller (rank 0, lane 0). Returns 1 when the alignment is finished.
 template <bool CPU_SEM>
-__device__ int control_step(const AlignParams& P, AlignShared& sh, const AlignJob& job,
+__device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, const AlignJob& job,
                             AlignOut& o, int it, double score, int ncorr) {
     double* pose = sh.pose;
     const double* g = sh.g;
     const double* H = sh.H;
     if (!CPU_SEM) {
         double x[6];
-        if (!solve_graph(H, g, x))
+        for (int i = 0; i < 6; ++i) x[i] = sh.solve.x[i];
+        if (!sh.solve.ok)
             for (int i = 0; i < 6; ++i) x[i] = -g[i] * 1e-4;
         double dphi = 0.0;
         for (int i = 0; i < 6; ++i) dphi += g[i] * x[i];
@@ -527,7 +672,8 @@ __device__ int control_step(const AlignParams& P, AlignShared& sh, const AlignJo
         for (int i = 0; i < 6; ++i) sh.best_pose[i] = pose[i];
     }
     double x[6];
-    if (!solve_cpu(H, g, x)) {
+    for (int i = 0; i < 6; ++i) x[i] = sh.solve.x[i];
+    if (!sh.solve.ok) {
         write_out(o, sh.best_pose, sh.best_score, sh.last_H, it, 0, sh.last_corr, sh.max_osc,
                   NDT_STATUS_SINGULAR_HESSIAN);
         return 1;
@@ -558,10 +704,11 @@ __device__ int control_step(const AlignParams& P, AlignShared& sh, const AlignJo
 }
 
 template <int THREADS, bool CPU_SEM>
-__global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
+__global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 128))
     k_ndt_align(const AlignParams P) {
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
+    extern __shared__ uint32_t nbl_smem[];  // [max_nb][THREADS] accepted slots per thread
     cg::cluster_group cluster = cg::this_cluster();
     const int K = P.cluster;
     const int rank = (int)cluster.block_rank();
@@ -584,15 +731,18 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
         sh.osc = sh.max_osc = 0;
         for (int i = 0; i < 36; ++i) sh.last_H[i] = 0.0;
         sh.done = 0;
-        pose_to_Rt(sh.pose, sh.Rt);
+        make_frame(sh.pose, CPU_SEM, sh.fr);
     }
     __syncthreads();
 
     uint64_t point_iters = 0, corr_total = 0;
+    if (tid == 0) {
+        sh.cyc[0] = sh.cyc[1] = sh.cyc[2] = sh.cyc[3] = 0ull;
+        sh.n_eigen = 0;
+    }
+    unsigned long long t0 = clock64();
     for (int it = 0;; ++it) {
-        float Rt[12];
-#pragma unroll
-        for (int i = 0; i < 12; ++i) Rt[i] = sh.Rt[i];
+        const float* fr = sh.fr;
         float acc[NACC];
 #pragma unroll
         for (int i = 0; i < NACC; ++i) acc[i] = 0.f;
@@ -601,7 +751,8 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
             float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                   pz = __ldg(pts + 3 * (size_t)i + 2);
             if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-            point_terms<CPU_SEM>(m, px, py, pz, Rt, P.max_nb, P.d1f, P.d2f, acc, nc);
+            point_terms<CPU_SEM>(m, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, nc,
+                                 nbl_smem + tid, THREADS);
         }
         // warp: two-sum compensated butterfly, then FP64 (fully unrolled: acc[] stays in
         // registers)
@@ -629,7 +780,9 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
             for (int w = 0; w < NW; ++w) s += sh.warp_part[w][k];
             sh.part[k] = s;
         }
+        unsigned long long t1 = clock64();
         cluster.sync();  // partials of every CTA of the cluster are ready
+        unsigned long long t2 = clock64();
         if (rank == 0) {
             for (int k = tid; k < NRED; k += THREADS) {
                 double s = 0.0;
@@ -643,7 +796,25 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
             if (warp == 0) {
                 finalize_gH(sh.tot, sh.pose, CPU_SEM, sh.g, sh.H, lane);
                 __syncwarp();
+                solve_warp<CPU_SEM>(sh.H, sh.g, sh.solve, lane);
                 if (lane == 0) {
+                    sh.n_eigen += sh.solve.path;
+                    if (P.trace && it < P.max_iter) {  // per-iteration record (opt-in)
+                        double* t = P.trace + ((size_t)jid * P.max_iter + it) * TRACE_REC;
+                        t[0] = it;
+                        t[1] = sh.tot[A_SC];
+                        t[2] = sh.tot[NACC];
+                        for (int i = 0; i < 6; ++i) {
+                            t[3 + i] = sh.pose[i];
+                            t[9 + i] = sh.g[i];
+                            t[36 + i] = sh.solve.x[i];
+                        }
+                        int u = 0;
+                        for (int i = 0; i < 6; ++i)
+                            for (int j = i; j < 6; ++j) t[15 + u++] = sh.H[i * 6 + j];
+                        t[42] = sh.solve.path;
+                        t[43] = sh.solve.ok;
+                    }
                     int ncorr = (int)sh.tot[NACC];
                     point_iters += n;
                     corr_total += (uint64_t)ncorr;
@@ -653,20 +824,34 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1))
                         o.point_iters = point_iters;
                         o.corr_total = corr_total;
                     }
-                    pose_to_Rt(sh.pose, sh.Rt);
+                    make_frame(sh.pose, CPU_SEM, sh.fr);
                     sh.done = done;
                 }
                 __syncwarp();
                 if (lane > 0 && lane < K) {
                     AlignShared* rs = cluster.map_shared_rank(&sh, lane);
                     for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
-                    for (int i = 0; i < 12; ++i) rs->Rt[i] = sh.Rt[i];
+                    for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
                     rs->done = sh.done;
                 }
             }
         }
+        unsigned long long t3 = clock64();
         cluster.sync();  // next pose (or done) visible in every CTA
+        unsigned long long t4 = clock64();
+        if (rank == 0 && tid == 0) {
+            sh.cyc[0] += t1 - t0;
+            sh.cyc[1] += t2 - t1;
+            sh.cyc[2] += t3 - t2;
+            sh.cyc[3] += t4 - t3;
+        }
+        t0 = t4;
         if (sh.done) break;
+    }
+    if (rank == 0 && tid == 0) {
+        AlignOut& o = P.out[jid];
+        for (int i = 0; i < 4; ++i) o.cycles[i] = sh.cyc[i];
+        o.n_eigen = sh.n_eigen;
     }
 }
 
@@ -675,7 +860,7 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.num_jobs * K, 1, 1);
     cfg.blockDim = dim3(T, 1, 1);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = (size_t)T * p.max_nb * sizeof(uint32_t);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -686,11 +871,15 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     cfg.numAttrs = 1;
     cudaError_t e;
     if (p.semantics == NDT_SEMANTICS_CPU) {
+        cudaFuncSetAttribute(k_ndt_align<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cfg.dynamicSmemBytes);
         if (K > 8)
             cudaFuncSetAttribute(k_ndt_align<T, true>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         e = cudaLaunchKernelEx(&cfg, k_ndt_align<T, true>, p);
     } else {
+        cudaFuncSetAttribute(k_ndt_align<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cfg.dynamicSmemBytes);
         if (K > 8)
             cudaFuncSetAttribute(k_ndt_align<T, false>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

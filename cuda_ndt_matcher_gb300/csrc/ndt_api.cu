@@ -95,6 +95,11 @@ struct ndt_ctx {
     double d1 = 0, d2 = 0;
     ndt_stats stats{};
     bool profile = false;
+    bool trace = false;
+    DevBuf d_trace;
+    std::vector<double> h_trace;       // last call's records, by job order
+    std::vector<uint32_t> trace_slot;  // job index -> caller's result index
+    int trace_iters = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
 };
 
@@ -201,7 +206,7 @@ int ndt_ctx_destroy(ndt_ctx* c) {
                       &c->bs.seg_ids, &c->bs.seg_starts, &c->bs.seg_valid, &c->bs.seg_rank,
                       &c->bs.seg_rec, &c->bs.small, &c->d_in, &c->d_jobs, &c->d_aout,
                       &c->d_sjobs, &c->d_sout, &c->d_part, &c->d_status, &c->d_q, &c->d_qidx,
-                      &c->d_qcnt})
+                      &c->d_qcnt, &c->d_trace})
         dev_free(*b);
     for (PinBuf* b : {&c->h_pts, &c->h_jobs, &c->h_aout, &c->h_sjobs, &c->h_sout, &c->h_misc})
         pin_free(*b);
@@ -237,6 +242,33 @@ int ndt_profile_enable(ndt_ctx* c, int enable) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
     c->profile = enable != 0;
     return NDT_OK;
+}
+
+int ndt_debug_trace(ndt_ctx* c, int enable) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    c->trace = enable != 0;
+    return NDT_OK;
+}
+
+int ndt_debug_read(ndt_ctx* c, uint64_t index, double* out, int32_t max_records,
+                   int32_t* num_records) {
+    if (!c || !out || !num_records) return NDT_ERR_INVALID_ARGUMENT;
+    *num_records = 0;
+    for (size_t j = 0; j < c->trace_slot.size(); ++j) {
+        if (c->trace_slot[j] != index) continue;
+        const double* src = c->h_trace.data() + j * (size_t)c->trace_iters * TRACE_REC;
+        int n = 0;
+        for (int it = 0; it < c->trace_iters && it < max_records; ++it) {
+            if (src[it * TRACE_REC] != src[it * TRACE_REC]) break;  // NaN: not run
+            std::memcpy(out + (size_t)it * TRACE_REC, src + (size_t)it * TRACE_REC,
+                        TRACE_REC * sizeof(double));
+            n++;
+        }
+        *num_records = n;
+        return NDT_OK;
+    }
+    set_error("no trace for that result index (enable ndt_debug_trace before aligning)");
+    return NDT_ERR_INVALID_ARGUMENT;
 }
 
 int ndt_stats_get(ndt_ctx* c, ndt_stats* out) {
@@ -411,6 +443,13 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         p.eps = (double)sqrtf(ef * ef);
     }
     p.status = (uint32_t*)c->d_status.p;
+    p.trace = nullptr;
+    if (c->trace) {
+        size_t tb = (size_t)nj * p.max_iter * TRACE_REC * sizeof(double);
+        if ((rc = dev_reserve(c->d_trace, tb))) return rc;
+        cudaMemsetAsync(c->d_trace.p, 0xFF, tb, st);  // NaN marks iterations not run
+        p.trace = (double*)c->d_trace.p;
+    }
     LaunchShape shape = choose_shape(c, nj, max_n);
     cudaEventRecord(c->ev0, st);
     if ((rc = launch_align(p, shape, st))) return rc;
@@ -429,6 +468,14 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
     c->stats.d2h_bytes += ob + sob + 4;
     if ((rc = cuda_fail(cudaStreamSynchronize(st), "align"))) return rc;
     if ((rc = check_status(c, *hst))) return rc;
+    if (c->trace) {
+        c->trace_iters = p.max_iter;
+        c->h_trace.resize((size_t)nj * p.max_iter * TRACE_REC);
+        cudaMemcpy(c->h_trace.data(), c->d_trace.p, c->h_trace.size() * sizeof(double),
+                   cudaMemcpyDeviceToHost);
+        c->trace_slot.resize(nj);
+        for (uint32_t j = 0; j < nj; ++j) c->trace_slot[j] = jobs[j].slot;
+    }
     float ams = 0.f, sms = 0.f;
     cudaEventElapsedTime(&ams, c->ev0, c->ev1);
     cudaEventElapsedTime(&sms, c->ev1, c->ev2);
@@ -457,6 +504,11 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         c->stats.iterations += (uint64_t)std::max(o.iterations, 0);
         c->stats.point_iterations += o.point_iters;
         c->stats.correspondences += o.corr_total;
+        c->stats.cycles_points += o.cycles[0];
+        c->stats.cycles_cluster_wait += o.cycles[1];
+        c->stats.cycles_control += o.cycles[2];
+        c->stats.cycles_broadcast += o.cycles[3];
+        c->stats.eigen_solves += (uint64_t)o.n_eigen;
     }
     return NDT_OK;
 }

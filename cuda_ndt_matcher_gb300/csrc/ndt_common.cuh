@@ -39,6 +39,7 @@ struct MapView {
     float inv_res;        // 1.0f / res, as the reference query computes it
     float r2;             // res * res (f32)
     uint32_t num_voxels;
+    int32_t exact_inv;    // inv_res is a power of two (q * inv_res is exact in f32)
 };
 
 // Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).
@@ -68,6 +69,32 @@ __device__ __forceinline__ uint32_t local_key(const MapView& m, int32_t gx, int3
     return lx | (ly << m.bits[0]) | (lz << (m.bits[0] + m.bits[1]));
 }
 
+// Home slot of a cell: a 32-bit avalanche mix ("lowbias32", two multiply-xorshift rounds)
+// of its 31-bit local key. The reference addresses its table with the MurmurHash3 64-bit
+// finaliser of a 63-bit key; which slot a voxel lands in is invisible to callers (a lookup
+// returns the voxel of exactly that cell), and the 32-bit mix costs a fraction of the
+// 64-bit multiplies while spreading keys as evenly (no primary clustering).
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// cell -> (local key, home slot); false when the cell lies outside the map's bounding box
+__device__ __forceinline__ bool cell_slot(const MapView& m, int32_t gx, int32_t gy, int32_t gz,
+                                          uint32_t& key, uint32_t& home) {
+    uint32_t lx = (uint32_t)(gx - m.min_cell[0]);
+    uint32_t ly = (uint32_t)(gy - m.min_cell[1]);
+    uint32_t lz = (uint32_t)(gz - m.min_cell[2]);
+    if ((lx >> m.bits[0]) | (ly >> m.bits[1]) | (lz >> m.bits[2])) return false;
+    key = lx | (ly << m.bits[0]) | (lz << (m.bits[0] + m.bits[1]));
+    home = mix32(key) & m.mask;
+    return true;
+}
+
 // Bounded linear probe: returns the slot holding `key` or -1. The bound max_probe + 1 is
 // exact (no stored key sits further than max_probe from its home), so the loop both matches
 // "probe to empty or match" and cannot spin.
@@ -84,6 +111,35 @@ __device__ __forceinline__ int32_t probe(const MapView& m, uint32_t key, uint32_
         s = (s + 1) & m.mask;
     }
     return -1;
+}
+
+// Continues a probe whose home slot held another key: slots home+1 .. home+max_probe.
+__device__ __forceinline__ int32_t probe_next(const MapView& m, uint32_t key, uint32_t home,
+                                              uint4* out) {
+    for (uint32_t j = 1; j <= m.max_probe; ++j) {
+        uint32_t s = (home + j) & m.mask;
+        uint4 v = __ldg(m.slots + s);
+        if (v.x == key) {
+            *out = v;
+            return (int32_t)s;
+        }
+        if (v.x == EMPTY_KEY) return -1;
+    }
+    return -1;
+}
+
+// Cell of the unevaluated sum qh + ql (|ql| <= half an ulp of qh): floor(qh * inv_res),
+// stepped down when qh * inv_res is exactly an integer and ql is negative. The correction
+// is exact when inv_res is a power of two (then qh * inv_res is exact).
+__device__ __forceinline__ void cell_of_sum(const MapView& m, const float* qh, const float* ql,
+                                            int32_t* gc) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float f = __fmul_rn(qh[i], m.inv_res);
+        float fl = floorf(f);
+        if (m.exact_inv && f == fl && ql[i] < 0.f) fl -= 1.f;
+        gc[i] = (int32_t)fl;
+    }
 }
 
 // Offsets in the reference's fixed order (ndt_graph_kernels.cu:29-39): dx outer, dz inner.

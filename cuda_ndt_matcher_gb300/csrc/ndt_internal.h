@@ -79,10 +79,19 @@ struct AlignOut {
     int32_t pad;
     uint64_t point_iters;
     uint64_t corr_total;
+    uint64_t cycles[4];  // SM cycles: points + CTA reduce, cluster wait, control, broadcast
+    int32_t n_eigen;     // iterations that took the eigen (indefinite) solver path
+    int32_t pad2;
 };
+
+// Per-iteration trace record (doubles): it, score, correspondences, pose before the step (6),
+// gradient (6), Hessian upper triangle (21), raw solver output (6), solver path, solver ok,
+// 4 reserved. Same layout as the oracle's trace.
+constexpr int TRACE_REC = 48;
 
 struct AlignParams {
     MapView map;
+    double* trace;     // nullptr unless tracing is enabled
     const float* pts;
     const AlignJob* jobs;
     AlignOut* out;

@@ -1,6 +1,7 @@
 // ndt_score.cu — per-pose scoring and the neighbour query on sm_103a.
 //
-// k_score: for each (scan, pose) job, every point is transformed (f32), the voxels whose
+// k_score: for each (scan, pose) job, every point is transformed (compensated f32: the
+// transform as hi/lo pairs, so x = q - mean keeps f32 precision), the voxels whose
 // centroid lies within one resolution are found through the 27-cell hash probe (all of
 // them: kiddo's `within` set, src/ndt_cuda/src/voxel_grid/search.rs:90-99), and the block
 // accumulates
@@ -26,40 +27,70 @@ struct ScorePartial {
     uint64_t ncorr;
 };
 
-__device__ void zyx_T(const double* pose, float* T) {
+// nalgebra from_euler_angles (Rz*Ry*Rx) transform in FP64
+__device__ void zyx_T(const double* pose, double* T) {
     double sr, cr, sp, cp, sy, cy;
     sincos(pose[3], &sr, &cr);
     sincos(pose[4], &sp, &cp);
     sincos(pose[5], &sy, &cy);
-    T[0] = (float)(cy * cp);
-    T[1] = (float)(cy * sp * sr - sy * cr);
-    T[2] = (float)(cy * sp * cr + sy * sr);
-    T[3] = (float)pose[0];
-    T[4] = (float)(sy * cp);
-    T[5] = (float)(sy * sp * sr + cy * cr);
-    T[6] = (float)(sy * sp * cr - cy * sr);
-    T[7] = (float)pose[1];
-    T[8] = (float)(-sp);
-    T[9] = (float)(cp * sr);
-    T[10] = (float)(cp * cr);
-    T[11] = (float)pose[2];
+    T[0] = cy * cp;
+    T[1] = cy * sp * sr - sy * cr;
+    T[2] = cy * sp * cr + sy * sr;
+    T[3] = pose[0];
+    T[4] = sy * cp;
+    T[5] = sy * sp * sr + cy * cr;
+    T[6] = sy * sp * cr - cy * sr;
+    T[7] = pose[1];
+    T[8] = -sp;
+    T[9] = cp * sr;
+    T[10] = cp * cr;
+    T[11] = pose[2];
+}
+
+// q = T p as an unevaluated sum qh + ql: T given as hi/lo f32 pairs, TwoProd/TwoSum
+__device__ __forceinline__ void transform_comp(const float* Th, const float* Tl, float px,
+                                               float py, float pz, float* qh, float* ql) {
+    const float pv[3] = {px, py, pz};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float hi = Th[4 * i + 3], lo = Tl[4 * i + 3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float r = Th[4 * i + j];
+            float ph = r * pv[j];
+            float pl = fmaf(r, pv[j], -ph);
+            float s = hi + ph;
+            float bb = s - hi;
+            float e = (hi - (s - bb)) + (ph - bb);
+            hi = s;
+            lo += e + pl + Tl[4 * i + j] * pv[j];
+        }
+        float s = hi + lo;
+        ql[i] = lo - (s - hi);
+        qh[i] = s;
+    }
 }
 
 __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict__ pts,
                                               const ScoreJob* __restrict__ jobs,
                                               const AlignOut* __restrict__ aout, float d1,
                                               float d2, ScorePartial* __restrict__ part) {
-    __shared__ float T[12];
+    __shared__ float Th[12], Tl[12];
     __shared__ double red[ST / 32][2];
     __shared__ unsigned long long redc[ST / 32][2];
     const ScoreJob job = jobs[blockIdx.y];
     const size_t pidx = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
     const uint32_t first = blockIdx.x * SCHUNK;
     if (threadIdx.x == 0) {
+        double T[12];
         if (job.pose_src == 1) {
             zyx_T(aout[job.out_index].pose, T);
         } else {
-            for (int i = 0; i < 12; ++i) T[i] = (float)job.T[i];
+            for (int i = 0; i < 12; ++i) T[i] = job.T[i];
+        }
+        for (int i = 0; i < 12; ++i) {
+            Th[i] = (float)T[i];
+            Tl[i] = (float)(T[i] - (double)Th[i]);
         }
     }
     __syncthreads();
@@ -71,12 +102,12 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
         float px = __ldg(P + 3 * (size_t)i), py = __ldg(P + 3 * (size_t)i + 1),
               pz = __ldg(P + 3 * (size_t)i + 2);
         if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-        float qx = fmaf(T[0], px, fmaf(T[1], py, fmaf(T[2], pz, T[3])));
-        float qy = fmaf(T[4], px, fmaf(T[5], py, fmaf(T[6], pz, T[7])));
-        float qz = fmaf(T[8], px, fmaf(T[9], py, fmaf(T[10], pz, T[11])));
-        int32_t gx = (int32_t)floorf(__fmul_rn(qx, m.inv_res));
-        int32_t gy = (int32_t)floorf(__fmul_rn(qy, m.inv_res));
-        int32_t gz = (int32_t)floorf(__fmul_rn(qz, m.inv_res));
+        float qh[3], ql[3];
+        transform_comp(Th, Tl, px, py, pz, qh, ql);
+        const float qx = qh[0], qy = qh[1], qz = qh[2];
+        int32_t gc[3];
+        cell_of_sum(m, qh, ql, gc);
+        const int32_t gx = gc[0], gy = gc[1], gz = gc[2];
         float best = -INFINITY, sum = 0.f;
         int cnt = 0;
 #pragma unroll 1
@@ -84,17 +115,20 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
             int dx, dy, dz;
             offset27(c, dx, dy, dz);
             int32_t cx = gx + dx, cy = gy + dy, cz = gz + dz;
-            uint32_t key = local_key(m, cx, cy, cz);
-            if (key == EMPTY_KEY) continue;
+            uint32_t key, home;
+            if (!cell_slot(m, cx, cy, cz, key, home)) continue;
             uint4 sv;
-            int32_t s = probe(m, key, (uint32_t)fmix64(pack21(cx, cy, cz)) & m.mask, &sv);
+            int32_t s = probe(m, key, home, &sv);
             if (s < 0) continue;
             float mx = __uint_as_float(sv.y), my = __uint_as_float(sv.z),
                   mz = __uint_as_float(sv.w);
-            if (dist2_rn(qx, qy, qz, mx, my, mz) > m.r2) continue;
+            {
+                float e0 = (qx - mx) + ql[0], e1 = (qy - my) + ql[1], e2 = (qz - mz) + ql[2];
+                if (fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2) continue;
+            }
             float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
             float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
-            float x0 = qx - mx, x1 = qy - my, x2 = qz - mz;
+            float x0 = (qx - mx) + ql[0], x1 = (qy - my) + ql[1], x2 = (qz - mz) + ql[2];
             float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
             float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
             float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
@@ -185,10 +219,10 @@ __global__ void k_query(MapView m, const float* __restrict__ q, size_t n, int ma
         int dx, dy, dz;
         offset27(k, dx, dy, dz);
         int32_t cx = gx + dx, cy = gy + dy, cz = gz + dz;
-        uint32_t key = local_key(m, cx, cy, cz);
-        if (key == EMPTY_KEY) continue;
+        uint32_t key, home;
+        if (!cell_slot(m, cx, cy, cz, key, home)) continue;
         uint4 sv;
-        int32_t s = probe(m, key, (uint32_t)fmix64(pack21(cx, cy, cz)) & m.mask, &sv);
+        int32_t s = probe(m, key, home, &sv);
         if (s < 0) continue;
         if (dist2_rn(qx, qy, qz, __uint_as_float(sv.y), __uint_as_float(sv.z),
                      __uint_as_float(sv.w)) <= m.r2)

@@ -553,8 +553,8 @@ __global__ void k_hash_insert(const int32_t* __restrict__ coord, const float4* _
     uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
     int32_t gx = coord[3 * v], gy = coord[3 * v + 1], gz = coord[3 * v + 2];
-    uint32_t key = local_key(m, gx, gy, gz);
-    uint32_t s = (uint32_t)fmix64(pack21(gx, gy, gz)) & m.mask;
+    uint32_t key, s;
+    cell_slot(m, gx, gy, gz, key, s);  // every voxel lies inside the map's bounding box
     for (uint32_t j = 0; j <= m.mask; ++j) {
         uint32_t old = atomicCAS(&slots[s].x, EMPTY_KEY, key);
         if (old == EMPTY_KEY) {
@@ -691,6 +691,11 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
     v.inv_res = 1.0f / cfg.resolution;
     v.r2 = cfg.resolution * cfg.resolution;
     v.num_voxels = V;
+    {
+        int ex = 0;
+        float fr = frexpf(v.inv_res, &ex);
+        v.exact_inv = (fr == 0.5f) ? 1 : 0;
+    }
     k_hash_insert<<<(V + 127) / 128, 128, 0, s>>>(
         (int32_t*)map.vox_coord.p, (float4*)map.vox_mean.p, (float*)map.vox_icov.p, V, v,
         (uint4*)map.slots.p, (float4*)map.slot_icov.p, (int32_t*)map.slot_vidx.p, mprobe,

@@ -119,6 +119,12 @@ typedef struct ndt_stats {
     double build_ms;
     uint64_t h2d_bytes;
     uint64_t d2h_bytes;
+    /* Newton kernel phase split, SM cycles summed over alignments (rank-0 CTA view) */
+    uint64_t cycles_points;        /* point work + CTA reduction */
+    uint64_t cycles_cluster_wait;  /* waiting for the other CTAs of the cluster */
+    uint64_t cycles_control;       /* FP64 reduction, Hessian assembly, 6x6 solve, step */
+    uint64_t cycles_broadcast;     /* pose broadcast barrier */
+    uint64_t eigen_solves;         /* iterations whose Hessian took the eigen path */
 } ndt_stats;
 
 typedef struct ndt_ctx ndt_ctx;
@@ -179,6 +185,16 @@ int ndt_stats_get(ndt_ctx* ctx, ndt_stats* out);
 int ndt_stats_reset(ndt_ctx* ctx);
 /* Enables CUDA-event timing of every kernel launch (read back through ndt_stats). */
 int ndt_profile_enable(ndt_ctx* ctx, int enable);
+
+/* Per-iteration records of the Newton loop (the K5 debug buffer of
+ * src/cuda_ffi/csrc/ndt_graph_common.cuh:101-114): when enabled, every alignment records per
+ * iteration 48 doubles: iteration, score, correspondences, pose before the step (6),
+ * gradient (6), Hessian upper triangle (21), raw solver output (6), solver path
+ * (0 Cholesky, 1 eigen), solver success, 4 reserved. ndt_debug_read copies the records of
+ * result `index` of the last alignment call. */
+int ndt_debug_trace(ndt_ctx* ctx, int enable);
+int ndt_debug_read(ndt_ctx* ctx, uint64_t index, double* out, int32_t max_records,
+                   int32_t* num_records);
 
 const char* ndt_last_error_string(void);
 

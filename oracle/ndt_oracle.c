@@ -1126,8 +1126,26 @@ void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* po
  * (:163-302), K3 solve without line search (:311-463), K5 update (:618-847), driven by
  * FullGpuPipelineV2::optimize (full_gpu_pipeline_v2.rs:487-669) and assembled by
  * NdtOptimizer::align_full_gpu (solver.rs:328-441). */
+static void align_gpu_sem_impl(const or_grid* g, const float* src, size_t n,
+                               const double* pose_in, const or_config* cfg, or_result* out,
+                               double* trace);
+
 void or_align_gpu_sem(const or_grid* g, const float* src, size_t n, const double* pose_in,
                       const or_config* cfg, or_result* out) {
+    align_gpu_sem_impl(g, src, n, pose_in, cfg, out, NULL);
+}
+
+/* same, recording the per-iteration trace (48 doubles per iteration, the layout of the
+ * GPU library's ndt_debug_read) */
+void or_align_gpu_sem_trace(const or_grid* g, const float* src, size_t n,
+                            const double* pose_in, const or_config* cfg, or_result* out,
+                            double* trace) {
+    align_gpu_sem_impl(g, src, n, pose_in, cfg, out, trace);
+}
+
+static void align_gpu_sem_impl(const or_grid* g, const float* src, size_t n,
+                               const double* pose_in, const or_config* cfg, or_result* out,
+                               double* trace) {
     double d1, d2;
     or_gauss_params(cfg->resolution, cfg->outlier_ratio, &d1, &d2);
     memset(out, 0, sizeof *out);
@@ -1142,7 +1160,24 @@ void or_align_gpu_sem(const or_grid* g, const float* src, size_t n, const double
         int32_t nc;
         or_derivatives_gpu_sem(g, src, n, pose, d1, d2, cfg->max_neighbors, &sc, gr, H, &nc);
         double dl[6];
-        if (!or_jacobi_svd_solve(H, gr, dl))
+        int solved = or_jacobi_svd_solve(H, gr, dl);
+        if (trace) {
+            double* t = trace + (size_t)it * 48;
+            t[0] = it;
+            t[1] = sc;
+            t[2] = nc;
+            int u = 0;
+            for (int i = 0; i < 6; ++i) {
+                t[3 + i] = pose[i];
+                t[9 + i] = gr[i];
+                t[36 + i] = dl[i];
+                for (int j = i; j < 6; ++j) t[15 + u++] = H[i * 6 + j];
+            }
+            t[42] = 1.0;
+            t[43] = solved;
+            t[44] = t[45] = t[46] = t[47] = 0.0;
+        }
+        if (!solved)
             for (int i = 0; i < 6; ++i) dl[i] = -gr[i] * 1e-4;
         double dphi = 0.0;
         for (int i = 0; i < 6; ++i) dphi += gr[i] * dl[i];

@@ -119,6 +119,9 @@ void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* po
                   const or_config* cfg, or_result* out);
 void or_align_gpu_sem(const or_grid* g, const float* src, size_t n, const double* pose_in,
                       const or_config* cfg, or_result* out);
+void or_align_gpu_sem_trace(const or_grid* g, const float* src, size_t n,
+                            const double* pose_in, const or_config* cfg, or_result* out,
+                            double* trace);
 /* many alignments on a thread pool (rayon par_iter in the reference, ndt.rs:921) */
 void or_align_batch(const or_grid* g, const float* const* srcs, const size_t* ns,
                     const double* poses_in, size_t m, const or_config* cfg, int semantics,

@@ -92,6 +92,8 @@ def lib():
                                     C.POINTER(OrResult)]),
             "or_align_gpu_sem": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
                                         C.POINTER(OrResult)]),
+            "or_align_gpu_sem_trace": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
+                                              C.POINTER(OrResult), f64p]),
             "or_align_batch": (None, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), f64p,
                                       C.c_size_t, C.POINTER(OrConfig), C.c_int, C.c_int,
                                       C.POINTER(OrResult)]),
@@ -239,6 +241,16 @@ class Grid:
         fn = lib().or_align_gpu_sem if semantics == "gpu" else lib().or_align_cpu
         fn(self.h, src, len(src), pose, C.byref(c), C.byref(r))
         return r.as_dict()
+
+    def align_trace(self, src, pose, **cfg):
+        """Graph-kernel semantics with the per-iteration trace (48 doubles per iteration)."""
+        c = config(resolution=self.res, **cfg)
+        r = OrResult()
+        src = _f32(src)
+        tr = np.full((c.max_iterations, 48), np.nan)
+        lib().or_align_gpu_sem_trace(self.h, src, len(src), np.ascontiguousarray(pose, np.float64),
+                                     C.byref(c), C.byref(r), tr)
+        return r.as_dict(), tr[:r.iterations]
 
     def align_batch(self, scans, poses, semantics="gpu", nthreads=0, **cfg):
         c = config(resolution=self.res, **cfg)

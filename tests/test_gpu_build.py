@@ -192,7 +192,7 @@ def test_build_errors_and_nan(gpu):
         ctx.set_target(np.full((100, 3), np.nan, np.float32))
     assert e.value.code == -3
     with pytest.raises(capi.NdtError) as e:  # every voxel below min points
-        ctx.set_target(np.arange(300, dtype=np.float32).reshape(100, 3) * 10)
+        ctx.set_target(np.random.default_rng(0).uniform(0, 100, (100, 3)).astype(np.float32))
     assert e.value.code == -4
     with pytest.raises(capi.NdtError) as e:
         capi.Context().align(np.zeros((10, 3), np.float32), np.zeros(6))
