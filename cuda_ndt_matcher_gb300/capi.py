@@ -26,7 +26,7 @@ EXPORTS = [
     "ndt_ctx_stream",
     "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
-    "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
+    "ndt_autotune", "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
     "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
     "ndt_radix_sort_pairs_u64_u32",
     "ndt_detect_segments", "ndt_morton_codes",
@@ -62,6 +62,12 @@ class Result(C.Structure):
 class Scan(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("num_points", C.c_uint64),
                 ("initial_pose", C.c_double * 6)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("cluster_size", C.c_int32), ("threads_per_cta", C.c_int32),
+                ("kernel_ms", C.c_double), ("aligns_per_s", C.c_double),
+                ("candidates", C.c_int32), ("registers", C.c_int32)]
 
 
 class MapInfo(C.Structure):
@@ -120,6 +126,7 @@ def load(build_if_missing=True):
         "ndt_align_multi_pose": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
         "ndt_align_batch": (C.c_int, [P, P, C.c_uint64, P]),
         "ndt_align_batch_device": (C.c_int, [P, P, P, P, C.c_uint64, P]),
+        "ndt_autotune": (C.c_int, [P, P, P, P, C.c_uint64, C.c_int32, C.POINTER(TuneResult)]),
         "ndt_eval_batch": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
         "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
@@ -274,6 +281,17 @@ class Context:
         check(self.lib.ndt_align_batch_device(self.h, d_xyz, offsets.ctypes.data,
                                               poses.ctypes.data, m, res))
         return [result_dict(r) for r in res]
+
+    def autotune(self, d_xyz, offsets, poses, repeats=2):
+        """Times the launch-shape candidates on a device-resident batch; returns the winner."""
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        poses = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 6))
+        r = TuneResult()
+        check(self.lib.ndt_autotune(self.h, d_xyz, offsets.ctypes.data, poses.ctypes.data,
+                                    len(poses), repeats, C.byref(r)))
+        return {"cluster_size": r.cluster_size, "threads_per_cta": r.threads_per_cta,
+                "kernel_ms": r.kernel_ms, "aligns_per_s": r.aligns_per_s,
+                "candidates": r.candidates, "registers": r.registers}
 
     def eval_batch(self, points, T34):
         p = as_xyz(points)

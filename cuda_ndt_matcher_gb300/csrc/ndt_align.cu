@@ -703,8 +703,10 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
     return 0;
 }
 
-template <int THREADS, bool CPU_SEM>
-__global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 128))
+// REGCAP: registers per thread the launch bounds allow (128: the default; 80: more resident
+// CTAs per SM at the price of a few spills; the autotuner picks)
+template <int THREADS, bool CPU_SEM, int REGCAP>
+__global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_align(const AlignParams P) {
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
@@ -855,7 +857,17 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 128))
     }
 }
 
-template <int T>
+template <int T, bool SEM, int CAP>
+static cudaError_t launch_k(cudaLaunchConfig_t& cfg, const AlignParams& p, int K) {
+    cudaFuncSetAttribute(k_ndt_align<T, SEM, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cfg.dynamicSmemBytes);
+    if (K > 8)
+        cudaFuncSetAttribute(k_ndt_align<T, SEM, CAP>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return cudaLaunchKernelEx(&cfg, k_ndt_align<T, SEM, CAP>, p);
+}
+
+template <int T, int CAP>
 static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.num_jobs * K, 1, 1);
@@ -869,22 +881,8 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e;
-    if (p.semantics == NDT_SEMANTICS_CPU) {
-        cudaFuncSetAttribute(k_ndt_align<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)cfg.dynamicSmemBytes);
-        if (K > 8)
-            cudaFuncSetAttribute(k_ndt_align<T, true>,
-                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaLaunchKernelEx(&cfg, k_ndt_align<T, true>, p);
-    } else {
-        cudaFuncSetAttribute(k_ndt_align<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)cfg.dynamicSmemBytes);
-        if (K > 8)
-            cudaFuncSetAttribute(k_ndt_align<T, false>,
-                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaLaunchKernelEx(&cfg, k_ndt_align<T, false>, p);
-    }
+    cudaError_t e = p.semantics == NDT_SEMANTICS_CPU ? launch_k<T, true, CAP>(cfg, p, K)
+                                                     : launch_k<T, false, CAP>(cfg, p, K);
     return cuda_fail(e, "ndt align launch");
 }
 
@@ -897,10 +895,11 @@ int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s) {
     }
     AlignParams q = p;
     q.cluster = K;
+    const bool dense = shape.regcap == 80;
     switch (shape.threads) {
-        case 128: return launch_t<128>(q, K, s);
-        case 256: return launch_t<256>(q, K, s);
-        case 512: return launch_t<512>(q, K, s);
+        case 128: return dense ? launch_t<128, 80>(q, K, s) : launch_t<128, 128>(q, K, s);
+        case 256: return dense ? launch_t<256, 80>(q, K, s) : launch_t<256, 128>(q, K, s);
+        case 512: return launch_t<512, 128>(q, K, s);
         default:
             set_error("threads per CTA must be 128, 256 or 512");
             return NDT_ERR_INVALID_ARGUMENT;

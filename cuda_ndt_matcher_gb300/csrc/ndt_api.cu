@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "ndt_internal.h"
@@ -101,6 +102,8 @@ struct ndt_ctx {
     std::vector<uint32_t> trace_slot;  // job index -> caller's result index
     int trace_iters = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    LaunchShape forced{0, 0, 0};                           // set only while autotuning
+    std::map<std::pair<int, int>, LaunchShape> tuned;      // (log2 jobs, log2 max points)
 };
 
 static int check_status(ndt_ctx* c, uint32_t st) {
@@ -374,16 +377,32 @@ int ndt_map_voxels(ndt_ctx* c, int32_t* coords, float* means, float* covs, float
 }  // extern "C"
 
 // Launch shape: enough CTAs to fill the GPU twice over, at least ~1k points per CTA.
+static int log2_bucket(uint64_t v) {
+    int b = 0;
+    while ((1ull << b) < v && b < 63) ++b;
+    return b;
+}
+
+// Launch shape: an explicit configuration wins, then an autotuned entry for this
+// (batch size, scan size) bucket, then the default: 512-thread CTAs for large scans, and
+// clusters doubled until the launch covers about three CTAs per SM while keeping at least
+// two points per thread per CTA.
 static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
-    LaunchShape sh;
-    sh.threads = c->cfg.threads_per_cta > 0 ? c->cfg.threads_per_cta : 256;
+    LaunchShape sh{0, 0, 128};
+    if (c->forced.cluster > 0) return c->forced;
+    auto it = c->tuned.find({log2_bucket(jobs), log2_bucket(max_n)});
+    if (it != c->tuned.end() && c->cfg.cluster_size <= 0 && c->cfg.threads_per_cta <= 0)
+        return it->second;
+    sh.threads = c->cfg.threads_per_cta > 0
+                     ? c->cfg.threads_per_cta
+                     : (max_n >= 4096 ? 512 : (max_n >= 1024 ? 256 : 128));
     if (c->cfg.cluster_size > 0) {
         sh.cluster = c->cfg.cluster_size;
         return sh;
     }
     int K = 1;
-    while (K < 8 && (uint64_t)jobs * K < 2ull * (uint64_t)c->num_sms &&
-           max_n / (uint32_t)(2 * K) >= (uint32_t)sh.threads * 4)
+    while (K < 8 && (uint64_t)jobs * K < 3ull * (uint64_t)c->num_sms &&
+           max_n / (uint32_t)(2 * K) >= (uint32_t)sh.threads * 2)
         K *= 2;
     sh.cluster = K;
     return sh;
@@ -631,6 +650,52 @@ int ndt_align_batch_device(ndt_ctx* c, const float* d_xyz, const uint64_t* offse
         ns[i] = jobs[i].n;
     }
     return run_align(c, d_xyz, jobs, ns, out);
+}
+
+int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const double* poses,
+                 uint64_t m, int32_t repeats, ndt_tune_result* out) {
+    if (!c || !d_xyz || !offsets || !poses || m == 0 || !out) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (repeats < 1) repeats = 1;
+    uint64_t max_n = 0;
+    for (uint64_t i = 0; i < m; ++i) max_n = std::max(max_n, offsets[i + 1] - offsets[i]);
+    std::vector<ndt_result> tmp(m);
+    ndt_stats saved = c->stats;
+    const int Ks[4] = {1, 2, 4, 8};
+    const int TC[5][2] = {{128, 128}, {128, 80}, {256, 128}, {256, 80}, {512, 128}};
+    LaunchShape best{0, 0, 128};
+    double best_ms = 1e300;
+    int tried = 0;
+    for (int K : Ks) {
+        for (const auto& tc : TC) {
+            c->forced = LaunchShape{K, tc[0], tc[1]};
+            rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());  // warm
+            if (rc) break;
+            double before = c->stats.align_kernel_ms;
+            for (int r = 0; r < repeats && !rc; ++r)
+                rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());
+            if (rc) break;
+            double ms = (c->stats.align_kernel_ms - before) / repeats;
+            tried++;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c->forced;
+            }
+        }
+        if (rc) break;
+    }
+    c->forced = LaunchShape{0, 0, 0};
+    c->stats = saved;
+    if (rc) return rc;
+    c->tuned[{log2_bucket(m), log2_bucket(max_n)}] = best;
+    out->cluster_size = best.cluster;
+    out->threads_per_cta = best.threads;
+    out->registers = best.regcap;
+    out->kernel_ms = best_ms;
+    out->aligns_per_s = best_ms > 0 ? 1000.0 * (double)m / best_ms : 0.0;
+    out->candidates = tried;
+    return NDT_OK;
 }
 
 int ndt_eval_batch(ndt_ctx* c, const float* xyz, uint64_t n, const double* T34, uint64_t m,

@@ -111,6 +111,7 @@ struct AlignParams {
 struct LaunchShape {
     int cluster;
     int threads;
+    int regcap;  // 128 (default) or 80 (denser residency for 128/256-thread CTAs)
 };
 
 int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s);

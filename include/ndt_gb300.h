@@ -168,6 +168,26 @@ int ndt_align_batch(ndt_ctx* ctx, const ndt_scan* scans, uint64_t num_scans, ndt
 int ndt_align_batch_device(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
                            const double* poses_in, uint64_t num_scans, ndt_result* out);
 
+/* Autotuner for the Newton kernel's launch shape (points per CTA = scan size / cluster
+ * size; threads per CTA): times every (cluster size 1, 2, 4, 8) x (128, 256, 512 threads)
+ * candidate, each with a 128- and an 80-register instance where the CTA size allows more
+ * than one resident CTA per SM, on the given device-resident batch (as ndt_align_batch_device takes it),
+ * `repeats` timed runs each, and records the fastest for batches of this size class (log2
+ * of the scan count and of the largest scan). Later calls in that class use it unless the
+ * configuration fixes cluster_size / threads_per_cta. No counterpart in the reference,
+ * whose launch shapes are constants. */
+typedef struct ndt_tune_result {
+    int32_t cluster_size;
+    int32_t threads_per_cta;
+    double kernel_ms;              /* Newton kernel time of the winner, per batch */
+    double aligns_per_s;           /* batch size / kernel_ms */
+    int32_t candidates;
+    int32_t registers;             /* register cap of the winning kernel instance */
+} ndt_tune_result;
+int ndt_autotune(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
+                 const double* poses_in, uint64_t num_scans, int32_t repeats,
+                 ndt_tune_result* out);
+
 /* evaluate_nvtl / evaluate_transform_probability / evaluate_nvtl_batch
  * (src/ndt_cuda/src/ndt.rs:681-890): per pose, NVTL (mean over points with a neighbour of
  * the best voxel score) and score / correspondences over all voxels within one resolution.
