@@ -28,7 +28,7 @@ EXPORTS = [
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
     "ndt_autotune", "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
     "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
-    "ndt_radix_sort_pairs_u64_u32",
+    "ndt_radix_sort_pairs_u64_u32", "ndt_radix_sort_pairs_u64_u32_static",
     "ndt_detect_segments", "ndt_morton_codes",
 ]
 
@@ -137,6 +137,8 @@ def load(build_if_missing=True):
         "ndt_last_error_string": (C.c_char_p, []),
         "ndt_radix_sort_pairs_u64_u32": (C.c_int, [P, P, C.c_uint64, C.c_int32, C.c_int32, P,
                                                    C.POINTER(C.c_uint64), P]),
+        "ndt_radix_sort_pairs_u64_u32_static": (C.c_int, [P, P, C.c_uint64, C.c_int32,
+                                                          C.c_int32, P]),
         "ndt_detect_segments": (C.c_int, [P, C.c_uint64, P, P, P, P, C.POINTER(C.c_uint64), P]),
         "ndt_morton_codes": (C.c_int, [P, C.c_uint64, C.c_float, P, P, P, P,
                                        C.POINTER(C.c_uint64), P]),

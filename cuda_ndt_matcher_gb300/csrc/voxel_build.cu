@@ -25,6 +25,7 @@
 // bit.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "ndt_internal.h"
 
@@ -253,6 +254,75 @@ int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, in
     }
     return cuda_fail(cudaGetLastError(), "radix sort");
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free radix sort: the passes above with their scratch (alternate key/value
+// buffers, digit histograms, scan block sums) in one fixed device array of this module.
+// Sized for STATIC_SORT_MAX_PAIRS pairs: 8 + 4 bytes per pair + 256 counters per 4096-pair
+// tile + the scan's block sums = 12,845,312 bytes. Nothing in it needs to start at zero:
+// every pass writes each word of the scratch before it reads it.
+// ---------------------------------------------------------------------------------------
+constexpr size_t STATIC_SORT_MAX_PAIRS = size_t(1) << 20;
+constexpr size_t STATIC_SORT_SCRATCH_BYTES = STATIC_SORT_MAX_PAIRS * 8 + STATIC_SORT_MAX_PAIRS * 4 +
+                                             256 * (STATIC_SORT_MAX_PAIRS / TILE) * 4 + 256;
+constexpr int STATIC_SORT_MAX_DEVICES = 64;
+
+static __device__ __align__(256) unsigned char g_static_sort_scratch[STATIC_SORT_SCRATCH_BYTES];
+
+static std::mutex g_static_sort_mu;
+static void* g_static_sort_ptr[STATIC_SORT_MAX_DEVICES];
+
+// Device address of the scratch array on the current device, resolved once per device (the
+// first call may load this module onto the device).
+static int static_sort_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "static radix sort: no current device");
+    if (dev < 0 || dev >= STATIC_SORT_MAX_DEVICES) {
+        set_error("static radix sort: device ordinal out of range");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_static_sort_mu);
+    if (!g_static_sort_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "static radix sort: scratch set-up");
+        if (radix_sort_temp_bytes(STATIC_SORT_MAX_PAIRS) > STATIC_SORT_SCRATCH_BYTES) {
+            set_error("static radix sort: scratch array smaller than the sort needs");
+            return NDT_ERR_CAPACITY;
+        }
+        g_static_sort_ptr[dev] = p;
+    }
+    *out = g_static_sort_ptr[dev];
+    return NDT_OK;
+}
+
+}  // namespace ndtgb
+
+extern "C" int ndt_radix_sort_pairs_u64_u32_static(uint64_t* d_keys, uint32_t* d_values,
+                                                   uint64_t n, int32_t begin_bit,
+                                                   int32_t end_bit, void* stream) {
+    using namespace ndtgb;
+    if (begin_bit < 0 || end_bit > 64 || begin_bit > end_bit) {
+        set_error("static radix sort: bit range must satisfy 0 <= begin_bit <= end_bit <= 64");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    if (n > STATIC_SORT_MAX_PAIRS) {
+        set_error("static radix sort: at most 1048576 pairs (fixed 12.25 MiB device scratch)");
+        return NDT_ERR_CAPACITY;
+    }
+    if (n && (!d_keys || !d_values)) {
+        set_error("static radix sort: null key or value pointer");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    void* scratch = nullptr;
+    int rc = static_sort_scratch(&scratch);
+    if (rc) return rc;
+    return radix_sort_pairs(d_keys, d_values, (size_t)n, begin_bit, end_bit, scratch,
+                            STATIC_SORT_SCRATCH_BYTES, (cudaStream_t)stream);
+}
+
+namespace ndtgb {
 
 // ---------------------------------------------------------------------------------------
 // Segments of sorted keys.

@@ -227,6 +227,22 @@ const char* ndt_last_error_string(void);
 int ndt_radix_sort_pairs_u64_u32(uint64_t* d_keys, uint32_t* d_values, uint64_t n,
                                  int32_t begin_bit, int32_t end_bit, void* d_temp,
                                  uint64_t* temp_bytes, void* stream);
+/* Allocation-free variant of ndt_radix_sort_pairs_u64_u32; it has no counterpart in the
+ * reference. It is for callers that may not allocate device memory while they run: a
+ * real-time loop where cudaMalloc/cudaFree would synchronise the device and stall the
+ * pipeline, or a process held to a fixed device-memory budget. Same result as
+ * ndt_radix_sort_pairs_u64_u32 (stable ascending sort of bits [begin_bit, end_bit), in place),
+ * but the scratch is one fixed array inside this library (12,845,312 bytes per device), so:
+ *  - n <= 1048576 pairs; larger n returns NDT_ERR_CAPACITY and touches nothing;
+ *  - the first call on each device does the set-up (resolves the array's device address,
+ *    which can load the library's kernels onto that device): make it, with that device
+ *    current, before any stream capture;
+ *  - the scratch needs no initial contents (nothing in it has to start at zero);
+ *  - all calls on one device share the scratch: two calls whose work overlaps on the GPU
+ *    (different streams, or host threads with no ordering between their streams) race and
+ *    corrupt each other's results. Issue them on one stream, or order them. */
+int ndt_radix_sort_pairs_u64_u32_static(uint64_t* d_keys, uint32_t* d_values, uint64_t n,
+                                        int32_t begin_bit, int32_t end_bit, void* stream);
 /* detect_boundaries_kernel + InclusiveSum + Flagged (src/cuda_ffi/csrc/segment_detect.cu:
  * 27-146): segment id per element and start index per segment of sorted keys. */
 int ndt_detect_segments(const uint64_t* d_sorted, uint64_t n, uint32_t* d_segment_ids,
