@@ -40,13 +40,16 @@ FLOP_PER_PAIR = 65
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--map-points", type=int, default=5_000_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--shape", default="",
+                    help="fixed Newton-kernel launch shape CLUSTER,THREADS,REGISTERS "
+                         "(e.g. 8,256,80) instead of the autotuner")
     return ap.parse_args()
 
 
@@ -233,8 +236,15 @@ def run_ours(args):
     def step_host():
         capi.check(ctx.lib.ndt_align_batch(ctx.h, scan_arr, B, res_e2e))
 
-    # launch shape for this batch class, chosen by the library's autotuner (untimed)
-    tune = ctx.autotune(C.c_void_p(d_pts.data_ptr()), off_c, pose_c, repeats=1)
+    if args.shape:
+        K, T, R = (int(v) for v in args.shape.split(","))
+        ctx.configure(cluster_size=K, threads_per_cta=T, max_registers=R)
+        tune = {"cluster_size": K, "threads_per_cta": T, "registers": R,
+                "chosen_by": "--shape"}
+    else:
+        # launch shape for this batch class, chosen by the library's autotuner (untimed)
+        tune = ctx.autotune(C.c_void_p(d_pts.data_ptr()), off_c, pose_c, repeats=1)
+        tune["chosen_by"] = "ndt_autotune"
     for _ in range(args.warmup):
         step_device()
         step_host()
@@ -311,7 +321,7 @@ def run_ours(args):
                        "launch_shape": {"cluster_size": tune["cluster_size"],
                                         "threads_per_cta": tune["threads_per_cta"],
                                         "registers": tune["registers"],
-                                        "chosen_by": "ndt_autotune"}},
+                                        "chosen_by": tune["chosen_by"]}},
             "e2e": {"value": e2e, "unit": "aligns/s",
                     "h2d_bytes_per_step": int(st_e2e["h2d_bytes"] // max(args.steps, 1)),
                     "d2h_bytes_per_step": int(st_e2e["d2h_bytes"] // max(args.steps, 1))},

@@ -47,7 +47,7 @@ class Config(C.Structure):
                 ("semantics", C.c_int32), ("min_correspondences", C.c_int32),
                 ("device", C.c_int32), ("cluster_size", C.c_int32),
                 ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("max_registers", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Result(C.Structure):

@@ -40,8 +40,10 @@ constexpr int NFR = 52;           // per-iteration frame: R,t hi (12), R,t lo (1
 constexpr int A_SC = 0, A_G = 1, A_GP = 4, A_M = 13, A_HTR = 19, A_HRR = 28;
 
 struct SolveScratch {
-    double A[36], V[36], cs[6], x[6];
+    double A[36], V[36], T[36], cs[6], x[6];
+    float A32[36], V32[36], cs32[6];
     int ok, path;  // path: 0 Cholesky, 1 eigen
+    int sweeps;    // FP64 Jacobi sweeps of the eigen path
 };
 
 struct AlignShared {
@@ -54,6 +56,8 @@ struct AlignShared {
     double pose[6];
     double H[36];
     double g[6];
+    double trig[16];            // sin/cos of roll, pitch, yaw, 1 (exact; then small-angle rule)
+    double Ad[27], Bd[54];      // dR/dtheta_k and d2R/dtheta_k dtheta_l at `pose` (FP64)
     float fr[NFR];
     int done;
     // rank-0 controller state
@@ -71,97 +75,82 @@ __device__ __forceinline__ int sym3(int a, int b) {
     return i == 0 ? j : (i == 1 ? 2 + j : 5);
 }
 
-// Angular derivative matrices (src/ndt_cuda/src/derivatives/angular.rs:37-189):
-// A[k] = dR/d(theta_k) for roll, pitch, yaw; B[kl] = d2R/d(theta_k)d(theta_l) for
-// kl = rr, rp, ry, pp, py, yy. `small` applies the CPU path's |angle| < 1e-5 rule.
-__device__ void angular_mats(const double* pose, bool small, double A[3][9], double B[6][9]) {
-    double sx, cx, sy, cy, sz, cz;
-    sincos(pose[3], &sx, &cx);
-    sincos(pose[4], &sy, &cy);
-    sincos(pose[5], &sz, &cz);
-    if (small) {
-        if (fabs(pose[3]) < 1e-5) sx = 0.0, cx = 1.0;
-        if (fabs(pose[4]) < 1e-5) sy = 0.0, cy = 1.0;
-        if (fabs(pose[5]) < 1e-5) sz = 0.0, cz = 1.0;
-    }
-    const double j[8][3] = {
-        {-sx * sz + cx * sy * cz, -sx * cz - cx * sy * sz, -cx * cy},
-        {cx * sz + sx * sy * cz, cx * cz - sx * sy * sz, -sx * cy},
-        {-sy * cz, sy * sz, cy},
-        {sx * cy * cz, -sx * cy * sz, sx * sy},
-        {-cx * cy * cz, cx * cy * sz, -cx * sy},
-        {-cy * sz, -cy * cz, 0.0},
-        {cx * cz - sx * sy * sz, -cx * sz - sx * sy * cz, 0.0},
-        {sx * cz + cx * sy * sz, cx * sy * cz - sx * sz, 0.0},
-    };
-    const double h[15][3] = {
-        {-cx * sz - sx * sy * cz, -cx * cz + sx * sy * sz, sx * cy},
-        {-sx * sz + cx * sy * cz, -cx * sy * sz - sx * cz, -cx * cy},
-        {cx * cy * cz, -cx * cy * sz, cx * sy},
-        {sx * cy * cz, -sx * cy * sz, sx * sy},
-        {-sx * cz - cx * sy * sz, sx * sz - cx * sy * cz, 0.0},
-        {cx * cz - sx * sy * sz, -sx * sy * cz - cx * sz, 0.0},
-        {-cy * cz, cy * sz, sy},
-        {-sx * sy * cz, sx * sy * sz, sx * cy},
-        {cx * sy * cz, -cx * sy * sz, -cx * cy},
-        {sy * sz, sy * cz, 0.0},
-        {-sx * cy * sz, -sx * cy * cz, 0.0},
-        {cx * cy * sz, cx * cy * cz, 0.0},
-        {-cy * cz, cy * sz, 0.0},
-        {-cx * sz - sx * sy * cz, -cx * cz + sx * sy * sz, 0.0},
-        {-sx * sz + cx * sy * cz, -cx * sy * sz - sx * cz, 0.0},
-    };
-    for (int q = 0; q < 9; ++q) {
-        A[0][q] = 0.0;
-        for (int k = 0; k < 6; ++k) B[k][q] = 0.0;
-    }
-    for (int c = 0; c < 3; ++c) {
-        A[0][3 + c] = j[0][c];
-        A[0][6 + c] = j[1][c];
-        A[1][c] = j[2][c];
-        A[1][3 + c] = j[3][c];
-        A[1][6 + c] = j[4][c];
-        A[2][c] = j[5][c];
-        A[2][3 + c] = j[6][c];
-        A[2][6 + c] = j[7][c];
-        B[0][3 + c] = h[0][c];   // roll-roll   a = [0, a2, a3]
-        B[0][6 + c] = h[1][c];
-        B[1][3 + c] = h[2][c];   // roll-pitch  b
-        B[1][6 + c] = h[3][c];
-        B[2][3 + c] = h[4][c];   // roll-yaw    c
-        B[2][6 + c] = h[5][c];
-        B[3][c] = h[6][c];       // pitch-pitch d
-        B[3][3 + c] = h[7][c];
-        B[3][6 + c] = h[8][c];
-        B[4][c] = h[9][c];       // pitch-yaw   e
-        B[4][3 + c] = h[10][c];
-        B[4][6 + c] = h[11][c];
-        B[5][c] = h[12][c];      // yaw-yaw     f
-        B[5][3 + c] = h[13][c];
-        B[5][6 + c] = h[14][c];
-    }
-}
+// Entries of R = Rx(roll) Ry(pitch) Rz(yaw), of A_k = dR/dtheta_k and of
+// B_kl = d2R/dtheta_k dtheta_l (kl = rr, rp, ry, pp, py, yy) — ten row-major 3x3 matrices,
+// 90 entries, in the order R, A_r, A_p, A_y, B_rr, B_rp, B_ry, B_pp, B_py, B_yy — written
+// as polynomials in f = {sin r, cos r, sin p, cos p, sin y, cos y, 1}: every entry is
+// c0 f[i0] f[i1] f[i2] + c1 f[j0] f[j1] f[j2] with c0, c1 in {0, +1, -1}. These are the
+// entries of the reference's angular tables (src/ndt_cuda/src/derivatives/angular.rs:37-189,
+// src/cuda_ffi/csrc/persistent_ndt_device.cuh:38-242): the derivatives of R, except that
+// B_pp[0][2] is +sin p where d2R/dpitch2 has -sin p — the reference's point-Hessian term
+// h_ang[(6, 2)] = sy (angular.rs:136-139, the PCL convention it follows), kept for parity.
+// Word layout: bits 0-8 hold the three 3-bit factor indices of term 0 (6 = the constant 1),
+// bits 9-17 those of term 1, bits 18-19 / 20-21 the coefficient codes of terms 0 / 1
+// (0: 0, 1: +1, 2: -1).
+__device__ const uint32_t FRAME_TERMS[90] = {
+    0x076dabu, 0x0b6da3u, 0x076db2u, 0x150ba1u, 0x2621a9u, 0x0b6d83u,
+    0x2553a0u, 0x162385u, 0x076d99u, 0x036db6u, 0x036db6u, 0x036db6u,
+    0x1953a0u, 0x2a2385u, 0x0b6d99u, 0x150ba1u, 0x2621a9u, 0x0b6d83u,
+    0x0b6d95u, 0x076da2u, 0x076db3u, 0x076c2bu, 0x0b6d03u, 0x076d90u,
+    0x0b6d59u, 0x076d19u, 0x0b6d91u, 0x0b6da3u, 0x0b6dabu, 0x036db6u,
+    0x2621a9u, 0x290ba1u, 0x036db6u, 0x162385u, 0x1953a0u, 0x036db6u,
+    0x036db6u, 0x036db6u, 0x036db6u, 0x290ba1u, 0x1a21a9u, 0x076d83u,
+    0x1953a0u, 0x2a2385u, 0x0b6d99u, 0x036db6u, 0x036db6u, 0x036db6u,
+    0x076d59u, 0x0b6d19u, 0x076d91u, 0x076c2bu, 0x0b6d03u, 0x076d90u,
+    0x036db6u, 0x036db6u, 0x036db6u, 0x2a2385u, 0x2553a0u, 0x036db6u,
+    0x2621a9u, 0x290ba1u, 0x036db6u, 0x0b6dabu, 0x076da3u, 0x076db2u,
+    0x0b6c85u, 0x076d10u, 0x076d83u, 0x076ca9u, 0x0b6d11u, 0x0b6d99u,
+    0x076da2u, 0x076d95u, 0x036db6u, 0x0b6d03u, 0x0b6c2bu, 0x036db6u,
+    0x076d19u, 0x076d59u, 0x036db6u, 0x0b6dabu, 0x076da3u, 0x036db6u,
+    0x290ba1u, 0x1a21a9u, 0x036db6u, 0x1953a0u, 0x2a2385u, 0x036db6u,
+};
 
-// Per-iteration frame for the per-point work: R = Rx(roll) Ry(pitch) Rz(yaw) and t as
-// hi/lo f32 pairs (hi = fl(v), lo = fl(v - hi)), and the angular Jacobian matrices A_k in f32.
-__device__ __noinline__ void make_frame(const double* pose, bool small, float* fr) {
-    double sr, cr, sp, cp, sy, cy;
-    sincos(pose[3], &sr, &cr);
-    sincos(pose[4], &sp, &cp);
-    sincos(pose[5], &sy, &cy);
-    double v[12] = {cp * cy, -cp * sy, sp,
-                    sr * sp * cy + cr * sy, cr * cy - sr * sp * sy, -sr * cp,
-                    sr * sy - cr * sp * cy, cr * sp * sy + sr * cy, cr * cp,
-                    pose[0], pose[1], pose[2]};
-    for (int i = 0; i < 12; ++i) {
-        float h = (float)v[i];
-        fr[i] = h;
-        fr[12 + i] = (float)(v[i] - (double)h);
+// Per-pose frame, computed by the 32 lanes of one warp (FP64 work is spread over the lanes:
+// one FP64 warp instruction costs the same with one lane active or 32). Lanes 0-2 evaluate
+// sin/cos of roll, pitch, yaw; every lane then evaluates up to three of the 90 table
+// entries. Outputs: the f32 frame of the point work (R and t as hi/lo pairs, A_k in f32) and
+// A_k, B_kl in FP64 for assembling g and H at this pose. `small` applies the CPU path's
+// |angle| < 1e-5 rule (sin = 0, cos = 1) to A_k and B_kl (angular.rs), not to R.
+__device__ __noinline__ void make_frame_warp(const double* pose, bool small, float* fr,
+                                             double* trig, double* Ad, double* Bd, int lane) {
+    if (lane < 3) {
+        double s, c;
+        sincos(pose[3 + lane], &s, &c);
+        trig[2 * lane] = s;
+        trig[2 * lane + 1] = c;
+        const bool tiny = small && fabs(pose[3 + lane]) < 1e-5;
+        trig[8 + 2 * lane] = tiny ? 0.0 : s;
+        trig[9 + 2 * lane] = tiny ? 1.0 : c;
+        const double t = pose[lane];
+        const float h = (float)t;
+        fr[9 + lane] = h;
+        fr[21 + lane] = (float)(t - (double)h);
     }
-    double A[3][9], B[6][9];
-    angular_mats(pose, small, A, B);
-    for (int k = 0; k < 3; ++k)
-        for (int q = 0; q < 9; ++q) fr[24 + 9 * k + q] = (float)A[k][q];
+    if (lane == 3) {
+        trig[6] = 1.0;
+        trig[14] = 1.0;
+    }
+    __syncwarp();
+    for (int e = lane; e < 90; e += 32) {
+        const uint32_t w = __ldg(FRAME_TERMS + e);
+        const double* f = e < 9 ? trig : trig + 8;
+        const double t0 = f[w & 7u] * f[(w >> 3) & 7u] * f[(w >> 6) & 7u];
+        const double t1 = f[(w >> 9) & 7u] * f[(w >> 12) & 7u] * f[(w >> 15) & 7u];
+        const uint32_t c0 = (w >> 18) & 3u, c1 = (w >> 20) & 3u;
+        const double v = (c0 == 0u ? 0.0 : (c0 == 1u ? t0 : -t0)) +
+                         (c1 == 0u ? 0.0 : (c1 == 1u ? t1 : -t1));
+        if (e < 9) {
+            const float h = (float)v;
+            fr[e] = h;
+            fr[12 + e] = (float)(v - (double)h);
+        } else if (e < 36) {
+            fr[24 + (e - 9)] = (float)v;
+            Ad[e - 9] = v;
+        } else {
+            Bd[e - 36] = v;
+        }
+    }
+    __syncwarp();
 }
 
 // ------------------------------------------------------------------------------------
@@ -173,21 +162,32 @@ __constant__ int8_t RR_PAIRS[5][3][2] = {
     {{0, 1}, {2, 5}, {3, 4}}, {{0, 2}, {1, 3}, {4, 5}}, {{0, 3}, {2, 4}, {1, 5}},
     {{0, 4}, {3, 5}, {1, 2}}, {{0, 5}, {1, 4}, {2, 3}}};
 
-// Warp-parallel Jacobi eigen-decomposition of the symmetric 6x6 in `A` (FP64, shared memory):
-// A becomes diagonal, V accumulates the rotations. Rotation angles and stopping rules follow
-// the reference's jacobi_svd_6x6.cuh:135-210 (tau formula, skip |a_pq| < 1e-15, stop when
-// 2 sum(offdiag^2) < 1e-28 sum(diag^2), <= 30 sweeps); the sweep order is parallel
-// round-robin instead of cyclic-by-row, which changes results only by FP64 rounding. Every
-// FP64 instruction does the work of up to 32 lanes (the FP64 pipe is narrow on this GPU).
-__device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int lane) {
-    if (lane < 36 - 32) V[32 + lane] = ((32 + lane) % 7 == 0) ? 1.0 : 0.0;
-    V[lane] = (lane % 7 == 0) ? 1.0 : 0.0;
+__device__ __forceinline__ float rsq(float v) { return rsqrtf(v); }
+__device__ __forceinline__ double rsq(double v) { return rsqrt(v); }
+
+// Warp-parallel Jacobi eigen-decomposition of the symmetric 6x6 in `A` (shared memory, type
+// T): A becomes diagonal and V accumulates the rotations, V <- V J, from the identity or,
+// when init_v is false, from the orthogonal V the caller left there. Rotation angles and
+// stopping rules follow the reference's jacobi_svd_6x6.cuh:135-210 (no rotation when
+// |a_pq| < skip; stop when 2 sum(offdiag^2) < stop * sum(diag^2); at most max_sweeps); the
+// sweep order is parallel round-robin instead of cyclic-by-row, which changes results only
+// by rounding. The tangent t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)) with
+// theta = (a_qq - a_pp) / (2 a_pq) is evaluated as
+// sgn(theta) |2 a_pq| / (|a_qq - a_pp| + sqrt((a_qq - a_pp)^2 + (2 a_pq)^2)) (one division),
+// and c = 1 / sqrt(t^2 + 1) as a reciprocal square root. Returns the sweeps that rotated.
+template <typename T>
+__device__ __noinline__ int jacobi6_warp(T* A, T* V, T* cs, int lane, bool init_v, T skip,
+                                         T stop, int max_sweeps) {
+    if (init_v) {
+        if (lane < 36 - 32) V[32 + lane] = ((32 + lane) % 7 == 0) ? T(1) : T(0);
+        V[lane] = (lane % 7 == 0) ? T(1) : T(0);
+    }
     __syncwarp();
     int sweeps = 0;
-    for (int sweep = 0; sweep < 30; ++sweep) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         // convergence test (lane i < 6 owns diagonal i; lanes < 15 own one off-diagonal pair)
-        double dg = lane < 6 ? A[lane * 7] * A[lane * 7] : 0.0;
-        double off = 0.0;
+        T dg = lane < 6 ? A[lane * 7] * A[lane * 7] : T(0);
+        T off = T(0);
         if (lane < 15) {
             int p = RR_PAIRS[lane / 3][lane % 3][0], q = RR_PAIRS[lane / 3][lane % 3][1];
             off = A[p * 6 + q] * A[p * 6 + q];
@@ -197,18 +197,18 @@ __device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int l
             dg += __shfl_xor_sync(0xffffffffu, dg, o);
             off += __shfl_xor_sync(0xffffffffu, off, o);
         }
-        if (2.0 * off < 1e-28 * dg) break;
+        if (T(2) * off < stop * dg) break;
         sweeps++;
         for (int r = 0; r < 5; ++r) {
             if (lane < 3) {
                 int p = RR_PAIRS[r][lane][0], q = RR_PAIRS[r][lane][1];
-                double apq = A[p * 6 + q];
-                double c = 1.0, sn = 0.0;
-                if (fabs(apq) >= 1e-15) {
-                    double tau = (A[q * 6 + q] - A[p * 6 + p]) / (2.0 * apq);
-                    double t = tau >= 0.0 ? 1.0 / (tau + sqrt(tau * tau + 1.0))
-                                          : -1.0 / (-tau + sqrt(tau * tau + 1.0));
-                    c = 1.0 / sqrt(t * t + 1.0);
+                T apq = A[p * 6 + q];
+                T c = T(1), sn = T(0);
+                if (fabs(apq) >= skip) {
+                    const T d = A[q * 6 + q] - A[p * 6 + p], a = T(2) * apq;
+                    T t = fabs(a) / (fabs(d) + sqrt(d * d + a * a));
+                    if (d * a < T(0)) t = -t;  // theta = d / a < 0; theta = 0 counts as +
+                    c = rsq(t * t + T(1));
                     sn = t * c;
                 }
                 cs[2 * lane] = c;
@@ -217,7 +217,7 @@ __device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int l
             __syncwarp();
             // rotation of index i: partner j and coefficients (own, partner) of row i of J^T
             // (p: c, -s; q: s, c)
-            double nA0 = 0.0, nV0 = 0.0, nV1 = 0.0;
+            T nA0 = T(0), nV0 = T(0), nV1 = T(0);
             int ai = 0, aj = 0;
             if (lane < 21) {  // upper-triangle entry (ai <= aj)
                 int t = lane;
@@ -228,7 +228,7 @@ __device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int l
                 }
                 aj = ai + t;
             }
-            auto coef = [&](int i, int& partner, double& cown, double& cpart) {
+            auto coef = [&](int i, int& partner, T& cown, T& cpart) {
                 for (int k = 0; k < 3; ++k) {
                     int p = RR_PAIRS[r][k][0], q = RR_PAIRS[r][k][1];
                     if (i == p) {
@@ -244,27 +244,27 @@ __device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int l
             };
             if (lane < 21) {
                 int pi, pj;
-                double ci, si, cj, sj;
+                T ci, si, cj, sj;
                 coef(ai, pi, ci, si);
                 coef(aj, pj, cj, sj);
                 if (pi == aj) {  // rotated pair itself: zeroed by construction
-                    nA0 = 0.0;
+                    nA0 = T(0);
                 } else {
-                    double a_ij = A[ai * 6 + aj], a_ipj = A[pi * 6 + aj];
-                    double a_ijp = A[ai * 6 + pj], a_ipjp = A[pi * 6 + pj];
+                    T a_ij = A[ai * 6 + aj], a_ipj = A[pi * 6 + aj];
+                    T a_ijp = A[ai * 6 + pj], a_ipjp = A[pi * 6 + pj];
                     nA0 = ci * (cj * a_ij + sj * a_ijp) + si * (cj * a_ipj + sj * a_ipjp);
                 }
             }
             // V' = V J: column j mixes with its partner
             {
                 int vi = lane / 6, vj = lane % 6, pj;
-                double cj, sj;
+                T cj, sj;
                 coef(vj, pj, cj, sj);
                 nV0 = cj * V[vi * 6 + vj] + sj * V[vi * 6 + pj];
                 if (lane < 4) {
                     int e = 32 + lane;
                     int wi = e / 6, wj = e % 6, pw;
-                    double cw, sw;
+                    T cw, sw;
                     coef(wj, pw, cw, sw);
                     nV1 = cw * V[wi * 6 + wj] + sw * V[wi * 6 + pw];
                 }
@@ -282,116 +282,252 @@ __device__ __noinline__ int jacobi6_warp(double* A, double* V, double* cs, int l
     return sweeps;
 }
 
-// Cholesky of a symmetric matrix (one lane); false if a pivot is not positive or the pivot
-// ratio falls below 1e-6 (then the caller takes the eigen path).
-__device__ __noinline__ bool chol6(const double* M, double* L) {
-    double dmin = 1e300, dmax = 0.0;
-    for (int i = 0; i < 6; ++i) {
-        for (int j = 0; j <= i; ++j) {
-            double s = M[i * 6 + j];
-            for (int k = 0; k < j; ++k) s -= L[i * 6 + k] * L[j * 6 + k];
-            if (i == j) {
-                if (!(s > 0.0)) return false;
-                dmin = fmin(dmin, s);
-                dmax = fmax(dmax, s);
-                L[i * 6 + i] = sqrt(s);
-            } else {
-                L[i * 6 + j] = s / L[j * 6 + j];
-            }
+// f32 Cholesky of s*H (s = +1 or -1; H symmetric FP64) by one lane. Every index is a
+// compile-time constant, so the factor stays in registers: L lower triangular, packed by
+// rows, and rinv[j] = 1 / L_jj. False if a pivot is not positive or the pivot ratio falls
+// below 1e-6 (the caller then takes the eigen path).
+struct Chol32 {
+    float L[21];
+    float rinv[6];
+};
+
+__device__ __forceinline__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__device__ __forceinline__ bool chol6f(const double* H, float sgn, Chol32& C) {
+    float dmin = 3.0e38f, dmax = 0.f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        float s = sgn * (float)H[j * 6 + j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) s = fmaf(-C.L[tri(j, k)], C.L[tri(j, k)], s);
+        if (!(s > 0.f)) return false;
+        dmin = fminf(dmin, s);
+        dmax = fmaxf(dmax, s);
+        const float r = rsqrtf(s);
+        C.rinv[j] = r;
+        C.L[tri(j, j)] = s * r;
+#pragma unroll
+        for (int i = j + 1; i < 6; ++i) {
+            float t = sgn * (float)H[i * 6 + j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) t = fmaf(-C.L[tri(i, k)], C.L[tri(j, k)], t);
+            C.L[tri(i, j)] = t * r;
         }
     }
-    return dmin > 1e-6 * dmax;
+    return dmin > 1e-6f * dmax;
 }
 
-__device__ void chol6_solve(const double* L, const double* b, double* x) {
-    double y[6];
+// x = (L L^T)^-1 b in f32
+__device__ __forceinline__ void chol6f_solve(const Chol32& C, const float* b, float* x) {
+    float y[6];
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
-        double s = b[i];
-        for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
-        y[i] = s / L[i * 6 + i];
+        float s = b[i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) s = fmaf(-C.L[tri(i, k)], y[k], s);
+        y[i] = s * C.rinv[i];
     }
+#pragma unroll
     for (int i = 5; i >= 0; --i) {
-        double s = y[i];
-        for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * x[k];
-        x[i] = s / L[i * 6 + i];
+        float s = y[i];
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) s = fmaf(-C.L[tri(k, i)], x[k], s);
+        x[i] = s * C.rinv[i];
     }
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
 // Newton step for both semantics; all 32 lanes of one warp call it, result in S.x / S.ok.
 //  graph (K3): x = V diag(1/|lambda|) V^T (-g), |lambda| > max(1e-10 max|lambda|, 1e-15)
 //              (jacobi_svd_solve_6x6_f64); definite H: x = (sH)^-1 (-g), s = sign
 //  cpu       : newton_step_negative_definite(g, H, -1e-3, 1e-10) (newton.rs:160-176)
+// Definite, well-conditioned H takes the Cholesky path (the negative-definite case, a
+// maximum of the score, is tried first). Otherwise the eigen path runs Jacobi in f32 to
+// convergence, makes the f32 eigenvectors orthogonal to FP64 rounding (two Newton-Schulz
+// steps V <- V (3I - V^T V) / 2), and finishes with FP64 Jacobi sweeps on V^T H V under the
+// reference's FP64 stopping rule: FP64 eigenpairs at a fraction of the FP64 sweeps.
 template <bool CPU_SEM>
 __device__ __noinline__ void solve_warp(const double* H, const double* g, SolveScratch& S,
                                         int lane) {
+    // Definite fast path: f32 Cholesky factor of (s H), then mixed-precision iterative
+    // refinement — the residual r = b - (s H) x in FP64 (lane i owns row i), the correction
+    // solved with the f32 factor — until the last correction is below 1e-13 of x (four f32
+    // solves reach FP64 accuracy while cond(H) stays below about 1e4; worse-conditioned
+    // definite Hessians take the eigen path).
+    Chol32 C;
+    int sgn = 0;
     if (lane == 0) {
-        double M[36], L[36];
         S.ok = 0;
         S.path = 1;
-        for (int sgn = 1; sgn >= -1; sgn -= 2) {
-            if (CPU_SEM && sgn == 1) continue;  // only the negative-definite fast path
-            for (int i = 0; i < 36; ++i) M[i] = sgn * H[i];
-            if (chol6(M, L)) {
-                double b[6];
-                for (int i = 0; i < 6; ++i) b[i] = CPU_SEM ? g[i] : -g[i];
-                chol6_solve(L, b, S.x);
-                S.ok = 1;
-                S.path = 0;
+        S.sweeps = 0;
+        for (int s = -1; s <= 1; s += 2) {
+            if (CPU_SEM && s == 1) continue;  // only the negative-definite fast path
+            if (chol6f(H, (float)s, C)) {
+                sgn = s;
                 break;
             }
         }
     }
-    __syncwarp();
-    if (S.path == 0) return;
-    S.A[lane] = H[lane];
-    if (lane < 4) S.A[32 + lane] = H[32 + lane];
-    __syncwarp();
-    jacobi6_warp(S.A, S.V, S.cs, lane);
-    if (lane == 0) {
-        double lam[6];
-        for (int i = 0; i < 6; ++i) lam[i] = S.A[i * 7];
-        double thr;
-        bool use_abs;
-        if (!CPU_SEM) {
-            double mx = 0.0;
-            for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(lam[i]));
-            thr = fmax(1e-10 * mx, 1e-15);
-            use_abs = true;
-        } else {
-            bool nd = true;
-            for (int i = 0; i < 6; ++i)
-                if (!(lam[i] < 0.0)) nd = false;
-            if (!nd)
-                for (int i = 0; i < 6; ++i)
-                    if (lam[i] > -1e-3) lam[i] = -1e-3;
-            double mx = 0.0;
-            for (int i = 0; i < 6; ++i) mx = fmax(mx, fabs(lam[i]));
-            thr = 1e-10;
-            use_abs = false;
-            if (mx < 1e-10) {
-                S.ok = 0;
-                return;
+    sgn = __shfl_sync(0xffffffffu, sgn, 0);
+    if (sgn != 0) {
+        const double b = lane < 6 ? (CPU_SEM ? g[lane] : -g[lane]) : 0.0;
+        double x = 0.0, r = b;
+        bool conv = false;
+        for (int ref = 0; ref < 4; ++ref) {
+            if (lane < 6) S.cs[lane] = r;
+            __syncwarp();
+            if (lane == 0) {
+                float rf[6], dx[6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i) rf[i] = (float)S.cs[i];
+                chol6f_solve(C, rf, dx);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) S.T[i] = (double)dx[i];
+            }
+            __syncwarp();
+            float adx = 0.f, ax = 0.f;
+            if (lane < 6) {
+                const double d = S.T[lane];
+                x += d;
+                S.x[lane] = x;
+                adx = fabsf((float)d);
+                ax = fabsf((float)x);
+            }
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) ax = fmaxf(ax, __shfl_xor_sync(0xffffffffu, ax, o));
+            ax = __shfl_sync(0xffffffffu, ax, 0);
+            conv = __all_sync(0xffffffffu, adx <= 1e-13f * ax);
+            if (conv) break;
+            __syncwarp();
+            if (lane < 6) {
+                double t = b;
+                for (int j = 0; j < 6; ++j) t = fma(-(double)sgn * H[lane * 6 + j], S.x[j], t);
+                r = t;
             }
         }
-        double z[6];
-        int nz = 0;
-        for (int i = 0; i < 6; ++i) {
-            double y = 0.0;
-            for (int j = 0; j < 6; ++j) y += S.V[j * 6 + i] * (-g[j]);
-            double al = fabs(lam[i]);
-            if (al > thr) {
-                z[i] = y / (use_abs ? al : lam[i]);
-                nz++;
-            } else {
-                z[i] = 0.0;
+        if (conv) {
+            if (lane == 0) {
+                S.ok = 1;
+                S.path = 0;
             }
+            __syncwarp();
+            return;
         }
-        for (int i = 0; i < 6; ++i) {
+    }
+    __syncwarp();
+    // f32 Jacobi
+    S.A32[lane] = (float)H[lane];
+    if (lane < 4) S.A32[32 + lane] = (float)H[32 + lane];
+    __syncwarp();
+    jacobi6_warp<float>(S.A32, S.V32, S.cs32, lane, true, 1e-30f, 1e-12f, 20);
+    S.V[lane] = (double)S.V32[lane];
+    if (lane < 4) S.V[32 + lane] = (double)S.V32[32 + lane];
+    __syncwarp();
+    // Newton-Schulz: T = 3I - V^T V; V <- V T / 2 (via A as scratch)
+    for (int ns = 0; ns < 2; ++ns) {
+        for (int e = lane; e < 36; e += 32) {
+            const int i = e / 6, j = e % 6;
             double s = 0.0;
-            for (int j = 0; j < 6; ++j) s += S.V[i * 6 + j] * z[j];
-            S.x[i] = s;
+            for (int k = 0; k < 6; ++k) s = fma(S.V[k * 6 + i], S.V[k * 6 + j], s);
+            S.T[e] = (i == j ? 3.0 : 0.0) - s;
         }
+        __syncwarp();
+        for (int e = lane; e < 36; e += 32) {
+            const int i = e / 6, j = e % 6;
+            double s = 0.0;
+            for (int k = 0; k < 6; ++k) s = fma(S.V[i * 6 + k], S.T[k * 6 + j], s);
+            S.A[e] = 0.5 * s;
+        }
+        __syncwarp();
+        S.V[lane] = S.A[lane];
+        if (lane < 4) S.V[32 + lane] = S.A[32 + lane];
+        __syncwarp();
+    }
+    // A = V^T H V (T = H V), symmetrised
+    for (int e = lane; e < 36; e += 32) {
+        const int i = e / 6, j = e % 6;
+        double s = 0.0;
+        for (int k = 0; k < 6; ++k) s = fma(H[i * 6 + k], S.V[k * 6 + j], s);
+        S.T[e] = s;
+    }
+    __syncwarp();
+    for (int e = lane; e < 36; e += 32) {
+        const int i = e / 6, j = e % 6;
+        double s = 0.0;
+        for (int k = 0; k < 6; ++k) s = fma(S.V[k * 6 + i], S.T[k * 6 + j], s);
+        S.A[e] = s;
+    }
+    __syncwarp();
+    {
+        double v = 0.0;
+        int ai = 0, aj = 0;
+        if (lane < 21) {
+            int t = lane;
+            while (t >= 6 - ai) {
+                t -= 6 - ai;
+                ++ai;
+            }
+            aj = ai + t;
+            v = 0.5 * (S.A[ai * 6 + aj] + S.A[aj * 6 + ai]);
+        }
+        __syncwarp();
+        if (lane < 21) {
+            S.A[ai * 6 + aj] = v;
+            S.A[aj * 6 + ai] = v;
+        }
+        __syncwarp();
+    }
+    const int sw = jacobi6_warp<double>(S.A, S.V, S.cs, lane, false, 1e-15, 1e-28, 30);
+    // pseudo-inverse step from the eigenpairs, lane i < 6 owning eigenpair i
+    double lam = lane < 6 ? S.A[lane * 7] : 0.0;
+    double thr;
+    bool use_abs;
+    if (!CPU_SEM) {
+        const double mx = warp_max(lane < 6 ? fabs(lam) : 0.0);
+        thr = fmax(1e-10 * mx, 1e-15);
+        use_abs = true;
+    } else {
+        const bool nd = __all_sync(0xffffffffu, lane >= 6 || lam < 0.0);
+        if (!nd && lane < 6 && lam > -1e-3) lam = -1e-3;
+        const double mx = warp_max(lane < 6 ? fabs(lam) : 0.0);
+        thr = 1e-10;
+        use_abs = false;
+        if (mx < 1e-10) {
+            if (lane == 0) {
+                S.ok = 0;
+                S.sweeps = sw;
+            }
+            __syncwarp();
+            return;
+        }
+    }
+    bool keep = false;
+    if (lane < 6) {
+        double y = 0.0;
+        for (int j = 0; j < 6; ++j) y += S.V[j * 6 + lane] * (-g[j]);
+        const double al = fabs(lam);
+        double z = 0.0;
+        if (al > thr) {
+            z = y / (use_abs ? al : lam);
+            keep = true;
+        }
+        S.cs[lane] = z;
+    }
+    const int nz = __popc(__ballot_sync(0xffffffffu, keep));
+    __syncwarp();
+    if (lane < 6) {
+        double s = 0.0;
+        for (int j = 0; j < 6; ++j) s += S.V[lane * 6 + j] * S.cs[j];
+        S.x[lane] = s;
+    }
+    if (lane == 0) {
         S.ok = CPU_SEM ? 1 : (nz > 0);
+        S.sweeps = sw;
     }
     __syncwarp();
 }
@@ -550,10 +686,11 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
 }
 
 // g (6) and H (6x6) in FP64 from the reduced accumulators; lanes of one warp share the work.
-__device__ __noinline__ void finalize_gH(const double* tot, const double* pose, bool small, double* g,
-                            double* H, int lane) {
-    double A[3][9], B[6][9];
-    angular_mats(pose, small, A, B);
+// Ad / Bd: A_k and B_kl at the pose the accumulators were taken at (make_frame_warp).
+__device__ __noinline__ void finalize_gH(const double* tot, const double* Ad, const double* Bd,
+                                         double* g, double* H, int lane) {
+    const double(*A)[9] = reinterpret_cast<const double(*)[9]>(Ad);
+    const double(*B)[9] = reinterpret_cast<const double(*)[9]>(Bd);
     const double* GP = tot + A_GP;
     if (lane < 6) {
         double v;
@@ -703,6 +840,60 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
     return 0;
 }
 
+// TwoSum: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+// Warp sums of the NACC per-thread accumulators, compensated (two-sum) and written as FP64
+// to out[0..NACC). Values 0..31 are reduced by recursive halving: at each exchange a lane
+// sends the half of its remaining values that its partner keeps, so lane l ends holding the
+// sum of value l (31 exchanges instead of 5 per value). Values 32.. use a butterfly.
+__device__ __forceinline__ void warp_sum_acc(const float* acc, int lane, double* out) {
+    static_assert(NACC >= 32, "recursive halving covers 32 values");
+    float s[16], c[16];
+    {
+        const bool up = (lane & 16) != 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float send = up ? acc[j] : acc[j + 16];
+            const float keep = up ? acc[j + 16] : acc[j];
+            const float recv = __shfl_xor_sync(0xffffffffu, send, 16);
+            two_sum(keep, recv, s[j], c[j]);
+        }
+    }
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < o; ++j) {
+            const float ss = up ? s[j] : s[j + o], cs = up ? c[j] : c[j + o];
+            const float sk = up ? s[j + o] : s[j], ck = up ? c[j + o] : c[j];
+            const float sr = __shfl_xor_sync(0xffffffffu, ss, o);
+            const float cr = __shfl_xor_sync(0xffffffffu, cs, o);
+            float e;
+            two_sum(sk, sr, s[j], e);
+            c[j] = ck + cr + e;
+        }
+    }
+    out[lane] = (double)s[0] + (double)c[0];
+#pragma unroll
+    for (int k = 32; k < NACC; ++k) {
+        float v = acc[k], cv = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float vo = __shfl_xor_sync(0xffffffffu, v, o);
+            const float co = __shfl_xor_sync(0xffffffffu, cv, o);
+            float e;
+            two_sum(v, vo, v, e);
+            cv = cv + co + e;
+        }
+        if (lane == 0) out[k] = (double)v + (double)cv;
+    }
+}
+
 // REGCAP: registers per thread the launch bounds allow (128: the default; 80: more resident
 // CTAs per SM at the price of a few spills; the autotuner picks)
 template <int THREADS, bool CPU_SEM, int REGCAP>
@@ -733,8 +924,9 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         sh.osc = sh.max_osc = 0;
         for (int i = 0; i < 36; ++i) sh.last_H[i] = 0.0;
         sh.done = 0;
-        make_frame(sh.pose, CPU_SEM, sh.fr);
     }
+    __syncthreads();
+    if (warp == 0) make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
     __syncthreads();
 
     uint64_t point_iters = 0, corr_total = 0;
@@ -756,25 +948,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             point_terms<CPU_SEM>(m, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, nc,
                                  nbl_smem + tid, THREADS);
         }
-        // warp: two-sum compensated butterfly, then FP64 (fully unrolled: acc[] stays in
-        // registers)
-#pragma unroll
-        for (int k = 0; k < NACC; ++k) {
-            float s = acc[k], c = 0.f;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                float so = __shfl_xor_sync(0xffffffffu, s, o);
-                float co = __shfl_xor_sync(0xffffffffu, c, o);
-                float t = s + so;
-                float bp = t - s;
-                float err = (s - (t - bp)) + (so - bp);
-                s = t;
-                c = c + co + err;
-            }
-            if (lane == 0) sh.warp_part[warp][k] = (double)s + (double)c;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nc += __shfl_xor_sync(0xffffffffu, nc, o);
+        warp_sum_acc(acc, lane, sh.warp_part[warp]);
+        nc = __reduce_add_sync(0xffffffffu, nc);
         if (lane == 0) sh.warp_part[warp][NACC] = (double)nc;
         __syncthreads();
         for (int k = tid; k < NRED; k += THREADS) {
@@ -796,13 +971,17 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             }
             __syncthreads();
             if (warp == 0) {
-                finalize_gH(sh.tot, sh.pose, CPU_SEM, sh.g, sh.H, lane);
+                const unsigned long long ca = clock64();
+                finalize_gH(sh.tot, sh.Ad, sh.Bd, sh.g, sh.H, lane);
                 __syncwarp();
+                const unsigned long long cb = clock64();
                 solve_warp<CPU_SEM>(sh.H, sh.g, sh.solve, lane);
+                const unsigned long long cc = clock64();
+                double* t = nullptr;
                 if (lane == 0) {
                     sh.n_eigen += sh.solve.path;
                     if (P.trace && it < P.max_iter) {  // per-iteration record (opt-in)
-                        double* t = P.trace + ((size_t)jid * P.max_iter + it) * TRACE_REC;
+                        t = P.trace + ((size_t)jid * P.max_iter + it) * TRACE_REC;
                         t[0] = it;
                         t[1] = sh.tot[A_SC];
                         t[2] = sh.tot[NACC];
@@ -826,10 +1005,16 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                         o.point_iters = point_iters;
                         o.corr_total = corr_total;
                     }
-                    make_frame(sh.pose, CPU_SEM, sh.fr);
                     sh.done = done;
                 }
                 __syncwarp();
+                make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                if (t) {  // controller sub-phase cycles: assembly, solve, step + next frame
+                    t[44] = (double)(cb - ca);
+                    t[45] = (double)(cc - cb);
+                    t[46] = (double)(clock64() - cc);
+                    t[47] = sh.solve.sweeps;
+                }
                 if (lane > 0 && lane < K) {
                     AlignShared* rs = cluster.map_shared_rank(&sh, lane);
                     for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];

@@ -147,6 +147,22 @@ int ndt_config_default(ndt_config* cfg) {
     return NDT_OK;
 }
 
+}  // extern "C"
+
+// Parameter ranges shared by create and configure; launch-shape knobs are 0 (automatic) or
+// one of the compiled variants.
+static bool config_ok(const ndt_config& c) {
+    const int K = c.cluster_size, T = c.threads_per_cta, R = c.max_registers;
+    return c.resolution > 0.f && c.max_iterations >= 1 && c.max_neighbors >= 1 &&
+           c.max_neighbors <= MAX_NB_ALL && c.step_size > 0.0 && c.outlier_ratio > 0.0 &&
+           c.outlier_ratio < 1.0 &&
+           (c.semantics == NDT_SEMANTICS_GPU_GRAPH || c.semantics == NDT_SEMANTICS_CPU) &&
+           (K == 0 || K == 1 || K == 2 || K == 4 || K == 8) &&
+           (T == 0 || T == 128 || T == 256 || T == 512) && (R == 0 || R == 80 || R == 128);
+}
+
+extern "C" {
+
 int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
     if (!out) return NDT_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -155,9 +171,7 @@ int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
         c = *cfg;
     else
         ndt_config_default(&c);
-    if (!(c.resolution > 0.f) || c.max_iterations < 1 || c.max_neighbors < 1 ||
-        c.max_neighbors > MAX_NB_ALL || !(c.step_size > 0.0) || !(c.outlier_ratio > 0.0) ||
-        !(c.outlier_ratio < 1.0)) {
+    if (!config_ok(c)) {
         set_error("invalid configuration");
         return NDT_ERR_INVALID_ARGUMENT;
     }
@@ -225,10 +239,7 @@ void* ndt_ctx_stream(ndt_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int ndt_ctx_configure(ndt_ctx* c, const ndt_config* cfg) {
     if (!c || !cfg) return NDT_ERR_INVALID_ARGUMENT;
     const ndt_config& n = *cfg;
-    if (!(n.resolution > 0.f) || n.max_iterations < 1 || n.max_neighbors < 1 ||
-        n.max_neighbors > MAX_NB_ALL || !(n.step_size > 0.0) || !(n.outlier_ratio > 0.0) ||
-        !(n.outlier_ratio < 1.0) || n.device != c->cfg.device ||
-        (n.semantics != NDT_SEMANTICS_GPU_GRAPH && n.semantics != NDT_SEMANTICS_CPU)) {
+    if (!config_ok(n) || n.device != c->cfg.device) {
         set_error("invalid configuration");
         return NDT_ERR_INVALID_ARGUMENT;
     }
@@ -396,6 +407,7 @@ static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
     sh.threads = c->cfg.threads_per_cta > 0
                      ? c->cfg.threads_per_cta
                      : (max_n >= 4096 ? 512 : (max_n >= 1024 ? 256 : 128));
+    if (c->cfg.max_registers > 0 && sh.threads <= 256) sh.regcap = c->cfg.max_registers;
     if (c->cfg.cluster_size > 0) {
         sh.cluster = c->cfg.cluster_size;
         return sh;

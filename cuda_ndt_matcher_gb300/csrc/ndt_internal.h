@@ -86,7 +86,9 @@ struct AlignOut {
 
 // Per-iteration trace record (doubles): it, score, correspondences, pose before the step (6),
 // gradient (6), Hessian upper triangle (21), raw solver output (6), solver path, solver ok,
-// 4 reserved. Same layout as the oracle's trace.
+// then 4 device-only fields: SM cycles of the g/H assembly, of the 6x6 solve and of the step
+// plus next frame, and the FP64 Jacobi sweeps of an eigen solve. Fields 0-43 have the same
+// layout as the oracle's trace (whose last 4 are zero).
 constexpr int TRACE_REC = 48;
 
 struct AlignParams {

@@ -67,7 +67,8 @@ typedef struct ndt_config {
     int32_t cluster_size;          /* CTAs per alignment; 0 = autotuned */
     int32_t threads_per_cta;       /* 0 = autotuned */
     int32_t hash_capacity_factor;  /* capacity = next pow2 >= factor * V; 2 = reference */
-    int32_t reserved[3];
+    int32_t max_registers;         /* Newton-kernel register cap (80 or 128); 0 = autotuned */
+    int32_t reserved[2];
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
