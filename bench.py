@@ -316,6 +316,8 @@ def run_ours(args):
             "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans, "
                                    "batched alignment", "batch": B, "scan_points": 20000,
                        "map_points": args.map_points, "map_voxels": int(info.num_voxels),
+                       "cell_index": (f"dense grid {info.dense_grid_mib:.1f} MiB"
+                                      if info.dense_grid_mib > 0 else "hash"),
                        "semantics": "graph kernels K1-K5", "l2": "flushed (256 MB write) "
                        "between steps",
                        "launch_shape": {"cluster_size": tune["cluster_size"],

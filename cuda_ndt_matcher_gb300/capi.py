@@ -47,7 +47,8 @@ class Config(C.Structure):
                 ("semantics", C.c_int32), ("min_correspondences", C.c_int32),
                 ("device", C.c_int32), ("cluster_size", C.c_int32),
                 ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
-                ("max_registers", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("max_registers", C.c_int32), ("cell_index", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -75,7 +76,7 @@ class MapInfo(C.Structure):
                 ("num_voxels", C.c_uint64), ("hash_capacity", C.c_uint64),
                 ("max_probe", C.c_uint32), ("key_bits", C.c_uint32 * 3),
                 ("min_coord", C.c_int32 * 3), ("max_coord", C.c_int32 * 3),
-                ("build_ms", C.c_float), ("reserved", C.c_float)]
+                ("build_ms", C.c_float), ("dense_grid_mib", C.c_float)]
 
 
 class Stats(C.Structure):

@@ -567,6 +567,39 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
     // shared memory, so the search runs with all lanes busy and the pair work below runs once
     // per listed voxel rather than once per cell
     int cnt = 0;
+    if (m.grid) {
+        // dense cell index: one 16-byte load per cell gives occupancy and centroid; the
+        // column's three cells (dz = -1, 0, 1) are adjacent entries
+        const uint32_t ux0 = (uint32_t)gc[0] - (uint32_t)m.min_cell[0];
+        const uint32_t uy0 = (uint32_t)gc[1] - (uint32_t)m.min_cell[1];
+        const uint32_t uz0 = (uint32_t)gc[2] - (uint32_t)m.min_cell[2];
+#pragma unroll 1
+        for (int c9 = 0; c9 < 9; ++c9) {
+            if (cnt >= max_nb) break;
+            const uint32_t ux = ux0 + (uint32_t)(c9 / 3 - 1), uy = uy0 + (uint32_t)(c9 % 3 - 1);
+            if (!grid_in(m, ux, uy)) continue;
+            const float4* col = m.grid + ((size_t)ux * m.ext[1] + uy) * m.ext[2];
+            float4 e[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t uz = uz0 + (uint32_t)(k - 1);
+                e[k] = uz < m.ext[2] ? __ldg(col + uz)
+                                     : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (cnt >= max_nb) break;
+                const int32_t s = __float_as_int(e[k].w);
+                if (s < 0) continue;
+                const float e0 = (qh[0] - e[k].x) + ql[0];
+                const float e1 = (qh[1] - e[k].y) + ql[1];
+                const float e2 = (qh[2] - e[k].z) + ql[2];
+                if (fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2) continue;
+                nbl[cnt * nbl_stride] = (uint32_t)s;
+                cnt++;
+            }
+        }
+    } else {
     const uint32_t bxy = m.bits[0] + m.bits[1];
     const uint32_t lz0 = (uint32_t)(gc[2] - m.min_cell[2]);
 #pragma unroll 1
@@ -606,6 +639,7 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
             nbl[cnt * nbl_stride] = (uint32_t)s;
             cnt++;
         }
+    }
     }
     if (cnt == 0) return;
     // ---- pairs: S, G, M aggregated over the listed voxels

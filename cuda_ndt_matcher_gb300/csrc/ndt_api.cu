@@ -158,7 +158,8 @@ static bool config_ok(const ndt_config& c) {
            c.outlier_ratio < 1.0 &&
            (c.semantics == NDT_SEMANTICS_GPU_GRAPH || c.semantics == NDT_SEMANTICS_CPU) &&
            (K == 0 || K == 1 || K == 2 || K == 4 || K == 8) &&
-           (T == 0 || T == 128 || T == 256 || T == 512) && (R == 0 || R == 80 || R == 128);
+           (T == 0 || T == 128 || T == 256 || T == 512) && (R == 0 || R == 80 || R == 128) &&
+           (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH);
 }
 
 extern "C" {

@@ -40,7 +40,18 @@ struct MapView {
     float r2;             // res * res (f32)
     uint32_t num_voxels;
     int32_t exact_inv;    // inv_res is a power of two (q * inv_res is exact in f32)
+    // dense cell index (null when the hash serves): grid[(lx * ext[1] + ly) * ext[2] + lz]
+    // = {centroid x, y, z, slot as int bits} of the voxel in local cell (lx, ly, lz), or
+    // slot -1 for an empty cell
+    const float4* grid;
+    uint32_t ext[3];
 };
+
+// Column (ux, uy) of local cells lies inside the dense index. Local coordinates are unsigned
+// (cell - min cell, wrapped), so a cell below the box reads as a huge value.
+__device__ __forceinline__ bool grid_in(const MapView& m, uint32_t ux, uint32_t uy) {
+    return ux < m.ext[0] && uy < m.ext[1];
+}
 
 // Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).
 __host__ __device__ __forceinline__ uint64_t pack21(int32_t gx, int32_t gy, int32_t gz) {
@@ -86,9 +97,9 @@ __host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 // cell -> (local key, home slot); false when the cell lies outside the map's bounding box
 __device__ __forceinline__ bool cell_slot(const MapView& m, int32_t gx, int32_t gy, int32_t gz,
                                           uint32_t& key, uint32_t& home) {
-    uint32_t lx = (uint32_t)(gx - m.min_cell[0]);
-    uint32_t ly = (uint32_t)(gy - m.min_cell[1]);
-    uint32_t lz = (uint32_t)(gz - m.min_cell[2]);
+    uint32_t lx = (uint32_t)gx - (uint32_t)m.min_cell[0];
+    uint32_t ly = (uint32_t)gy - (uint32_t)m.min_cell[1];
+    uint32_t lz = (uint32_t)gz - (uint32_t)m.min_cell[2];
     if ((lx >> m.bits[0]) | (ly >> m.bits[1]) | (lz >> m.bits[2])) return false;
     key = lx | (ly << m.bits[0]) | (lz << (m.bits[0] + m.bits[1]));
     home = mix32(key) & m.mask;
@@ -126,6 +137,31 @@ __device__ __forceinline__ int32_t probe_next(const MapView& m, uint32_t key, ui
         if (v.x == EMPTY_KEY) return -1;
     }
     return -1;
+}
+
+// Voxel of cell (gx, gy, gz): its slot (or -1) and centroid, through the dense index when
+// the map has one, else through the hash.
+__device__ __forceinline__ int32_t find_cell(const MapView& m, int32_t gx, int32_t gy,
+                                             int32_t gz, float* cx, float* cy, float* cz) {
+    if (m.grid) {
+        const uint32_t ux = (uint32_t)gx - (uint32_t)m.min_cell[0];
+        const uint32_t uy = (uint32_t)gy - (uint32_t)m.min_cell[1];
+        const uint32_t uz = (uint32_t)gz - (uint32_t)m.min_cell[2];
+        if (ux >= m.ext[0] || uy >= m.ext[1] || uz >= m.ext[2]) return -1;
+        const float4 e = __ldg(m.grid + ((size_t)ux * m.ext[1] + uy) * m.ext[2] + uz);
+        *cx = e.x;
+        *cy = e.y;
+        *cz = e.z;
+        return __float_as_int(e.w);
+    }
+    uint32_t key, home;
+    if (!cell_slot(m, gx, gy, gz, key, home)) return -1;
+    uint4 sv;
+    const int32_t s = probe(m, key, home, &sv);
+    *cx = __uint_as_float(sv.y);
+    *cy = __uint_as_float(sv.z);
+    *cz = __uint_as_float(sv.w);
+    return s;
 }
 
 // Cell of the unevaluated sum qh + ql (|ql| <= half an ulp of qh): floor(qh * inv_res),

@@ -32,7 +32,7 @@ int cuda_fail(cudaError_t e, const char* what);
 
 // Device-resident voxel map.
 struct Map {
-    DevBuf slots, slot_icov, slot_vidx;
+    DevBuf slots, slot_icov, slot_vidx, grid;
     DevBuf vox_coord, vox_mean, vox_cov, vox_icov, vox_count;
     MapView view{};
     ndt_map_info info{};
@@ -90,6 +90,9 @@ struct AlignOut {
 // plus next frame, and the FP64 Jacobi sweeps of an eigen solve. Fields 0-43 have the same
 // layout as the oracle's trace (whose last 4 are zero).
 constexpr int TRACE_REC = 48;
+
+// Largest dense cell index a map build makes (bytes); beyond it the kernels probe the hash.
+constexpr uint64_t DENSE_GRID_MAX_BYTES = 512ull << 20;
 
 struct AlignParams {
     MapView map;

@@ -114,14 +114,11 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
         for (int c = 0; c < 27; ++c) {
             int dx, dy, dz;
             offset27(c, dx, dy, dz);
-            int32_t cx = gx + dx, cy = gy + dy, cz = gz + dz;
-            uint32_t key, home;
-            if (!cell_slot(m, cx, cy, cz, key, home)) continue;
-            uint4 sv;
-            int32_t s = probe(m, key, home, &sv);
+            float mx, my, mz;
+            const int32_t s = find_cell(m, (int32_t)((uint32_t)gx + (uint32_t)dx),
+                                        (int32_t)((uint32_t)gy + (uint32_t)dy),
+                                        (int32_t)((uint32_t)gz + (uint32_t)dz), &mx, &my, &mz);
             if (s < 0) continue;
-            float mx = __uint_as_float(sv.y), my = __uint_as_float(sv.z),
-                  mz = __uint_as_float(sv.w);
             {
                 float e0 = (qx - mx) + ql[0], e1 = (qy - my) + ql[1], e2 = (qz - mz) + ql[2];
                 if (fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2) continue;
@@ -218,14 +215,12 @@ __global__ void k_query(MapView m, const float* __restrict__ q, size_t n, int ma
     for (int k = 0; k < 27 && c < max_nb; ++k) {
         int dx, dy, dz;
         offset27(k, dx, dy, dz);
-        int32_t cx = gx + dx, cy = gy + dy, cz = gz + dz;
-        uint32_t key, home;
-        if (!cell_slot(m, cx, cy, cz, key, home)) continue;
-        uint4 sv;
-        int32_t s = probe(m, key, home, &sv);
+        float mx, my, mz;
+        const int32_t s = find_cell(m, (int32_t)((uint32_t)gx + (uint32_t)dx),
+                                    (int32_t)((uint32_t)gy + (uint32_t)dy),
+                                    (int32_t)((uint32_t)gz + (uint32_t)dz), &mx, &my, &mz);
         if (s < 0) continue;
-        if (dist2_rn(qx, qy, qz, __uint_as_float(sv.y), __uint_as_float(sv.z),
-                     __uint_as_float(sv.w)) <= m.r2)
+        if (dist2_rn(qx, qy, qz, mx, my, mz) <= m.r2)
             idx[i * (size_t)max_nb + c++] = m.slot_vidx[s];
     }
     for (int k = c; k < max_nb; ++k) idx[i * (size_t)max_nb + k] = -1;

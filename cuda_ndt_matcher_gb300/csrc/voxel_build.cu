@@ -644,6 +644,21 @@ __global__ void k_hash_insert(const int32_t* __restrict__ coord, const float4* _
     atomicOr(status, ST_HASH_FULL);
 }
 
+// Dense cell index: every occupied hash slot writes {centroid, slot} into the entry of its
+// cell (the grid was set to all-ones first: slot -1 marks an empty cell).
+__global__ void k_grid_fill(MapView m, float4* __restrict__ grid) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > m.mask) return;
+    const uint4 v = m.slots[s];
+    if (v.x == EMPTY_KEY) return;
+    const uint32_t lx = v.x & ((1u << m.bits[0]) - 1u);
+    const uint32_t ly = (v.x >> m.bits[0]) & ((1u << m.bits[1]) - 1u);
+    const uint32_t lz = v.x >> (m.bits[0] + m.bits[1]);
+    const size_t idx = ((size_t)lx * m.ext[1] + ly) * m.ext[2] + lz;
+    grid[idx] = make_float4(__uint_as_float(v.y), __uint_as_float(v.z), __uint_as_float(v.w),
+                            __int_as_float((int32_t)s));
+}
+
 static uint32_t bit_width(uint32_t x) {
     uint32_t b = 0;
     while (b < 32 && (x >> b)) ++b;
@@ -770,6 +785,19 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
         (int32_t*)map.vox_coord.p, (float4*)map.vox_mean.p, (float*)map.vox_icov.p, V, v,
         (uint4*)map.slots.p, (float4*)map.slot_icov.p, (int32_t*)map.slot_vidx.p, mprobe,
         d_status);
+    // dense cell index over the bounding box of the map's cells, when it fits the budget
+    uint64_t cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        v.ext[a] = (uint32_t)((int64_t)hmm[3 + a] - (int64_t)hmm[a] + 1);
+        cells *= v.ext[a];
+    }
+    v.grid = nullptr;
+    if (cfg.cell_index == NDT_CELL_INDEX_AUTO && cells * 16 <= DENSE_GRID_MAX_BYTES) {
+        if ((rc = dev_reserve(map.grid, (size_t)cells * 16))) return rc;
+        cudaMemsetAsync(map.grid.p, 0xFF, (size_t)cells * 16, s);
+        k_grid_fill<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (float4*)map.grid.p);
+        v.grid = (const float4*)map.grid.p;
+    }
     cudaEventRecord(e1, s);
     uint32_t hprobe = 0;
     cudaMemcpyAsync(&hprobe, mprobe, 4, cudaMemcpyDeviceToHost, s);
@@ -793,6 +821,7 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
         info.max_coord[a] = hmm[3 + a];
     }
     info.build_ms = ms;
+    info.dense_grid_mib = v.grid ? (float)((double)cells * 16.0 / (1024.0 * 1024.0)) : 0.f;
     map.valid = true;
     return 0;
 }

@@ -46,6 +46,13 @@ extern "C" {
 #define NDT_SEMANTICS_GPU_GRAPH 0   /* align_gpu: graph kernels K1-K5 */
 #define NDT_SEMANTICS_CPU 1         /* align with use_gpu = false: NdtOptimizer::align */
 
+/* Cell lookup of the search kernels. Both give the same voxel for a cell (one voxel per
+ * cell); they differ in cost. The hash table (the reference's structure, voxel_hash.cu) is
+ * always built. The dense index is an array over the map's cell bounding box, 16 bytes per
+ * cell {centroid, slot}, built when it takes at most 512 MiB: a lookup is one load. */
+#define NDT_CELL_INDEX_AUTO 0       /* dense index when it fits, else the hash */
+#define NDT_CELL_INDEX_HASH 1       /* hash probing only */
+
 #define NDT_STATUS_CONVERGED 0
 #define NDT_STATUS_MAX_ITERATIONS 1
 #define NDT_STATUS_NO_CORRESPONDENCES 2
@@ -68,7 +75,8 @@ typedef struct ndt_config {
     int32_t threads_per_cta;       /* 0 = autotuned */
     int32_t hash_capacity_factor;  /* capacity = next pow2 >= factor * V; 2 = reference */
     int32_t max_registers;         /* Newton-kernel register cap (80 or 128); 0 = autotuned */
-    int32_t reserved[2];
+    int32_t cell_index;            /* NDT_CELL_INDEX_*: how kernels find a cell's voxel */
+    int32_t reserved;
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
@@ -103,7 +111,7 @@ typedef struct ndt_map_info {
     int32_t min_coord[3];
     int32_t max_coord[3];
     float build_ms;                /* device time of the last set_target build */
-    float reserved;
+    float dense_grid_mib;          /* size of the dense cell index, 0 when the hash serves */
 } ndt_map_info;
 
 /* Counters accumulated by a context since creation or the last ndt_stats_reset. */

@@ -35,11 +35,11 @@ def assert_parity(got, want, what=""):
 
 
 @pytest.mark.parametrize("semantics", [0, 1])
-@pytest.mark.parametrize("cluster", [1, 4])
-def test_single_alignment_parity(gpu, oracle, single_cases, semantics, cluster):
+@pytest.mark.parametrize("cluster,cell_index", [(1, 0), (4, 0), (4, 1)])
+def test_single_alignment_parity(gpu, oracle, single_cases, semantics, cluster, cell_index):
     sem_name = "gpu" if semantics == 0 else "cpu"
     for i, case in enumerate(single_cases):
-        ctx = capi.Context(semantics=semantics, cluster_size=cluster)
+        ctx = capi.Context(semantics=semantics, cluster_size=cluster, cell_index=cell_index)
         ctx.set_target(case.map_points)
         got = ctx.align(case.scan, case.guess)
         g = oracle.Grid(case.map_points, 2.0)
@@ -154,9 +154,10 @@ def test_multi_pose_wide_basin(gpu, oracle, single_cases):
         shadow_check(ctx, g, case.scan, p)
 
 
-def test_eval_batch_matches_oracle(gpu, oracle, single_cases):
+@pytest.mark.parametrize("cell_index", [0, 1])
+def test_eval_batch_matches_oracle(gpu, oracle, single_cases, cell_index):
     case = single_cases[2]
-    ctx = capi.Context()
+    ctx = capi.Context(cell_index=cell_index)
     ctx.set_target(case.map_points)
     g = oracle.Grid(case.map_points, 2.0)
     Ts = []

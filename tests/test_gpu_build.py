@@ -169,10 +169,12 @@ def test_map_build_matches_oracle(gpu, oracle, name):
     assert info.num_voxels == g.n and info.hash_capacity == g.capacity
 
 
-def test_neighbors_bitexact(gpu, oracle):
+@pytest.mark.parametrize("cell_index", [0, 1])   # dense cell index / hash probing
+def test_neighbors_bitexact(gpu, oracle, cell_index):
     case = synth.single_case(2)
-    ctx = capi.Context()
+    ctx = capi.Context(cell_index=cell_index)
     ctx.set_target(case.map_points)
+    assert (ctx.map_info().dense_grid_mib > 0) == (cell_index == 0)
     g = oracle.Grid(case.map_points, 2.0)
     rng = np.random.default_rng(0)
     q = np.concatenate([g.means + rng.normal(0, 0.8, g.means.shape).astype(np.float32),
