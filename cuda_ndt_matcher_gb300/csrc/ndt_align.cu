@@ -41,9 +41,11 @@ constexpr int A_SC = 0, A_G = 1, A_GP = 4, A_M = 13, A_HTR = 19, A_HRR = 28;
 
 struct SolveScratch {
     double A[36], V[36], T[36], cs[6], x[6];
+    double W[36];  // eigenvectors of the alignment's last eigen solve (warm start)
     float A32[36], V32[36], cs32[6];
     int ok, path;  // path: 0 Cholesky, 1 eigen
     int sweeps;    // FP64 Jacobi sweeps of the eigen path
+    int have_w;    // W is set
 };
 
 struct AlignShared {
@@ -165,6 +167,19 @@ __constant__ int8_t RR_PAIRS[5][3][2] = {
 __device__ __forceinline__ float rsq(float v) { return rsqrtf(v); }
 __device__ __forceinline__ double rsq(double v) { return rsqrt(v); }
 
+// Role of index i in round r of the round-robin schedule: partner index (bits 0-2), slot of
+// the round's rotation (bits 3-4), and bit 5 set when i is the q of its pair (p < q).
+__device__ __forceinline__ int rr_role(int r, int i) {
+    int role = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int p = RR_PAIRS[r][k][0], q = RR_PAIRS[r][k][1];
+        if (i == p) role = q | (k << 3);
+        if (i == q) role = p | (k << 3) | 32;
+    }
+    return role;
+}
+
 // Warp-parallel Jacobi eigen-decomposition of the symmetric 6x6 in `A` (shared memory, type
 // T): A becomes diagonal and V accumulates the rotations, V <- V J, from the identity or,
 // when init_v is false, from the orthogonal V the caller left there. Rotation angles and
@@ -174,7 +189,9 @@ __device__ __forceinline__ double rsq(double v) { return rsqrt(v); }
 // by rounding. The tangent t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)) with
 // theta = (a_qq - a_pp) / (2 a_pq) is evaluated as
 // sgn(theta) |2 a_pq| / (|a_qq - a_pp| + sqrt((a_qq - a_pp)^2 + (2 a_pq)^2)) (one division),
-// and c = 1 / sqrt(t^2 + 1) as a reciprocal square root. Returns the sweeps that rotated.
+// and c = 1 / sqrt(t^2 + 1) as a reciprocal square root. Lanes 0-20 own one upper-triangle
+// entry of A, every lane one entry of V (lanes 0-3 a second); each lane's partners in the
+// five rounds are resolved once, before the sweeps. Returns the sweeps that rotated.
 template <typename T>
 __device__ __noinline__ int jacobi6_warp(T* A, T* V, T* cs, int lane, bool init_v, T skip,
                                          T stop, int max_sweeps) {
@@ -182,16 +199,37 @@ __device__ __noinline__ int jacobi6_warp(T* A, T* V, T* cs, int lane, bool init_
         if (lane < 36 - 32) V[32 + lane] = ((32 + lane) % 7 == 0) ? T(1) : T(0);
         V[lane] = (lane % 7 == 0) ? T(1) : T(0);
     }
+    int ai = 0, aj = 0;  // upper-triangle entry (ai <= aj) of lanes < 21
+    if (lane < 21) {
+        int t = lane;
+        while (t >= 6 - ai) {
+            t -= 6 - ai;
+            ++ai;
+        }
+        aj = ai + t;
+    }
+    const int vi = lane / 6, vj = lane % 6, wi = (32 + lane) / 6, wj = (32 + lane) % 6;
+    int ra[5], rb[5], rv[5], rw[5], rp[5], rq[5];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+        ra[r] = rr_role(r, ai);
+        rb[r] = rr_role(r, aj);
+        rv[r] = rr_role(r, vj);
+        rw[r] = rr_role(r, wj);
+        const int l3 = lane < 3 ? lane : 0;
+        rp[r] = RR_PAIRS[r][l3][0];
+        rq[r] = RR_PAIRS[r][l3][1];
+    }
+    int op = 0, oq = 0;  // off-diagonal pair of lanes < 15 for the convergence test
+    if (lane < 15) {
+        op = RR_PAIRS[lane / 3][lane % 3][0];
+        oq = RR_PAIRS[lane / 3][lane % 3][1];
+    }
     __syncwarp();
     int sweeps = 0;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-        // convergence test (lane i < 6 owns diagonal i; lanes < 15 own one off-diagonal pair)
         T dg = lane < 6 ? A[lane * 7] * A[lane * 7] : T(0);
-        T off = T(0);
-        if (lane < 15) {
-            int p = RR_PAIRS[lane / 3][lane % 3][0], q = RR_PAIRS[lane / 3][lane % 3][1];
-            off = A[p * 6 + q] * A[p * 6 + q];
-        }
+        T off = lane < 15 ? A[op * 6 + oq] * A[op * 6 + oq] : T(0);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             dg += __shfl_xor_sync(0xffffffffu, dg, o);
@@ -199,10 +237,11 @@ __device__ __noinline__ int jacobi6_warp(T* A, T* V, T* cs, int lane, bool init_
         }
         if (T(2) * off < stop * dg) break;
         sweeps++;
+#pragma unroll
         for (int r = 0; r < 5; ++r) {
             if (lane < 3) {
-                int p = RR_PAIRS[r][lane][0], q = RR_PAIRS[r][lane][1];
-                T apq = A[p * 6 + q];
+                const int p = rp[r], q = rq[r];
+                const T apq = A[p * 6 + q];
                 T c = T(1), sn = T(0);
                 if (fabs(apq) >= skip) {
                     const T d = A[q * 6 + q] - A[p * 6 + p], a = T(2) * apq;
@@ -215,64 +254,35 @@ __device__ __noinline__ int jacobi6_warp(T* A, T* V, T* cs, int lane, bool init_
                 cs[2 * lane + 1] = sn;
             }
             __syncwarp();
-            // rotation of index i: partner j and coefficients (own, partner) of row i of J^T
-            // (p: c, -s; q: s, c)
-            T nA0 = T(0), nV0 = T(0), nV1 = T(0);
-            int ai = 0, aj = 0;
-            if (lane < 21) {  // upper-triangle entry (ai <= aj)
-                int t = lane;
-                ai = 0;
-                while (t >= 6 - ai) {
-                    t -= 6 - ai;
-                    ++ai;
-                }
-                aj = ai + t;
-            }
-            auto coef = [&](int i, int& partner, T& cown, T& cpart) {
-                for (int k = 0; k < 3; ++k) {
-                    int p = RR_PAIRS[r][k][0], q = RR_PAIRS[r][k][1];
-                    if (i == p) {
-                        partner = q;
-                        cown = cs[2 * k];
-                        cpart = -cs[2 * k + 1];
-                    } else if (i == q) {
-                        partner = p;
-                        cown = cs[2 * k];
-                        cpart = cs[2 * k + 1];
-                    }
-                }
+            // row i of J^T: own coefficient c, partner coefficient -s (i = p) or s (i = q)
+            auto own = [&](int role) { return cs[2 * ((role >> 3) & 3)]; };
+            auto part = [&](int role) {
+                const T s = cs[2 * ((role >> 3) & 3) + 1];
+                return (role & 32) ? s : -s;
             };
+            T nA = T(0), nV0, nV1 = T(0);
             if (lane < 21) {
-                int pi, pj;
-                T ci, si, cj, sj;
-                coef(ai, pi, ci, si);
-                coef(aj, pj, cj, sj);
-                if (pi == aj) {  // rotated pair itself: zeroed by construction
-                    nA0 = T(0);
-                } else {
-                    T a_ij = A[ai * 6 + aj], a_ipj = A[pi * 6 + aj];
-                    T a_ijp = A[ai * 6 + pj], a_ipjp = A[pi * 6 + pj];
-                    nA0 = ci * (cj * a_ij + sj * a_ijp) + si * (cj * a_ipj + sj * a_ipjp);
+                const int pi = ra[r] & 7, pj = rb[r] & 7;
+                if (pi != aj) {  // the rotated pair itself becomes zero
+                    const T ci = own(ra[r]), si = part(ra[r]);
+                    const T cj = own(rb[r]), sj = part(rb[r]);
+                    const T a_ij = A[ai * 6 + aj], a_ipj = A[pi * 6 + aj];
+                    const T a_ijp = A[ai * 6 + pj], a_ipjp = A[pi * 6 + pj];
+                    nA = ci * (cj * a_ij + sj * a_ijp) + si * (cj * a_ipj + sj * a_ipjp);
                 }
             }
-            // V' = V J: column j mixes with its partner
-            {
-                int vi = lane / 6, vj = lane % 6, pj;
-                T cj, sj;
-                coef(vj, pj, cj, sj);
-                nV0 = cj * V[vi * 6 + vj] + sj * V[vi * 6 + pj];
+            {  // V' = V J: column j mixes with its partner
+                const int pj = rv[r] & 7;
+                nV0 = own(rv[r]) * V[vi * 6 + vj] + part(rv[r]) * V[vi * 6 + pj];
                 if (lane < 4) {
-                    int e = 32 + lane;
-                    int wi = e / 6, wj = e % 6, pw;
-                    T cw, sw;
-                    coef(wj, pw, cw, sw);
-                    nV1 = cw * V[wi * 6 + wj] + sw * V[wi * 6 + pw];
+                    const int pw = rw[r] & 7;
+                    nV1 = own(rw[r]) * V[wi * 6 + wj] + part(rw[r]) * V[wi * 6 + pw];
                 }
             }
             __syncwarp();
             if (lane < 21) {
-                A[ai * 6 + aj] = nA0;
-                A[aj * 6 + ai] = nA0;
+                A[ai * 6 + aj] = nA;
+                A[aj * 6 + ai] = nA;
             }
             V[lane] = nV0;
             if (lane < 4) V[32 + lane] = nV1;
@@ -334,6 +344,23 @@ __device__ __forceinline__ void chol6f_solve(const Chol32& C, const float* b, fl
         for (int k = i + 1; k < 6; ++k) s = fmaf(-C.L[tri(k, i)], x[k], s);
         x[i] = s * C.rinv[i];
     }
+}
+
+// Z = op(X) Y for 6x6 FP64 matrices in shared memory (op(X) = X, or X^T when xt); each lane
+// owns entries of Z, each a 6-term dot product split in two chains of three FMAs.
+__device__ __forceinline__ void mm6(const double* X, bool xt, const double* Y, double* Z,
+                                    int lane) {
+    for (int e = lane; e < 36; e += 32) {
+        const int i = e / 6, j = e % 6;
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; k += 2) {
+            s0 = fma(xt ? X[k * 6 + i] : X[i * 6 + k], Y[k * 6 + j], s0);
+            s1 = fma(xt ? X[(k + 1) * 6 + i] : X[i * 6 + k + 1], Y[(k + 1) * 6 + j], s1);
+        }
+        Z[e] = s0 + s1;
+    }
+    __syncwarp();
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -420,49 +447,45 @@ __device__ __noinline__ void solve_warp(const double* H, const double* g, SolveS
         }
     }
     __syncwarp();
-    // f32 Jacobi
-    S.A32[lane] = (float)H[lane];
-    if (lane < 4) S.A32[32 + lane] = (float)H[32 + lane];
+    // eigen path. f32 Jacobi on W^T H W, where W holds the eigenvectors of this alignment's
+    // previous eigen solve (H changes little between iterations, so few sweeps remain) or
+    // the identity; then V = W V32 made orthogonal to FP64 rounding (two Newton-Schulz steps
+    // V <- V (3I - V^T V) / 2) and FP64 Jacobi sweeps on V^T H V under the reference's FP64
+    // stopping rule.
+    const bool warm = S.have_w != 0;
+    if (warm) {
+        mm6(H, false, S.W, S.T, lane);    // T = H W
+        mm6(S.W, true, S.T, S.A, lane);   // A = W^T H W
+        S.A32[lane] = (float)S.A[lane];
+        if (lane < 4) S.A32[32 + lane] = (float)S.A[32 + lane];
+    } else {
+        S.A32[lane] = (float)H[lane];
+        if (lane < 4) S.A32[32 + lane] = (float)H[32 + lane];
+    }
     __syncwarp();
     jacobi6_warp<float>(S.A32, S.V32, S.cs32, lane, true, 1e-30f, 1e-12f, 20);
-    S.V[lane] = (double)S.V32[lane];
-    if (lane < 4) S.V[32 + lane] = (double)S.V32[32 + lane];
-    __syncwarp();
-    // Newton-Schulz: T = 3I - V^T V; V <- V T / 2 (via A as scratch)
+    if (warm) {
+        S.T[lane] = (double)S.V32[lane];
+        if (lane < 4) S.T[32 + lane] = (double)S.V32[32 + lane];
+        __syncwarp();
+        mm6(S.W, false, S.T, S.V, lane);  // V = W V32
+    } else {
+        S.V[lane] = (double)S.V32[lane];
+        if (lane < 4) S.V[32 + lane] = (double)S.V32[32 + lane];
+        __syncwarp();
+    }
     for (int ns = 0; ns < 2; ++ns) {
-        for (int e = lane; e < 36; e += 32) {
-            const int i = e / 6, j = e % 6;
-            double s = 0.0;
-            for (int k = 0; k < 6; ++k) s = fma(S.V[k * 6 + i], S.V[k * 6 + j], s);
-            S.T[e] = (i == j ? 3.0 : 0.0) - s;
-        }
+        mm6(S.V, true, S.V, S.T, lane);   // T = V^T V
+        S.T[lane] = ((lane % 7) == 0 ? 3.0 : 0.0) - S.T[lane];
+        if (lane < 4) S.T[32 + lane] = ((32 + lane) % 7 == 0 ? 3.0 : 0.0) - S.T[32 + lane];
         __syncwarp();
-        for (int e = lane; e < 36; e += 32) {
-            const int i = e / 6, j = e % 6;
-            double s = 0.0;
-            for (int k = 0; k < 6; ++k) s = fma(S.V[i * 6 + k], S.T[k * 6 + j], s);
-            S.A[e] = 0.5 * s;
-        }
-        __syncwarp();
-        S.V[lane] = S.A[lane];
-        if (lane < 4) S.V[32 + lane] = S.A[32 + lane];
+        mm6(S.V, false, S.T, S.A, lane);  // A = V (3I - V^T V)
+        S.V[lane] = 0.5 * S.A[lane];
+        if (lane < 4) S.V[32 + lane] = 0.5 * S.A[32 + lane];
         __syncwarp();
     }
-    // A = V^T H V (T = H V), symmetrised
-    for (int e = lane; e < 36; e += 32) {
-        const int i = e / 6, j = e % 6;
-        double s = 0.0;
-        for (int k = 0; k < 6; ++k) s = fma(H[i * 6 + k], S.V[k * 6 + j], s);
-        S.T[e] = s;
-    }
-    __syncwarp();
-    for (int e = lane; e < 36; e += 32) {
-        const int i = e / 6, j = e % 6;
-        double s = 0.0;
-        for (int k = 0; k < 6; ++k) s = fma(S.V[k * 6 + i], S.T[k * 6 + j], s);
-        S.A[e] = s;
-    }
-    __syncwarp();
+    mm6(H, false, S.V, S.T, lane);        // T = H V
+    mm6(S.V, true, S.T, S.A, lane);       // A = V^T H V
     {
         double v = 0.0;
         int ai = 0, aj = 0;
@@ -483,6 +506,9 @@ __device__ __noinline__ void solve_warp(const double* H, const double* g, SolveS
         __syncwarp();
     }
     const int sw = jacobi6_warp<double>(S.A, S.V, S.cs, lane, false, 1e-15, 1e-28, 30);
+    S.W[lane] = S.V[lane];
+    if (lane < 4) S.W[32 + lane] = S.V[32 + lane];
+    if (lane == 0) S.have_w = 1;
     // pseudo-inverse step from the eigenpairs, lane i < 6 owning eigenpair i
     double lam = lane < 6 ? S.A[lane * 7] : 0.0;
     double thr;
@@ -766,11 +792,14 @@ __device__ __forceinline__ void osc_update(AlignShared& sh, const double* pose, 
             cv[a] = pose[a] - sh.prev[a];
             pv[a] = sh.prev[a] - sh.prev2[a];
         }
-        double cn = sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
-        double pn = sqrt(pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]);
-        if (cn > 1e-10 && pn > 1e-10) {
-            double cosv = (cv[0] * pv[0] + cv[1] * pv[1] + cv[2] * pv[2]) / (cn * pn);
-            sh.osc = cosv < -0.9 ? sh.osc + 1 : 0;
+        // |c| > 1e-10, |p| > 1e-10 and cos(c, p) < -0.9, compared on squares (no square roots
+        // or division on the controller's FP64 path)
+        const double cn2 = cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2];
+        const double pn2 = pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2];
+        if (cn2 > 1e-20 && pn2 > 1e-20) {
+            const double dot = cv[0] * pv[0] + cv[1] * pv[1] + cv[2] * pv[2];
+            const bool rev = dot < 0.0 && dot * dot > 0.81 * (cn2 * pn2);
+            sh.osc = rev ? sh.osc + 1 : 0;
             if (sh.osc > sh.max_osc) sh.max_osc = sh.osc;
         } else {
             sh.osc = 0;
@@ -780,6 +809,14 @@ __device__ __forceinline__ void osc_update(AlignShared& sh, const double* pose, 
         sh.prev2[a] = sh.prev[a];
         sh.prev[a] = pose[a];
     }
+}
+
+// 6-term FP64 dot product summed as a tree (dependency depth 4 instead of 6)
+__device__ __forceinline__ double dot6(const double* a, const double* b) {
+    const double p0 = fma(a[1], b[1], a[0] * b[0]);
+    const double p1 = fma(a[3], b[3], a[2] * b[2]);
+    const double p2 = fma(a[5], b[5], a[4] * b[4]);
+    return (p0 + p1) + p2;
 }
 
 __device__ void write_out(AlignOut& o, const double* pose, double score, const double* H,
@@ -806,13 +843,10 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
         for (int i = 0; i < 6; ++i) x[i] = sh.solve.x[i];
         if (!sh.solve.ok)
             for (int i = 0; i < 6; ++i) x[i] = -g[i] * 1e-4;
-        double dphi = 0.0;
-        for (int i = 0; i < 6; ++i) dphi += g[i] * x[i];
+        const double dphi = dot6(g, x);
         if (dphi <= 0.0)
             for (int i = 0; i < 6; ++i) x[i] = -x[i];
-        double dn = 0.0;
-        for (int i = 0; i < 6; ++i) dn += x[i] * x[i];
-        dn = sqrt(dn);
+        const double dn = sqrt(dot6(x, x));
         double step = dn > P.step_size ? P.step_size : dn;
         double scale = dn > 1e-10 ? step / dn : 0.0;
         for (int i = 0; i < 6; ++i) pose[i] += scale * x[i];
@@ -849,9 +883,7 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
                   NDT_STATUS_SINGULAR_HESSIAN);
         return 1;
     }
-    double dn = 0.0;
-    for (int i = 0; i < 6; ++i) dn += x[i] * x[i];
-    dn = sqrt(dn);
+    const double dn = sqrt(dot6(x, x));
     if (dn < P.eps) {
         write_out(o, pose, score, H, it + 1, 1, ncorr, sh.max_osc, NDT_STATUS_CONVERGED);
         return 1;
@@ -958,6 +990,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         sh.osc = sh.max_osc = 0;
         for (int i = 0; i < 36; ++i) sh.last_H[i] = 0.0;
         sh.done = 0;
+        sh.solve.have_w = 0;
     }
     __syncthreads();
     if (warp == 0) make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
@@ -996,12 +1029,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         unsigned long long t2 = clock64();
         if (rank == 0) {
             for (int k = tid; k < NRED; k += THREADS) {
-                double s = 0.0;
-                for (int r = 0; r < K; ++r) {
-                    const double* rp = cluster.map_shared_rank(sh.part, r);
-                    s += rp[k];
-                }
-                sh.tot[k] = s;
+                // all remote loads first, then a fixed-order tree (deterministic)
+                double v[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r)
+                    v[r] = r < K ? cluster.map_shared_rank(sh.part, r)[k] : 0.0;
+                sh.tot[k] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
             }
             __syncthreads();
             if (warp == 0) {
