@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 METRIC = "scan aligns/s (20k pts, 5M-pt map); init-pose est/s, learned vs plain"
 FLOP_PER_POINT_ITER = 165
 FLOP_PER_PAIR = 65
+# DRAM bytes (read + write) of one k_ndt_align launch of the default workload (256 scans,
+# 5M-point map, seed 2), from one ncu capture of this bench (profiles/k_ndt_align_seq5M_b256.md)
+NCU_ALIGN_TRAFFIC = {(256, 5_000_000, 2): 73.3e6}
 
 
 def parse():
@@ -330,7 +333,8 @@ def run_ours(args):
             "roofline": {"bound": "fp32", "kernel": "k_ndt_align", "achieved": achieved,
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None,
-                         "traffic": None,
+                         "traffic": NCU_ALIGN_TRAFFIC.get((B, args.map_points, args.seed)),
+                         "traffic_unit": "bytes per launch (ncu dram read + write)",
                          "peak_source": f"derived: SMs x 128 FP32 lanes x 2 x sm_max_mhz "
                                         f"({src} MEASURED_PEAKS.json clock)",
                          "flops_per_launch": flops / max(launches, 1),
