@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--map-points", type=int, default=5_000_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--extras", type=int, default=1,
+                    help="also run the initial-pose search and the uneven-queue workloads")
     ap.add_argument("--shape", default="",
                     help="fixed Newton-kernel launch shape CLUSTER,THREADS,REGISTERS "
                          "(e.g. 8,256,80) instead of the autotuner")
@@ -156,6 +158,79 @@ def cpu_baseline(grid_args, scans, poses, seconds, semantics="cpu"):
     return {"value": done / dt, "unit": "aligns/s", "cores": cores, "kind": "port",
             "sample": f"{done} of the bench's 20k-point scans, NdtOptimizer::align restated "
                       f"(FP64, all neighbours, ND-clamp + SVD step), {cores} threads, {dt:.1f} s"}
+
+
+def init_pose_bench(repeats, cpu_seconds):
+    """Initial-pose search: 16 queries x 200 particles (x, y +-2 m, yaw over the circle),
+    30 iterations, NVTL-ranked, on the 200k-point single-workload map. Wall time of the
+    public entry point with host scans (copies, one alignment launch for all 3200
+    particles, NVTL scoring, selection), replayed as a CUDA graph."""
+    from cuda_ndt_matcher_gb300 import capi, synth
+    w = synth.search_queries(seed=21, n_queries=16)
+    ctx = capi.Context(cuda_graph=1)
+    ctx.set_target(w.map_points)
+    kw = dict(num_particles=200, xy_range=2.0, yaw_range=np.pi, seed=5)
+    est = ctx.initial_pose_search(w.scans, w.priors, **kw)  # warm-up + graph capture
+    ctx.stats_reset()
+    t0 = time.perf_counter()
+    for r in range(repeats):
+        est = ctx.initial_pose_search(w.scans, w.priors, **dict(kw, seed=5 + r))
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    ok = 0
+    for e, t in zip(est, w.true_poses):
+        dyaw = (e["pose"][5] - t[5] + np.pi) % (2 * np.pi) - np.pi
+        ok += int(np.linalg.norm(e["pose"][:2] - t[:2]) < 0.2 and abs(dyaw) < np.radians(1.0))
+    out = {"metric": "init-pose est/s (plain 200-particle search)",
+           "value": 16 * repeats / wall, "unit": "estimates/s", "queries": 16,
+           "particles": 200, "ms_per_search_of_16": wall / repeats * 1e3,
+           "gpu_ms_per_search_of_16": (st["align_kernel_ms"] + st["score_kernel_ms"]) / repeats,
+           "success_rate": ok / len(est), "success": "error < 0.2 m and < 1 deg",
+           "scan_points_mean": float(np.mean([len(s) for s in w.scans])), "cuda_graph": True}
+    ctx.close()
+    if cpu_seconds > 0:  # the restated CPU path on the host cores: one query's 200 particles
+        from oracle import oracle as O
+        g = O.Grid(w.map_points, 2.0)
+        cores = os.cpu_count() or 1
+        starts = [O.particle(w.priors[0], 0, k, 2.0, np.pi, seed=5) for k in range(200)]
+        t0 = time.perf_counter()
+        res = g.align_batch([w.scans[0]] * 200, starts, semantics="cpu", nthreads=cores)
+        for r in res:
+            T = O.pose_T34_zyx(r["pose"])
+            g.nvtl(w.scans[0], T)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "estimates/s", "cores": cores,
+                               "kind": "port", "sample": f"1 query x 200 particles, "
+                               f"NdtOptimizer::align restated + NVTL, {cores} threads, "
+                               f"{dt:.1f} s"}
+    return out
+
+
+def queue_bench(repeats):
+    """A queue of 64 scans of log-uniform size 2k-40k points in one launch (CUDA graph):
+    throughput and per-scan completion latency (device clock, from the batch's first start)."""
+    from cuda_ndt_matcher_gb300 import capi, synth
+    w = synth.queue_scans(seed=22, n_scans=64)
+    ctx = capi.Context(cuda_graph=1)
+    ctx.set_target(w.map_points)
+    ctx.align_batch(w.scans, w.priors)
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        ctx.align_batch(w.scans, w.priors)
+        _, fin = ctx.batch_timings(len(w.scans))
+        lat.append(fin)
+    wall = time.perf_counter() - t0
+    lat = np.concatenate(lat)
+    out = {"metric": "queue aligns/s (64 scans, 2k-40k points, one launch)",
+           "value": 64 * repeats / wall, "unit": "aligns/s",
+           "latency_ms_p50": float(np.percentile(lat, 50)),
+           "latency_ms_p99": float(np.percentile(lat, 99)),
+           "latency": "scan completion on the device clock from the batch's first start",
+           "points": [int(min(len(s) for s in w.scans)), int(max(len(s) for s in w.scans))],
+           "cuda_graph": True}
+    ctx.close()
+    return out
 
 
 def run_reference(args):
@@ -309,6 +384,10 @@ def run_ours(args):
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline((seq.map, 2.0), scans, poses, args.cpu_seconds)
+    extra = {}
+    if rank == 0 and args.extras:
+        extra["init_pose"] = init_pose_bench(5, args.cpu_seconds)
+        extra["queue"] = queue_bench(10)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "aligns/s", "n_gpus": world,
@@ -356,6 +435,7 @@ def run_ours(args):
             "accuracy": {"median_xy_err_m": float(np.median(perr)),
                          "p99_xy_err_m": float(np.percentile(perr, 99))},
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

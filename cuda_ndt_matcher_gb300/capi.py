@@ -26,7 +26,8 @@ EXPORTS = [
     "ndt_ctx_stream",
     "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
-    "ndt_autotune", "ndt_eval_batch", "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
+    "ndt_autotune", "ndt_eval_batch", "ndt_batch_timings", "ndt_initial_pose_search",
+    "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
     "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
     "ndt_radix_sort_pairs_u64_u32", "ndt_radix_sort_pairs_u64_u32_static",
     "ndt_detect_segments", "ndt_morton_codes",
@@ -48,7 +49,7 @@ class Config(C.Structure):
                 ("device", C.c_int32), ("cluster_size", C.c_int32),
                 ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
                 ("max_registers", C.c_int32), ("cell_index", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("cuda_graph", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -69,6 +70,20 @@ class TuneResult(C.Structure):
     _fields_ = [("cluster_size", C.c_int32), ("threads_per_cta", C.c_int32),
                 ("kernel_ms", C.c_double), ("aligns_per_s", C.c_double),
                 ("candidates", C.c_int32), ("registers", C.c_int32)]
+
+
+class ParticleConfig(C.Structure):
+    _fields_ = [("num_particles", C.c_uint32), ("reserved", C.c_uint32),
+                ("xy_range", C.c_double), ("yaw_range", C.c_double),
+                ("z_sigma", C.c_double), ("roll_pitch_sigma", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class PoseEstimate(C.Structure):
+    _fields_ = [("pose", C.c_double * 6), ("initial_pose", C.c_double * 6),
+                ("nvtl", C.c_double), ("score", C.c_double), ("selection_score", C.c_double),
+                ("particle", C.c_int32), ("iterations", C.c_int32), ("converged", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class MapInfo(C.Structure):
@@ -129,6 +144,9 @@ def load(build_if_missing=True):
         "ndt_align_batch_device": (C.c_int, [P, P, P, P, C.c_uint64, P]),
         "ndt_autotune": (C.c_int, [P, P, P, P, C.c_uint64, C.c_int32, C.POINTER(TuneResult)]),
         "ndt_eval_batch": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P, P]),
+        "ndt_batch_timings": (C.c_int, [P, P, P, C.c_uint64]),
+        "ndt_initial_pose_search": (C.c_int, [P, P, C.c_uint64, C.POINTER(ParticleConfig),
+                                              P, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
         "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
         "ndt_stats_reset": (C.c_int, [P]),
@@ -295,6 +313,40 @@ class Context:
         return {"cluster_size": r.cluster_size, "threads_per_cta": r.threads_per_cta,
                 "kernel_ms": r.kernel_ms, "aligns_per_s": r.aligns_per_s,
                 "candidates": r.candidates, "registers": r.registers}
+
+    def batch_timings(self, n):
+        """Start / finish (ms, device clock) of each alignment of the last call."""
+        start = np.zeros(n)
+        finish = np.zeros(n)
+        check(self.lib.ndt_batch_timings(self.h, start.ctypes.data, finish.ctypes.data, n))
+        return start, finish
+
+    def initial_pose_search(self, queries, priors, num_particles=200, xy_range=2.0,
+                            yaw_range=np.pi, z_sigma=0.0, roll_pitch_sigma=0.0, seed=0,
+                            return_particles=False):
+        """Batched multi-particle search; returns one estimate dict per query (and, when
+        asked, every particle's result, query-major)."""
+        qs = [as_xyz(q) for q in queries]
+        m = len(qs)
+        arr = (Scan * m)()
+        for i, (s, pose) in enumerate(zip(qs, priors)):
+            arr[i].xyz = s.ctypes.data
+            arr[i].num_points = len(s)
+            for k in range(6):
+                arr[i].initial_pose[k] = float(pose[k])
+        pc = ParticleConfig(num_particles=num_particles, xy_range=xy_range,
+                            yaw_range=yaw_range, z_sigma=z_sigma,
+                            roll_pitch_sigma=roll_pitch_sigma, seed=seed)
+        est = (PoseEstimate * m)()
+        parts = (Result * (m * num_particles))() if return_particles else None
+        check(self.lib.ndt_initial_pose_search(self.h, arr, m, C.byref(pc), est, parts))
+        out = [{"pose": np.array(e.pose), "initial_pose": np.array(e.initial_pose),
+                "nvtl": e.nvtl, "score": e.score, "selection_score": e.selection_score,
+                "particle": e.particle, "iterations": e.iterations,
+                "converged": bool(e.converged)} for e in est]
+        if return_particles:
+            return out, [result_dict(r) for r in parts]
+        return out
 
     def eval_batch(self, points, T34):
         p = as_xyz(points)

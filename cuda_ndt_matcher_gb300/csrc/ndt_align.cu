@@ -906,6 +906,13 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
     return 0;
 }
 
+// GPU global timer (ns): per-alignment start / finish times for latency percentiles
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // TwoSum: s + e == a + b exactly
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
@@ -997,6 +1004,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     __syncthreads();
 
     uint64_t point_iters = 0, corr_total = 0;
+    const uint64_t t_start = global_ns();
     if (tid == 0) {
         sh.cyc[0] = sh.cyc[1] = sh.cyc[2] = sh.cyc[3] = 0ull;
         sh.n_eigen = 0;
@@ -1106,6 +1114,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         AlignOut& o = P.out[jid];
         for (int i = 0; i < 4; ++i) o.cycles[i] = sh.cyc[i];
         o.n_eigen = sh.n_eigen;
+        o.t_start = t_start;
+        o.t_end = global_ns();
     }
 }
 

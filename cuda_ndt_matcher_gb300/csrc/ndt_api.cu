@@ -104,7 +104,22 @@ struct ndt_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     LaunchShape forced{0, 0, 0};                           // set only while autotuning
     std::map<std::pair<int, int>, LaunchShape> tuned;      // (log2 jobs, log2 max points)
+    // captured batches, most recently used last; a key holds everything the captured
+    // launches bake in (sizes, launch shape, buffer addresses, map and parameter versions)
+    struct GraphEntry {
+        std::vector<uint64_t> key;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::vector<GraphEntry> graphs;
+    uint64_t map_gen = 0, cfg_gen = 0;
+    std::vector<double> t_start_ms, t_finish_ms;           // last call, by result index
 };
+
+static void drop_graphs(ndt_ctx* c) {
+    for (auto& g : c->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
 
 static int check_status(ndt_ctx* c, uint32_t st) {
     if (st == 0) return 0;
@@ -159,7 +174,8 @@ static bool config_ok(const ndt_config& c) {
            (c.semantics == NDT_SEMANTICS_GPU_GRAPH || c.semantics == NDT_SEMANTICS_CPU) &&
            (K == 0 || K == 1 || K == 2 || K == 4 || K == 8) &&
            (T == 0 || T == 128 || T == 256 || T == 512) && (R == 0 || R == 80 || R == 128) &&
-           (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH);
+           (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
+           (c.cuda_graph == 0 || c.cuda_graph == 1);
 }
 
 extern "C" {
@@ -218,7 +234,9 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     if (!c) return NDT_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (DevBuf* b : {&c->map.slots, &c->map.slot_icov, &c->map.slot_vidx, &c->map.vox_coord,
+    drop_graphs(c);
+    for (DevBuf* b : {&c->map.slots, &c->map.slot_icov, &c->map.slot_vidx, &c->map.grid,
+                      &c->map.vox_coord,
                       &c->map.vox_mean, &c->map.vox_cov, &c->map.vox_icov, &c->map.vox_count,
                       &c->bs.keys_a, &c->bs.keys_b, &c->bs.vals_a, &c->bs.vals_b, &c->bs.tmp,
                       &c->bs.seg_ids, &c->bs.seg_starts, &c->bs.seg_valid, &c->bs.seg_rank,
@@ -249,6 +267,7 @@ int ndt_ctx_configure(ndt_ctx* c, const ndt_config* cfg) {
         return NDT_ERR_INVALID_ARGUMENT;
     }
     c->cfg = n;
+    c->cfg_gen++;
     gauss_params((double)n.resolution, n.outlier_ratio, &c->d1, &c->d2);
     return NDT_OK;
 }
@@ -300,6 +319,7 @@ int ndt_stats_reset(ndt_ctx* c) {
 
 static int set_target_dev(ndt_ctx* c, const float* d_xyz, uint64_t n) {
     c->map.valid = false;
+    c->map_gen++;  // captured batches bake the map in
     float ms = 0.f;
     int rc = build_map(c->map, c->bs, d_xyz, (size_t)n, c->cfg, (uint32_t*)c->d_status.p,
                        c->stream, &ms);
@@ -449,8 +469,6 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         hs[j] = s;
     }
     cudaStream_t st = c->stream;
-    cudaMemcpyAsync(c->d_jobs.p, hj, jb + 0, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
     c->stats.h2d_bytes += jb + sjb;
     AlignParams p{};
     p.map = c->map.view;
@@ -483,20 +501,69 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         p.trace = (double*)c->d_trace.p;
     }
     LaunchShape shape = choose_shape(c, nj, max_n);
-    cudaEventRecord(c->ev0, st);
-    if ((rc = launch_align(p, shape, st))) return rc;
-    cudaEventRecord(c->ev1, st);
-    if ((rc = launch_score(c->map.view, d_pts, (const ScoreJob*)c->d_sjobs.p, nj, max_n,
-                           (const AlignOut*)c->d_aout.p, c->d_part.p, (ScoreOut*)c->d_sout.p,
-                           (float)c->d1, (float)c->d2, st)))
-        return rc;
-    cudaEventRecord(c->ev2, st);
     AlignOut* ho = (AlignOut*)c->h_aout.p;
     ScoreOut* hso = (ScoreOut*)((char*)c->h_aout.p + ob);
     uint32_t* hst = (uint32_t*)((char*)c->h_aout.p + ob + sob);
-    cudaMemcpyAsync(ho, c->d_aout.p, ob, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(hso, c->d_sout.p, sob, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(hst, c->d_status.p, 4, cudaMemcpyDeviceToHost, st);
+    // the batch on the stream: job tables in, Newton kernel, NVTL scoring, results out (the
+    // events are graph nodes when captured)
+    auto enqueue = [&](unsigned evf) -> int {
+        cudaMemcpyAsync(c->d_jobs.p, hj, jb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
+        cudaEventRecordWithFlags(c->ev0, st, evf);
+        int r = launch_align(p, shape, st);
+        if (r) return r;
+        cudaEventRecordWithFlags(c->ev1, st, evf);
+        r = launch_score(c->map.view, d_pts, (const ScoreJob*)c->d_sjobs.p, nj, max_n,
+                         (const AlignOut*)c->d_aout.p, c->d_part.p, (ScoreOut*)c->d_sout.p,
+                         (float)c->d1, (float)c->d2, st);
+        if (r) return r;
+        cudaEventRecordWithFlags(c->ev2, st, evf);
+        cudaMemcpyAsync(ho, c->d_aout.p, ob, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(hso, c->d_sout.p, sob, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(hst, c->d_status.p, 4, cudaMemcpyDeviceToHost, st);
+        return cuda_fail(cudaGetLastError(), "align enqueue");
+    };
+    if (c->cfg.cuda_graph && !c->trace) {
+        const std::vector<uint64_t> key = {
+            nj, max_n, (uint64_t)shape.cluster, (uint64_t)shape.threads, (uint64_t)shape.regcap,
+            c->map_gen, c->cfg_gen, (uint64_t)(uintptr_t)d_pts, (uint64_t)(uintptr_t)c->d_jobs.p,
+            (uint64_t)(uintptr_t)c->d_aout.p, (uint64_t)(uintptr_t)c->d_sjobs.p,
+            (uint64_t)(uintptr_t)c->d_sout.p, (uint64_t)(uintptr_t)c->d_part.p,
+            (uint64_t)(uintptr_t)c->h_jobs.p, (uint64_t)(uintptr_t)c->h_aout.p};
+        size_t gi = c->graphs.size();
+        for (size_t i = 0; i < c->graphs.size(); ++i)
+            if (c->graphs[i].key == key) gi = i;
+        if (gi == c->graphs.size()) {
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+            rc = enqueue(cudaEventRecordExternal);  // event nodes inside the graph
+            e = cudaStreamEndCapture(st, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+            if (c->graphs.size() >= 8) {
+                cudaGraphExecDestroy(c->graphs.front().exec);
+                c->graphs.erase(c->graphs.begin());
+            }
+            c->graphs.push_back({key, exec});
+            gi = c->graphs.size() - 1;
+        } else if (gi + 1 != c->graphs.size()) {  // most recently used last
+            auto g = c->graphs[gi];
+            c->graphs.erase(c->graphs.begin() + (long)gi);
+            c->graphs.push_back(g);
+            gi = c->graphs.size() - 1;
+        }
+        if ((rc = cuda_fail(cudaGraphLaunch(c->graphs[gi].exec, st), "graph launch"))) return rc;
+    } else if ((rc = enqueue(cudaEventRecordDefault))) {
+        return rc;
+    }
     c->stats.d2h_bytes += ob + sob + 4;
     if ((rc = cuda_fail(cudaStreamSynchronize(st), "align"))) return rc;
     if ((rc = check_status(c, *hst))) return rc;
@@ -515,9 +582,15 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
     c->stats.align_kernel_ms += ams;
     c->stats.score_launches++;
     c->stats.score_kernel_ms += sms;
+    uint64_t t0 = UINT64_MAX;
+    for (uint32_t j = 0; j < nj; ++j) t0 = std::min(t0, ho[j].t_start);
+    c->t_start_ms.assign(nj, 0.0);
+    c->t_finish_ms.assign(nj, 0.0);
     for (uint32_t j = 0; j < nj; ++j) {
         const AlignOut& o = ho[j];
         const ScoreOut& so = hso[j];
+        c->t_start_ms[jobs[j].slot] = (double)(o.t_start - t0) * 1e-6;
+        c->t_finish_ms[jobs[j].slot] = (double)(o.t_end - t0) * 1e-6;
         ndt_result& r = out[jobs[j].slot];
         std::memset(&r, 0, sizeof r);
         for (int i = 0; i < 6; ++i) r.pose[i] = o.pose[i];
@@ -593,6 +666,142 @@ int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* o
         cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
     c->stats.h2d_bytes += total * 12;
     return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
+}
+
+int ndt_batch_timings(ndt_ctx* c, double* start_ms, double* finish_ms, uint64_t n) {
+    if (!c || (n && (!start_ms || !finish_ms))) return NDT_ERR_INVALID_ARGUMENT;
+    if (n > c->t_start_ms.size()) {
+        set_error("more timings requested than alignments in the last call");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    for (uint64_t i = 0; i < n; ++i) {
+        start_ms[i] = c->t_start_ms[i];
+        finish_ms[i] = c->t_finish_ms[i];
+    }
+    return NDT_OK;
+}
+
+}  // extern "C"
+
+// SplitMix64 (Steele, Lea, Flood 2014): the particle generator's stream
+static inline uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+static inline double unit_double(uint64_t& s) {  // [0, 1), 53 bits
+    return (double)(splitmix64(s) >> 11) * 0x1.0p-53;
+}
+
+// Particle k of query q (documented with ndt_initial_pose_search): stream seeded by
+// (seed, q, k); draws in the order x, y, yaw, then z, roll, pitch (Box-Muller normals).
+static void make_particle(const ndt_particle_config& pc, uint64_t q, uint64_t k,
+                          const double* prior, double* pose) {
+    uint64_t s = pc.seed ^ (0x9e3779b97f4a7c15ull * (q + 1)) ^ (0xd1b54a32d192ed03ull * (k + 1));
+    splitmix64(s);
+    for (int i = 0; i < 6; ++i) pose[i] = prior[i];
+    pose[0] += (2.0 * unit_double(s) - 1.0) * pc.xy_range;
+    pose[1] += (2.0 * unit_double(s) - 1.0) * pc.xy_range;
+    pose[5] += (2.0 * unit_double(s) - 1.0) * pc.yaw_range;
+    const double sig[3] = {pc.z_sigma, pc.roll_pitch_sigma, pc.roll_pitch_sigma};
+    const int dim[3] = {2, 3, 4};
+    for (int i = 0; i < 3; ++i) {
+        const double u1 = 1.0 - unit_double(s), u2 = unit_double(s);
+        const double nrm = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        if (sig[i] > 0.0) pose[dim[i]] += sig[i] * nrm;
+    }
+}
+
+extern "C" {
+
+int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
+                            const ndt_particle_config* pc, ndt_pose_estimate* out,
+                            ndt_result* particles) {
+    if (!c || !pc || (nq && (!queries || !out))) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (nq == 0) return NDT_OK;
+    const uint64_t np = pc->num_particles;
+    if (np == 0 || !(pc->xy_range >= 0.0) || !(pc->yaw_range >= 0.0) ||
+        !(pc->z_sigma >= 0.0) || !(pc->roll_pitch_sigma >= 0.0)) {
+        set_error("invalid particle configuration");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    if (nq * np > 0xFFFFFFull) {
+        set_error("too many particles in one search (queries x particles > 2^24)");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaSetDevice(c->device);
+    uint64_t total = 0;
+    for (uint64_t q = 0; q < nq; ++q) {
+        if (queries[q].num_points == 0) {
+            set_error("Source point cloud is empty");
+            return NDT_ERR_EMPTY_INPUT;
+        }
+        if (!queries[q].xyz) return NDT_ERR_INVALID_ARGUMENT;
+        if (queries[q].num_points > 0xFFFFFFF0ull) {
+            set_error("scan exceeds 2^32 points");
+            return NDT_ERR_CAPACITY;
+        }
+        total += queries[q].num_points;
+    }
+    // each query's points are uploaded once; all of its particles share them
+    if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
+        return rc;
+    std::vector<AlignJob> jobs(nq * np);
+    std::vector<uint64_t> ns(nq * np);
+    uint64_t off = 0;
+    char* hp = (char*)c->h_pts.p;
+    for (uint64_t q = 0; q < nq; ++q) {
+        std::memcpy(hp + off * 12, queries[q].xyz, queries[q].num_points * 12);
+        for (uint64_t k = 0; k < np; ++k) {
+            AlignJob& j = jobs[q * np + k];
+            j.offset = off;
+            j.n = (uint32_t)queries[q].num_points;
+            j.slot = (uint32_t)(q * np + k);
+            make_particle(*pc, q, k, queries[q].initial_pose, j.pose);
+            ns[q * np + k] = queries[q].num_points;
+        }
+        off += queries[q].num_points;
+    }
+    cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
+    c->stats.h2d_bytes += total * 12;
+    std::vector<AlignJob> starts = jobs;  // run_align reorders its copy
+    std::vector<ndt_result> local;
+    ndt_result* res = particles;
+    if (!res) {
+        local.resize(nq * np);
+        res = local.data();
+    }
+    if ((rc = run_align(c, (const float*)c->d_in.p, jobs, ns, res))) return rc;
+    // select_best_particle: highest selection score, the later particle on ties
+    for (uint64_t q = 0; q < nq; ++q) {
+        int64_t best = -1;
+        double best_sel = -INFINITY;
+        for (uint64_t k = 0; k < np; ++k) {
+            const ndt_result& r = res[q * np + k];
+            const double sel = r.nvtl > 0.0 ? r.nvtl : 5.0 * std::exp(-r.score / 10.0);
+            if (best < 0 || sel >= best_sel) {
+                best = (int64_t)k;
+                best_sel = sel;
+            }
+        }
+        const ndt_result& r = res[q * np + (uint64_t)best];
+        ndt_pose_estimate& e = out[q];
+        std::memset(&e, 0, sizeof e);
+        for (int i = 0; i < 6; ++i) {
+            e.pose[i] = r.pose[i];
+            e.initial_pose[i] = starts[q * np + (uint64_t)best].pose[i];
+        }
+        e.nvtl = r.nvtl;
+        e.score = r.score;
+        e.selection_score = best_sel;
+        e.particle = (int32_t)best;
+        e.iterations = r.iterations;
+        e.converged = r.converged;
+    }
+    return NDT_OK;
 }
 
 int ndt_align(ndt_ctx* c, const float* xyz, uint64_t n, const double pose_in[6], ndt_result* out) {

@@ -82,6 +82,7 @@ struct AlignOut {
     uint64_t cycles[4];  // SM cycles: points + CTA reduce, cluster wait, control, broadcast
     int32_t n_eigen;     // iterations that took the eigen (indefinite) solver path
     int32_t pad2;
+    uint64_t t_start, t_end;  // global timer (ns) when the alignment started / finished
 };
 
 // Per-iteration trace record (doubles): it, score, correspondences, pose before the step (6),

@@ -208,3 +208,59 @@ def voxelize_pcd(points, leaf):
     np.add.at(sums, inv_idx, p.astype(np.float64))
     cnt = np.bincount(inv_idx, minlength=len(uk)).astype(np.float64)
     return np.ascontiguousarray((sums / cnt[:, None]).astype(np.float32))
+
+
+@dataclass
+class SearchWorkload:
+    map_points: np.ndarray
+    scans: list
+    true_poses: np.ndarray
+    priors: np.ndarray
+
+
+def search_queries(seed=21, n_queries=16, n_map=200_000, prior_xy=1.0):
+    """Initial-pose queries on one 100x100 m single-workload map: 32-ring scans from seeded
+    poses; each prior is the true pose with x, y + U(+-prior_xy) and an unknown heading
+    (yaw uniform on the circle)."""
+    rng = np.random.default_rng(seed)
+    xy = rng.uniform(-30, 30, size=(n_queries, 2))
+    yaw = rng.uniform(-math.pi, math.pi, size=n_queries)
+    scene = Scene(seed, 100.0, 12, 40, 0, clear_xy=xy)
+    mp = scene.map_points(n_map)
+    scans, truth, priors = [], [], []
+    for i in range(n_queries):
+        t4 = np.array([xy[i, 0], xy[i, 1], 1.8, yaw[i]])
+        scans.append(scene.scan(t4, Lidar(rings=32), seed * 100 + i))
+        t6 = pose6(t4)
+        p = t6.copy()
+        p[:2] += rng.uniform(-prior_xy, prior_xy, 2)
+        p[5] = rng.uniform(-math.pi, math.pi)
+        truth.append(t6)
+        priors.append(p)
+    return SearchWorkload(mp, scans, np.array(truth), np.array(priors))
+
+
+def queue_scans(seed=22, n_scans=64, lo=2000, hi=40000, n_map=200_000):
+    """A queue of scans of uneven size on one single-workload map: 128-ring scans (dense
+    band) from seeded poses, each subsampled to a log-uniform size in [lo, hi] (capped by
+    what the ray cast returns); guesses perturbed like the single workload."""
+    rng = np.random.default_rng(seed)
+    xy = rng.uniform(-30, 30, size=(n_scans, 2))
+    yaw = rng.uniform(-math.pi, math.pi, size=n_scans)
+    scene = Scene(seed, 100.0, 12, 40, 0, clear_xy=xy)
+    mp = scene.map_points(n_map)
+    lidar = Lidar(rings=128, dense=96, leaf=0.3)
+    scans, truth, guesses = [], [], []
+    for i in range(n_scans):
+        t4 = np.array([xy[i, 0], xy[i, 1], 1.8, yaw[i]])
+        s = scene.scan(t4, lidar, seed * 100 + i)
+        m = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        m = min(m, len(s))
+        scans.append(np.ascontiguousarray(s[np.sort(rng.choice(len(s), m, replace=False))]))
+        t6 = pose6(t4)
+        g = t6.copy()
+        g[:2] += rng.uniform(-0.5, 0.5, 2)
+        g[5] += math.radians(rng.uniform(-2.0, 2.0))
+        truth.append(t6)
+        guesses.append(g)
+    return SearchWorkload(mp, scans, np.array(truth), np.array(guesses))

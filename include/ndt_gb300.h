@@ -76,7 +76,8 @@ typedef struct ndt_config {
     int32_t hash_capacity_factor;  /* capacity = next pow2 >= factor * V; 2 = reference */
     int32_t max_registers;         /* Newton-kernel register cap (80 or 128); 0 = autotuned */
     int32_t cell_index;            /* NDT_CELL_INDEX_*: how kernels find a cell's voxel */
-    int32_t reserved;
+    int32_t cuda_graph;            /* 1: batches run as captured CUDA graphs (replayed while
+                                      the batch shape repeats); 0: direct launches */
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
@@ -203,6 +204,51 @@ int ndt_autotune(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
  * T34 = num_poses row-major 3x4 world transforms (host). nvtl / tp may be NULL. */
 int ndt_eval_batch(ndt_ctx* ctx, const float* xyz, uint64_t num_points, const double* T34,
                    uint64_t num_poses, double* nvtl, double* transform_probability);
+
+/* Per-alignment device timing of the last alignment call (any ndt_align* entry): start and
+ * finish of each alignment in ms, relative to the earliest start of that call, by the
+ * caller's result index. n must not exceed the number of alignments of that call. */
+int ndt_batch_timings(ndt_ctx* ctx, double* start_ms, double* finish_ms, uint64_t n);
+
+/* Multi-particle initial-pose search: estimate_initial_pose + align_batch_gpu +
+ * select_best_particle (src/cuda_ndt_matcher/src/initial_pose.rs:115-460,
+ * src/ndt_cuda/src/optimization/solver.rs:459-561, src/cuda_ndt_matcher/src/particle.rs:36-42).
+ * Every query's particles are aligned in one launch (all queries together), each result is
+ * scored by NVTL at its aligned pose, and the particle with the highest selection score wins:
+ * NVTL when positive, else 5 exp(-score / 10) (initial_pose.rs:233-245); ties go to the later
+ * particle, as Rust's max_by does. Particle k of query q starts from the query's prior pose
+ * with x, y + U(-xy_range, xy_range), yaw + U(-yaw_range, yaw_range) (yaw_range = pi covers
+ * the circle, like the reference's uniform yaw) and z, roll, pitch + N(0, sigma^2) — drawn
+ * from a SplitMix64 stream seeded by (seed, q, k), so a search is reproducible. The
+ * reference's later TPE-guided particles are sequential by design; this batched search draws
+ * all of its particles up front. */
+typedef struct ndt_particle_config {
+    uint32_t num_particles;        /* particles per query (200) */
+    uint32_t reserved;
+    double xy_range;               /* 2.0 m */
+    double yaw_range;              /* pi */
+    double z_sigma;                /* 0 */
+    double roll_pitch_sigma;       /* 0 */
+    uint64_t seed;
+} ndt_particle_config;
+
+typedef struct ndt_pose_estimate {
+    double pose[6];                /* aligned pose of the best particle */
+    double initial_pose[6];        /* the particle it started from */
+    double nvtl;
+    double score;
+    double selection_score;
+    int32_t particle;              /* index of the best particle within its query */
+    int32_t iterations;
+    int32_t converged;
+    int32_t reserved;
+} ndt_pose_estimate;
+
+/* out: num_queries estimates; particles (optional, may be NULL): num_queries *
+ * num_particles results, query-major. Each query's ndt_scan gives its points and prior. */
+int ndt_initial_pose_search(ndt_ctx* ctx, const ndt_scan* queries, uint64_t num_queries,
+                            const ndt_particle_config* cfg, ndt_pose_estimate* out,
+                            ndt_result* particles);
 
 /* 27-cell hash neighbour query (graph_hash_query_inline, ndt_graph_kernels.cu:47-104;
  * voxel_hash_query_kernel, voxel_hash.cu:136-210) for host query points; idx is

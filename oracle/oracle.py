@@ -314,3 +314,59 @@ def eigen_sym(a):
     V = np.zeros(n * n)
     (lib().or_eigen_sym3 if n == 3 else lib().or_eigen_sym6)(a.ravel(), ev, V)
     return ev, V.reshape(n, n)
+
+
+# ---------------------------------------------------------------------------------------
+# Initial-pose search (estimate_initial_pose + select_best_particle,
+# src/cuda_ndt_matcher/src/initial_pose.rs:115-460, src/cuda_ndt_matcher/src/particle.rs:36-42)
+# ---------------------------------------------------------------------------------------
+_M64 = (1 << 64) - 1
+
+
+def _splitmix64(state):
+    state = (state + 0x9E3779B97F4A7C15) & _M64
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+    return state, z ^ (z >> 31)
+
+
+def particle(prior, q, k, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0, roll_pitch_sigma=0.0,
+             seed=0):
+    """Starting pose of particle k of query q: SplitMix64 stream seeded by (seed, q, k);
+    x, y + U(-xy_range, xy_range), yaw + U(-yaw_range, yaw_range), then z, roll, pitch +
+    N(0, sigma^2) by Box-Muller."""
+    s = (seed ^ ((0x9E3779B97F4A7C15 * (q + 1)) & _M64) ^ ((0xD1B54A32D192ED03 * (k + 1)) & _M64))
+    s, _ = _splitmix64(s)
+
+    def unit():
+        nonlocal s
+        s, z = _splitmix64(s)
+        return (z >> 11) * 2.0 ** -53
+
+    p = np.array(prior, dtype=np.float64).copy()
+    p[0] += (2.0 * unit() - 1.0) * xy_range
+    p[1] += (2.0 * unit() - 1.0) * xy_range
+    p[5] += (2.0 * unit() - 1.0) * yaw_range
+    for sig, d in ((z_sigma, 2), (roll_pitch_sigma, 3), (roll_pitch_sigma, 4)):
+        u1 = 1.0 - unit()
+        u2 = unit()
+        nrm = np.sqrt(-2.0 * np.log(u1)) * np.cos(6.283185307179586 * u2)
+        if sig > 0.0:
+            p[d] += sig * nrm
+    return p
+
+
+def selection_score(nvtl, score):
+    """initial_pose.rs:233-245: NVTL when positive, else 5 exp(-score / 10)."""
+    return nvtl if nvtl > 0.0 else 5.0 * np.exp(-score / 10.0)
+
+
+def select_best(results):
+    """particle.rs:36-42 (Iterator::max_by: the last of equal maxima)."""
+    best, best_sel = -1, -np.inf
+    for i, r in enumerate(results):
+        sel = selection_score(r["nvtl"], r["score"])
+        if best < 0 or sel >= best_sel:
+            best, best_sel = i, sel
+    return best, best_sel

@@ -1,0 +1,106 @@
+"""Batched initial-pose search, CUDA-graph replay and per-alignment device timings, through
+the C ABI, against the oracle (particle stream, per-particle alignment, selection rule)."""
+import numpy as np
+import pytest
+
+from cuda_ndt_matcher_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+NP = 24
+
+
+def test_initial_pose_search_matches_oracle(gpu, oracle, single_cases):
+    case = single_cases[0]
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    g = oracle.Grid(case.map_points, 2.0)
+    off = np.array([0.6, -0.4, 0.0, 0.0, 0.0, 0.25])
+    priors = [case.guess, case.true_pose + off]
+    queries = [case.scan, case.scan]
+    est, parts = ctx.initial_pose_search(queries, priors, num_particles=NP, xy_range=1.0,
+                                         yaw_range=0.3, seed=11, return_particles=True)
+    agree = 0
+    for q in range(2):
+        starts = [oracle.particle(priors[q], q, k, 1.0, 0.3, seed=11) for k in range(NP)]
+        e = est[q]
+        # the winner started from particle e["particle"] of the documented stream
+        np.testing.assert_allclose(e["initial_pose"], starts[e["particle"]], rtol=0, atol=1e-12)
+        got = parts[q * NP:(q + 1) * NP]
+        # the selection rule applied to the GPU's particle results picks the GPU's estimate
+        b, sel = oracle.select_best(got)
+        assert b == e["particle"]
+        assert abs(sel - e["selection_score"]) <= 1e-12 * abs(sel)
+        np.testing.assert_array_equal(e["pose"], got[b]["pose"])
+        # every particle against the oracle's alignment from the same start. Particles that
+        # start far off wander through indefinite Hessians, where trajectories are chaotic
+        # (the per-iteration shadow tests pin the kernel there); most reproduce end to end
+        want = [g.align(queries[q], s, semantics="gpu") for s in starts]
+        for r, w in zip(got, want):
+            if (r["iterations"] == w["iterations"]
+                    and np.abs(r["pose"][:3] - w["pose"][:3]).max() <= 1e-4
+                    and np.abs(r["pose"][3:] - w["pose"][3:]).max() <= 1e-5
+                    and abs(r["nvtl"] - w["nvtl"]) <= 1e-5 * abs(w["nvtl"])):
+                agree += 1
+        # the best particle of the oracle's search reaches the same optimum
+        bo, selo = oracle.select_best(want)
+        assert abs(sel - selo) <= 1e-4 * abs(selo)
+        assert np.abs(e["pose"][:3] - want[bo]["pose"][:3]).max() <= 0.05
+    assert agree >= int(0.75 * 2 * NP), agree
+
+
+def test_initial_pose_search_finds_truth(gpu, single_cases):
+    """Full-circle yaw, +-2 m: the search recovers the true pose of a seeded scene."""
+    case = single_cases[1]
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    prior = case.true_pose.copy()
+    prior[:2] += [1.2, -0.9]
+    prior[5] += 2.5
+    est = ctx.initial_pose_search([case.scan], [prior], num_particles=200, xy_range=2.0,
+                                  yaw_range=np.pi, seed=3)[0]
+    assert np.abs(est["pose"][:2] - case.true_pose[:2]).max() < 0.2
+    dyaw = (est["pose"][5] - case.true_pose[5] + np.pi) % (2 * np.pi) - np.pi
+    assert abs(dyaw) < np.radians(1.0)
+
+
+def test_cuda_graph_replay_matches_direct_launch(gpu):
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=40, scan_points=4000)
+    scans = [seq.scan(k) for k in (3, 9, 15, 21)]
+    poses_a = [seq.guess(k) for k in (3, 9, 15, 21)]
+    poses_b = [p + np.array([0.05, -0.03, 0, 0, 0, 0.004]) for p in poses_a]
+    direct = capi.Context()
+    graph = capi.Context(cuda_graph=1)
+    for c in (direct, graph):
+        c.set_target(seq.map)
+    for poses in (poses_a, poses_b, poses_a):  # capture, replay with new job tables, replay
+        want = direct.align_batch(scans, poses)
+        got = graph.align_batch(scans, poses)
+        for w, r in zip(want, got):
+            np.testing.assert_array_equal(r["pose"], w["pose"])
+            np.testing.assert_array_equal(r["hessian"], w["hessian"])
+            assert r["score"] == w["score"] and r["nvtl"] == w["nvtl"]
+            assert r["iterations"] == w["iterations"]
+    # a different batch shape is captured separately
+    got = graph.align_batch(scans[:3], poses_a[:3])
+    want = direct.align_batch(scans[:3], poses_a[:3])
+    for w, r in zip(want, got):
+        np.testing.assert_array_equal(r["pose"], w["pose"])
+
+
+def test_batch_timings(gpu):
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=40, scan_points=0)
+    rng = np.random.default_rng(2)
+    scans = []
+    for k in range(3, 19):
+        s = seq.scan(k)
+        m = int(rng.integers(2000, min(len(s), 40_000) + 1))
+        scans.append(s[np.sort(rng.choice(len(s), m, replace=False))])
+    ctx = capi.Context()
+    ctx.set_target(seq.map)
+    res = ctx.align_batch(scans, [seq.guess(k) for k in range(3, 19)])
+    start, finish = ctx.batch_timings(len(scans))
+    assert start.min() == 0.0 and np.all(finish > start)
+    assert all(r["iterations"] >= 1 for r in res)
+    with pytest.raises(capi.NdtError):
+        ctx.batch_timings(len(scans) + 1)
