@@ -18,7 +18,8 @@ SYNTH_LIB = os.path.join(OUT, "libndt_synth.so")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["voxel_build.cu", "ndt_align.cu", "ndt_score.cu", "ndt_api.cu"]
+CU_SOURCES = ["voxel_build.cu", "ndt_align.cu", "ndt_score.cu", "ndt_api.cu", "tc_gemm.cu",
+              "mlp.cu"]
 CU_DEPS = ["ndt_common.cuh", "ndt_internal.h"]
 
 

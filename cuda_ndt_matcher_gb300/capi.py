@@ -27,6 +27,9 @@ EXPORTS = [
     "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
     "ndt_autotune", "ndt_eval_batch", "ndt_batch_timings", "ndt_initial_pose_search",
+    "ndt_pnet_config_default", "ndt_pnet_create", "ndt_pnet_destroy", "ndt_pnet_get_config",
+    "ndt_pnet_add_map", "ndt_pnet_add_scan", "ndt_pnet_train", "ndt_pnet_propose",
+    "ndt_pnet_debug_grad", "ndt_pnet_params", "ndt_learned_pose_search", "ndt_gemm_bf16",
     "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
     "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
     "ndt_radix_sort_pairs_u64_u32", "ndt_radix_sort_pairs_u64_u32_static",
@@ -84,6 +87,12 @@ class PoseEstimate(C.Structure):
                 ("nvtl", C.c_double), ("score", C.c_double), ("selection_score", C.c_double),
                 ("particle", C.c_int32), ("iterations", C.c_int32), ("converged", C.c_int32),
                 ("reserved", C.c_int32)]
+
+
+class PNetConfig(C.Structure):
+    _fields_ = [("input_dim", C.c_int32), ("hidden", C.c_int32), ("hidden_layers", C.c_int32),
+                ("proposals", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_float),
+                ("xy_range", C.c_float), ("yaw_weight", C.c_float), ("seed", C.c_uint64)]
 
 
 class MapInfo(C.Structure):
@@ -145,6 +154,19 @@ def load(build_if_missing=True):
         "ndt_autotune": (C.c_int, [P, P, P, P, C.c_uint64, C.c_int32, C.POINTER(TuneResult)]),
         "ndt_eval_batch": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P, P]),
         "ndt_batch_timings": (C.c_int, [P, P, P, C.c_uint64]),
+        "ndt_pnet_config_default": (C.c_int, [C.POINTER(PNetConfig)]),
+        "ndt_pnet_create": (C.c_int, [C.POINTER(PNetConfig), C.c_int32, C.POINTER(C.c_void_p)]),
+        "ndt_pnet_destroy": (C.c_int, [P]),
+        "ndt_pnet_get_config": (C.c_int, [P, C.POINTER(PNetConfig)]),
+        "ndt_pnet_add_map": (C.c_int, [P, P, C.c_uint64, C.POINTER(C.c_int32)]),
+        "ndt_pnet_add_scan": (C.c_int, [P, C.c_int32, P, C.c_uint64, P, C.POINTER(C.c_int32)]),
+        "ndt_pnet_train": (C.c_int, [P, C.c_uint64, P]),
+        "ndt_pnet_propose": (C.c_int, [P, C.c_int32, P, C.c_uint64, P, P]),
+        "ndt_pnet_debug_grad": (C.c_int, [P, P, P, C.c_uint64, P, P]),
+        "ndt_pnet_params": (C.c_int, [P, P, C.POINTER(C.c_uint64), C.c_int32]),
+        "ndt_learned_pose_search": (C.c_int, [P, P, C.c_int32, P, C.c_uint64, C.c_double,
+                                              C.POINTER(ParticleConfig), P, P]),
+        "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, P]),
         "ndt_initial_pose_search": (C.c_int, [P, P, C.c_uint64, C.POINTER(ParticleConfig),
                                               P, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
@@ -382,3 +404,123 @@ class Context:
 
     def stats_reset(self):
         check(self.lib.ndt_stats_reset(self.h))
+
+    def learned_pose_search(self, net, map_id, queries, coarse, nvtl_threshold=2.3,
+                            fallback=None):
+        """Proposal network + NDT refinement (+ plain particle search below the NVTL
+        threshold when `fallback` is a dict of initial_pose_search particle settings)."""
+        qs = [as_xyz(q) for q in queries]
+        m = len(qs)
+        arr = (Scan * m)()
+        for i, (s, pose) in enumerate(zip(qs, coarse)):
+            arr[i].xyz = s.ctypes.data
+            arr[i].num_points = len(s)
+            for k in range(6):
+                arr[i].initial_pose[k] = float(pose[k])
+        pc = None
+        if fallback is not None:
+            f = dict(num_particles=200, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0,
+                     roll_pitch_sigma=0.0, seed=0)
+            f.update(fallback)
+            pc = ParticleConfig(**f)
+        est = (PoseEstimate * m)()
+        used = np.zeros(m, np.int32)
+        check(self.lib.ndt_learned_pose_search(self.h, net.h, map_id, arr, m, nvtl_threshold,
+                                               C.byref(pc) if pc is not None else None, est,
+                                               used.ctypes.data))
+        return [{"pose": np.array(e.pose), "initial_pose": np.array(e.initial_pose),
+                 "nvtl": e.nvtl, "score": e.score, "selection_score": e.selection_score,
+                 "particle": e.particle, "iterations": e.iterations,
+                 "converged": bool(e.converged), "fallback": bool(u)}
+                for e, u in zip(est, used)]
+
+
+class PNet:
+    """The learned initial-pose proposal network (libndt_gb300 ndt_pnet_*)."""
+
+    def __init__(self, device=0, **cfg):
+        self.lib = load()
+        self.cfg = PNetConfig()
+        check(self.lib.ndt_pnet_config_default(C.byref(self.cfg)))
+        for k, v in cfg.items():
+            setattr(self.cfg, k, v)
+        h = C.c_void_p()
+        check(self.lib.ndt_pnet_create(C.byref(self.cfg), device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ndt_pnet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_map(self, points):
+        p = as_xyz(points)
+        mid = C.c_int32()
+        check(self.lib.ndt_pnet_add_map(self.h, p.ctypes.data, len(p), C.byref(mid)))
+        return mid.value
+
+    def add_scan(self, map_id, points, pose):
+        p = as_xyz(points)
+        pose = np.ascontiguousarray(pose, np.float64)
+        sid = C.c_int32()
+        check(self.lib.ndt_pnet_add_scan(self.h, map_id, p.ctypes.data, len(p),
+                                         pose.ctypes.data, C.byref(sid)))
+        return sid.value
+
+    def train(self, steps):
+        loss = np.zeros(steps, np.float32)
+        check(self.lib.ndt_pnet_train(self.h, steps, loss.ctypes.data))
+        return loss
+
+    def propose(self, map_id, queries, coarse):
+        qs = [as_xyz(q) for q in queries]
+        m = len(qs)
+        arr = (Scan * m)()
+        for i, (s, pose) in enumerate(zip(qs, coarse)):
+            arr[i].xyz = s.ctypes.data
+            arr[i].num_points = len(s)
+            for k in range(6):
+                arr[i].initial_pose[k] = float(pose[k])
+        P = self.cfg.proposals
+        poses = np.zeros((m, P, 6))
+        logits = np.zeros((m, P))
+        check(self.lib.ndt_pnet_propose(self.h, map_id, arr, m, poses.ctypes.data,
+                                        logits.ctypes.data))
+        return poses, logits
+
+    def params(self):
+        n = C.c_uint64()
+        check(self.lib.ndt_pnet_params(self.h, None, C.byref(n), 0))
+        out = np.zeros(n.value, np.float32)
+        check(self.lib.ndt_pnet_params(self.h, out.ctypes.data, C.byref(n), 0))
+        return out
+
+    def set_params(self, values):
+        v = np.ascontiguousarray(values, np.float32)
+        n = C.c_uint64(len(v))
+        check(self.lib.ndt_pnet_params(self.h, v.ctypes.data, C.byref(n), 1))
+
+    def debug_grad(self, x, targets):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        n = C.c_uint64()
+        check(self.lib.ndt_pnet_params(self.h, None, C.byref(n), 0))
+        g = np.zeros(n.value, np.float32)
+        loss = C.c_float()
+        check(self.lib.ndt_pnet_debug_grad(self.h, x.ctypes.data, t.ctypes.data, len(x),
+                                           C.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+
+def gemm_bf16(a, b):
+    """D = A B^T for torch bf16 CUDA tensors A [m x k], B [n x k] (k % 64 == 0)."""
+    import torch
+    m, k = a.shape
+    n = b.shape[0]
+    d = torch.empty((m, n), dtype=torch.float32, device=a.device)
+    check(load().ndt_gemm_bf16(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                               C.c_void_p(d.data_ptr()), m, n, k, None))
+    return d

@@ -713,25 +713,31 @@ static void make_particle(const ndt_particle_config& pc, uint64_t q, uint64_t k,
     }
 }
 
-extern "C" {
-
-int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
-                            const ndt_particle_config* pc, ndt_pose_estimate* out,
-                            ndt_result* particles) {
-    if (!c || !pc || (nq && (!queries || !out))) return NDT_ERR_INVALID_ARGUMENT;
-    int rc = need_target(c);
-    if (rc) return rc;
-    if (nq == 0) return NDT_OK;
-    const uint64_t np = pc->num_particles;
-    if (np == 0 || !(pc->xy_range >= 0.0) || !(pc->yaw_range >= 0.0) ||
-        !(pc->z_sigma >= 0.0) || !(pc->roll_pitch_sigma >= 0.0)) {
-        set_error("invalid particle configuration");
-        return NDT_ERR_INVALID_ARGUMENT;
+static int check_queries(const ndt_scan* queries, uint64_t nq) {
+    for (uint64_t q = 0; q < nq; ++q) {
+        if (queries[q].num_points == 0) {
+            set_error("Source point cloud is empty");
+            return NDT_ERR_EMPTY_INPUT;
+        }
+        if (!queries[q].xyz) return NDT_ERR_INVALID_ARGUMENT;
+        if (queries[q].num_points > 0xFFFFFFF0ull) {
+            set_error("scan exceeds 2^32 points");
+            return NDT_ERR_CAPACITY;
+        }
     }
+    return 0;
+}
+
+// np starting poses per query (starts: nq * np * 6) aligned in one launch, each scored by
+// NVTL at its aligned pose, then select_best_particle per query.
+static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, uint64_t np,
+                              const double* starts, ndt_pose_estimate* out,
+                              ndt_result* particles) {
     if (nq * np > 0xFFFFFFull) {
         set_error("too many particles in one search (queries x particles > 2^24)");
         return NDT_ERR_CAPACITY;
     }
+    int rc;
     cudaSetDevice(c->device);
     uint64_t total = 0;
     for (uint64_t q = 0; q < nq; ++q) {
@@ -760,14 +766,13 @@ int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
             j.offset = off;
             j.n = (uint32_t)queries[q].num_points;
             j.slot = (uint32_t)(q * np + k);
-            make_particle(*pc, q, k, queries[q].initial_pose, j.pose);
+            for (int d = 0; d < 6; ++d) j.pose[d] = starts[6 * (q * np + k) + d];
             ns[q * np + k] = queries[q].num_points;
         }
         off += queries[q].num_points;
     }
     cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
     c->stats.h2d_bytes += total * 12;
-    std::vector<AlignJob> starts = jobs;  // run_align reorders its copy
     std::vector<ndt_result> local;
     ndt_result* res = particles;
     if (!res) {
@@ -792,7 +797,7 @@ int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
         std::memset(&e, 0, sizeof e);
         for (int i = 0; i < 6; ++i) {
             e.pose[i] = r.pose[i];
-            e.initial_pose[i] = starts[q * np + (uint64_t)best].pose[i];
+            e.initial_pose[i] = starts[6 * (q * np + (uint64_t)best) + i];
         }
         e.nvtl = r.nvtl;
         e.score = r.score;
@@ -801,6 +806,65 @@ int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
         e.iterations = r.iterations;
         e.converged = r.converged;
     }
+    return NDT_OK;
+}
+
+extern "C" {
+
+int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
+                            const ndt_particle_config* pc, ndt_pose_estimate* out,
+                            ndt_result* particles) {
+    if (!c || !pc || (nq && (!queries || !out))) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (nq == 0) return NDT_OK;
+    const uint64_t np = pc->num_particles;
+    if (np == 0 || !(pc->xy_range >= 0.0) || !(pc->yaw_range >= 0.0) ||
+        !(pc->z_sigma >= 0.0) || !(pc->roll_pitch_sigma >= 0.0)) {
+        set_error("invalid particle configuration");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    if ((rc = check_queries(queries, nq))) return rc;
+    if (nq * np > 0xFFFFFFull) {
+        set_error("too many particles in one search (queries x particles > 2^24)");
+        return NDT_ERR_CAPACITY;
+    }
+    std::vector<double> starts(nq * np * 6);
+    for (uint64_t q = 0; q < nq; ++q)
+        for (uint64_t k = 0; k < np; ++k)
+            make_particle(*pc, q, k, queries[q].initial_pose, &starts[6 * (q * np + k)]);
+    return search_from_starts(c, queries, nq, np, starts.data(), out, particles);
+}
+
+int ndt_learned_pose_search(ndt_ctx* c, ndt_pnet* net, int32_t map_id, const ndt_scan* queries,
+                            uint64_t nq, double nvtl_threshold,
+                            const ndt_particle_config* fallback, ndt_pose_estimate* out,
+                            int32_t* used_fallback) {
+    if (!c || !net || (nq && (!queries || !out))) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (nq == 0) return NDT_OK;
+    if ((rc = check_queries(queries, nq))) return rc;
+    ndt_pnet_config pcfg;
+    if ((rc = ndt_pnet_get_config(net, &pcfg))) return rc;
+    const uint64_t np = (uint64_t)pcfg.proposals;
+    std::vector<double> starts(nq * np * 6);
+    if ((rc = ndt_pnet_propose(net, map_id, queries, nq, starts.data(), nullptr))) return rc;
+    if ((rc = search_from_starts(c, queries, nq, np, starts.data(), out, nullptr))) return rc;
+    std::vector<uint64_t> redo;
+    for (uint64_t q = 0; q < nq; ++q) {
+        const bool fb = fallback && out[q].nvtl < nvtl_threshold;
+        if (used_fallback) used_fallback[q] = fb ? 1 : 0;
+        if (fb) redo.push_back(q);
+    }
+    if (redo.empty()) return NDT_OK;
+    std::vector<ndt_scan> sub(redo.size());
+    for (size_t i = 0; i < redo.size(); ++i) sub[i] = queries[redo[i]];
+    std::vector<ndt_pose_estimate> sub_out(redo.size());
+    if ((rc = ndt_initial_pose_search(c, sub.data(), sub.size(), fallback, sub_out.data(),
+                                      nullptr)))
+        return rc;
+    for (size_t i = 0; i < redo.size(); ++i) out[redo[i]] = sub_out[i];
     return NDT_OK;
 }
 

@@ -250,6 +250,69 @@ int ndt_initial_pose_search(ndt_ctx* ctx, const ndt_scan* queries, uint64_t num_
                             const ndt_particle_config* cfg, ndt_pose_estimate* out,
                             ndt_result* particles);
 
+/* ---- Learned initial-pose proposals ---------------------------------------------------
+ * No counterpart in the reference, which draws all initial-pose particles at random (or from
+ * its sequential TPE). A small network (the "proposal network") maps a scan and a coarse
+ * pose to a few candidate poses. Each candidate is refined by plain NDT and judged by NVTL;
+ * when the best NVTL is below a threshold, the plain particle search runs instead.
+ * - Input: a 64 x 64 x 8 occupancy grid of the scan at 1 m, rotated by the coarse yaw, plus
+ *   a 64 x 64 crop at 1 m of the map's height image around the coarse position.
+ * - Layers: hidden_layers x hidden (GELU), then proposals x (dx, dy, dyaw, logit).
+ * - Every matrix product runs on the tcgen05 tensor cores (bf16 operands, f32 accumulate).
+ * - Training pairs come from scans with known converged poses (ndt_pnet_add_scan), perturbed
+ *   on the device: x, y + U(-xy_range, xy_range), yaw uniform on the circle. */
+typedef struct ndt_pnet_config {
+    int32_t input_dim;             /* 36864 = 64*64*8 scan grid + 64*64 map crop */
+    int32_t hidden;                /* 512 */
+    int32_t hidden_layers;         /* 4 */
+    int32_t proposals;             /* 16 */
+    int32_t batch;                 /* 256: training batch, inference chunk */
+    float learning_rate;           /* Adam, 3e-4 */
+    float xy_range;                /* training perturbation of x, y (m): 5 */
+    float yaw_weight;              /* loss weight of the yaw error (its scale pi / yaw_weight
+                                      against 4 m for x, y): 8 */
+    uint64_t seed;                 /* weight initialisation and training samples */
+} ndt_pnet_config;
+
+typedef struct ndt_pnet ndt_pnet;
+
+int ndt_pnet_config_default(ndt_pnet_config* cfg);
+int ndt_pnet_create(const ndt_pnet_config* cfg, int32_t device, ndt_pnet** out);
+int ndt_pnet_destroy(ndt_pnet* net);
+int ndt_pnet_get_config(ndt_pnet* net, ndt_pnet_config* out);
+/* Adds a map (host points) for features: its 1 m height image. Returns its id. */
+int ndt_pnet_add_map(ndt_pnet* net, const float* xyz, uint64_t num_points, int32_t* map_id);
+/* Adds a training scan (sensor frame, host) of map `map_id` with its converged pose. */
+int ndt_pnet_add_scan(ndt_pnet* net, int32_t map_id, const float* xyz, uint64_t num_points,
+                      const double pose[6], int32_t* scan_id);
+/* `steps` Adam steps of `batch` freshly perturbed samples; loss_out (optional) per step. */
+int ndt_pnet_train(ndt_pnet* net, uint64_t steps, float* loss_out);
+/* Candidate poses of each query (its ndt_scan's initial_pose is the coarse pose):
+ * poses num_queries * proposals * 6, logits num_queries * proposals (optional). */
+int ndt_pnet_propose(ndt_pnet* net, int32_t map_id, const ndt_scan* queries,
+                     uint64_t num_queries, double* poses, double* logits);
+/* One forward + backward on given inputs x (b x input_dim, rounded to bf16) and targets
+ * (b x 3: dx, dy in m, dyaw in rad): mean loss and every parameter's gradient (the
+ * ndt_pnet_params order), without an update. For checking against an FP64 restatement. */
+int ndt_pnet_debug_grad(ndt_pnet* net, const float* x, const float* targets, uint64_t b,
+                        float* loss, float* grads);
+/* Parameters in f32, layer by layer (W out x in row-major, then b): read (set = 0) or
+ * write (set = 1). With params NULL, *count receives the number of values. */
+int ndt_pnet_params(ndt_pnet* net, float* params, uint64_t* count, int32_t set);
+/* Learned initial-pose search on the context's target map (also added to the network as
+ * map_id): proposals -> one alignment launch for all queries -> NVTL -> selection as in
+ * ndt_initial_pose_search; queries whose best NVTL is below nvtl_threshold (2.3) rerun as
+ * a plain particle search with `fallback`. used_fallback (optional): 1 per such query. */
+int ndt_learned_pose_search(ndt_ctx* ctx, ndt_pnet* net, int32_t map_id, const ndt_scan* queries,
+                            uint64_t num_queries, double nvtl_threshold,
+                            const ndt_particle_config* fallback, ndt_pose_estimate* out,
+                            int32_t* used_fallback);
+
+/* The network's GEMM: D[m x n] (f32, row-major) = A[m x k] B[n x k]^T with A, B bf16
+ * row-major (device), k a multiple of 64; synchronous (checks the kernel's wait limits). */
+int ndt_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
+                  void* stream);
+
 /* 27-cell hash neighbour query (graph_hash_query_inline, ndt_graph_kernels.cu:47-104;
  * voxel_hash_query_kernel, voxel_hash.cu:136-210) for host query points; idx is
  * num_points * max_neighbors voxel indices (Morton order), -1 padded. */
