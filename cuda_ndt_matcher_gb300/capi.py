@@ -166,7 +166,7 @@ def load(build_if_missing=True):
         "ndt_pnet_params": (C.c_int, [P, P, C.POINTER(C.c_uint64), C.c_int32]),
         "ndt_learned_pose_search": (C.c_int, [P, P, C.c_int32, P, C.c_uint64, C.c_double,
                                               C.POINTER(ParticleConfig), P, P]),
-        "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, P]),
+        "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
         "ndt_initial_pose_search": (C.c_int, [P, P, C.c_uint64, C.POINTER(ParticleConfig),
                                               P, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
@@ -515,12 +515,13 @@ class PNet:
         return loss.value, g
 
 
-def gemm_bf16(a, b):
-    """D = A B^T for torch bf16 CUDA tensors A [m x k], B [n x k] (k % 64 == 0)."""
+def gemm_bf16(a, b, splits=1):
+    """D = A B^T for torch bf16 CUDA tensors A [m x k], B [n x k] (k % 64 == 0); with
+    splits > 1 the split-K partial products are computed and summed here."""
     import torch
     m, k = a.shape
     n = b.shape[0]
-    d = torch.empty((m, n), dtype=torch.float32, device=a.device)
+    d = torch.empty((splits, m, n), dtype=torch.float32, device=a.device)
     check(load().ndt_gemm_bf16(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
-                               C.c_void_p(d.data_ptr()), m, n, k, None))
-    return d
+                               C.c_void_p(d.data_ptr()), m, n, k, splits, None))
+    return d.sum(0) if splits > 1 else d[0]

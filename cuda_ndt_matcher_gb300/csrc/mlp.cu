@@ -35,7 +35,8 @@
 namespace ndtgb {
 
 int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, int ldd,
-                 uint32_t* d_err, cudaStream_t s);
+                 uint32_t* d_err, cudaStream_t s, int splits);
+constexpr int PN_MAX_SPLITS = 16;
 
 constexpr int PN_GRID = 64, PN_ZB = 8;
 constexpr int PN_SCAN_FEATS = PN_GRID * PN_GRID * PN_ZB;  // 32768
@@ -61,14 +62,22 @@ __device__ __forceinline__ float wrap_pi(float a) {
 }
 
 // ---- elementwise kernels ----------------------------------------------------------
-// Z [B x N] f32 (+ bias) -> X [B x N] bf16 and XT [N x B] bf16 (GELU unless `linear`)
-__global__ void k_bias_act(float* __restrict__ Z, const float* __restrict__ bias, int B, int N,
-                           int linear, __nv_bfloat16* __restrict__ X,
-                           __nv_bfloat16* __restrict__ XT) {
+// Z [B x N] f32 (+ bias) -> X [B x N] bf16 and XT [N x B] bf16 (GELU unless `linear`);
+// with split-K partials Zp (splits x [B x N]) Z is their sum
+__global__ void k_bias_act(float* __restrict__ Z, const float* __restrict__ Zp, int splits,
+                           const float* __restrict__ bias, int B, int N, int linear,
+                           __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ XT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B * N) return;
     const int b = i / N, n = i % N;
-    const float z = Z[i] + bias[n];
+    float acc;
+    if (Zp) {
+        acc = 0.f;
+        for (int s = 0; s < splits; ++s) acc += Zp[(size_t)s * B * N + i];
+    } else {
+        acc = Z[i];
+    }
+    const float z = acc + bias[n];
     Z[i] = z;
     if (X) {
         const __nv_bfloat16 h = __float2bfloat16(linear ? z : gelu(z));
@@ -333,6 +342,7 @@ struct ndt_pnet {
     int cap_b = 0;
     std::vector<DevBuf> X, XT, Z, dZ, dZT, dZf, dX;  // per layer
     DevBuf loss, T, smp, coarse, poses, logits, err;
+    DevBuf Zp;              // split-K partial products
     DevBuf q_pts, q_scans;  // inference queries
     // data
     std::vector<PnMap> maps_h;
@@ -390,6 +400,9 @@ static int pn_reserve_batch(ndt_pnet* p, int B) {
             return rc;
     }
     const size_t no = (size_t)p->cfg.proposals * PN_OUT_PER;
+    size_t max_out = 0;
+    for (auto& L : p->L) max_out = std::max(max_out, (size_t)L.out);
+    if ((rc = dev_reserve(p->Zp, (size_t)PN_MAX_SPLITS * B * max_out * 4))) return rc;
     if ((rc = dev_reserve(p->loss, (size_t)B * 4)) || (rc = dev_reserve(p->T, (size_t)B * 12)) ||
         (rc = dev_reserve(p->smp, (size_t)B * sizeof(PnSample))) ||
         (rc = dev_reserve(p->coarse, (size_t)B * 48)) ||
@@ -435,12 +448,19 @@ static int pn_forward(ndt_pnet* p, int B) {
     int rc;
     for (int l = 0; l < nl; ++l) {
         PnLayer& L = p->L[l];
-        if ((rc = gemm_bf16_tn(p->X[l].p, L.wb.p, (float*)p->Z[l].p, B, L.out, L.in, L.out,
-                               (uint32_t*)p->err.p, s)))
+        // a long K over few output tiles (the input layer) is split so every SM streams a
+        // share of the operands
+        const int tiles = ((B + 127) / 128) * ((L.out + 127) / 128);
+        int splits = 1;
+        if (tiles < 64 && L.in >= 4096) splits = std::min(PN_MAX_SPLITS, L.in / 64 / 8);
+        float* dst = splits > 1 ? (float*)p->Zp.p : (float*)p->Z[l].p;
+        if ((rc = gemm_bf16_tn(p->X[l].p, L.wb.p, dst, B, L.out, L.in, L.out,
+                               (uint32_t*)p->err.p, s, splits)))
             return rc;
         const bool last = l == nl - 1;
         k_bias_act<<<blocks((size_t)B * L.out), 256, 0, s>>>(
-            (float*)p->Z[l].p, (const float*)L.b.p, B, L.out, last ? 1 : 0,
+            (float*)p->Z[l].p, splits > 1 ? (const float*)p->Zp.p : nullptr, splits,
+            (const float*)L.b.p, B, L.out, last ? 1 : 0,
             last ? nullptr : (__nv_bfloat16*)p->X[l + 1].p,
             last ? nullptr : (__nv_bfloat16*)p->XT[l + 1].p);
     }
@@ -456,14 +476,14 @@ static int pn_backward(ndt_pnet* p, int B) {
         PnLayer& L = p->L[l];
         // dW = dZ^T X  (A = dZ^T [out x B], B-operand = X^T [in x B])
         if ((rc = gemm_bf16_tn(p->dZT[l].p, p->XT[l].p, (float*)L.gw.p, L.out, L.in, B, L.in,
-                               (uint32_t*)p->err.p, s)))
+                               (uint32_t*)p->err.p, s, 1)))
             return rc;
         k_colsum<<<blocks(L.out), 256, 0, s>>>((const float*)p->dZf[l].p, B, L.out,
                                                (float*)L.gb.p);
         if (l > 0) {
             // dX = dZ W  (A = dZ [B x out], B-operand = W^T [in x out])
             if ((rc = gemm_bf16_tn(p->dZ[l].p, L.wbt.p, (float*)p->dX[l].p, B, L.in, L.out,
-                                   L.in, (uint32_t*)p->err.p, s)))
+                                   L.in, (uint32_t*)p->err.p, s, 1)))
                 return rc;
             k_gelu_back<<<blocks((size_t)B * L.in), 256, 0, s>>>(
                 (const float*)p->dX[l].p, (const float*)p->Z[l - 1].p, B, L.in,
@@ -622,7 +642,7 @@ int ndt_pnet_destroy(ndt_pnet* p) {
         for (auto& b : *v) dev_free(b);
     for (auto& b : p->map_imgs) dev_free(b);
     for (DevBuf* b : {&p->loss, &p->T, &p->smp, &p->coarse, &p->poses, &p->logits, &p->err,
-                      &p->q_pts, &p->q_scans, &p->maps_d, &p->scan_pts_d, &p->scans_d,
+                      &p->q_pts, &p->q_scans, &p->Zp, &p->maps_d, &p->scan_pts_d, &p->scans_d,
                       &p->conv_d})
         dev_free(*b);
     pin_free(p->h_loss);

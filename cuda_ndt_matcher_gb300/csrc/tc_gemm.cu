@@ -81,7 +81,8 @@ __host__ __device__ constexpr uint32_t mma_idesc_bf16(int m, int n) {
 
 __global__ void __launch_bounds__(128, 1)
     k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   float* __restrict__ D, int M, int N, int K, int ldd, uint32_t* err) {
+                   float* __restrict__ D, int M, int N, int K, int ldd, int splits,
+                   size_t split_stride, uint32_t* err) {
     extern __shared__ __align__(1024) uint8_t gb_smem_raw[];
     __shared__ __align__(8) uint64_t full[GB_STAGES], empty[GB_STAGES], done;
     __shared__ uint32_t tmem_base;
@@ -89,7 +90,11 @@ __global__ void __launch_bounds__(128, 1)
     uint8_t* smem = (uint8_t*)(((uintptr_t)gb_smem_raw + 1023) & ~(uintptr_t)1023);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-    const int nk = K / GB_K;
+    // split-K: blockIdx.z takes k-blocks [kb0, kb1) and writes its own f32 partial of D
+    const int nk_all = K / GB_K, z = (int)blockIdx.z;
+    const int kb0 = (int)((long long)nk_all * z / splits);
+    const int nk = (int)((long long)nk_all * (z + 1) / splits) - kb0;
+    D += (size_t)z * split_stride;
 
     if (tid == 0) {
         for (int s = 0; s < GB_STAGES; ++s) {
@@ -128,7 +133,8 @@ __global__ void __launch_bounds__(128, 1)
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
                          "r"(GB_STAGE_BYTES)
                          : "memory");
-            const int kx = kb * GB_K;  // innermost coordinate: multiple of 64 bf16 = 128 B
+            const int kx = (kb0 + kb) * GB_K;  // innermost coordinate: a multiple of 64 bf16
+                                               // = 128 B
             asm volatile(
                 "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(sa)),
@@ -256,11 +262,14 @@ static int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t co
     return 0;
 }
 
+// splits > 1: split-K, partial products of k-range z at D + z * M * ldd (the caller sums)
 int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, int ldd,
-                 uint32_t* d_err, cudaStream_t s) {
+                 uint32_t* d_err, cudaStream_t s, int splits) {
     if (M <= 0 || N <= 0 || K <= 0 || K % GB_K || ldd < N || ((uintptr_t)A & 15) ||
-        ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || (ldd & 3)) {
-        set_error("gemm: K must be a multiple of 64, operands 16-byte aligned, ldd >= N");
+        ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || (ldd & 3) || splits < 1 ||
+        splits > K / GB_K || splits > 65535) {
+        set_error("gemm: K must be a multiple of 64, operands 16-byte aligned, ldd >= N, "
+                  "1 <= splits <= K / 64");
         return NDT_ERR_INVALID_ARGUMENT;
     }
     CUtensorMap ta, tb;
@@ -273,8 +282,10 @@ int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, in
         cudaFuncSetAttribute(k_gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
         attr = true;
     }
-    dim3 grid((unsigned)((N + GB_N - 1) / GB_N), (unsigned)((M + GB_M - 1) / GB_M));
-    k_gemm_bf16_tn<<<grid, 128, GB_SMEM, s>>>(ta, tb, D, M, N, K, ldd, d_err);
+    dim3 grid((unsigned)((N + GB_N - 1) / GB_N), (unsigned)((M + GB_M - 1) / GB_M),
+              (unsigned)splits);
+    k_gemm_bf16_tn<<<grid, 128, GB_SMEM, s>>>(ta, tb, D, M, N, K, ldd, splits,
+                                              (size_t)M * ldd, d_err);
     return cuda_fail(cudaGetLastError(), "gemm launch");
 }
 
@@ -284,14 +295,14 @@ static __device__ uint32_t g_gemm_err;
 }  // namespace ndtgb
 
 extern "C" int ndt_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n,
-                             int32_t k, void* stream) {
+                             int32_t k, int32_t splits, void* stream) {
     using namespace ndtgb;
     uint32_t* err = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&err, g_gemm_err);
     if (e != cudaSuccess) return cuda_fail(e, "gemm error word");
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemsetAsync(err, 0, 4, s);
-    int rc = gemm_bf16_tn(d_a, d_b, d_d, m, n, k, n, err, s);
+    int rc = gemm_bf16_tn(d_a, d_b, d_d, m, n, k, n, err, s, splits);
     if (rc) return rc;
     uint32_t h = 0;
     cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, s);

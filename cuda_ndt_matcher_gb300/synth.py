@@ -240,6 +240,45 @@ def search_queries(seed=21, n_queries=16, n_map=200_000, prior_xy=1.0):
     return SearchWorkload(mp, scans, np.array(truth), np.array(priors))
 
 
+@dataclass
+class ProposalMap:
+    map_points: np.ndarray
+    train_scans: list
+    train_poses: np.ndarray
+    test_scans: list
+    test_poses: np.ndarray
+
+
+def _proposal_map(seed, n_train, n_test, extent, n_map):
+    rng = np.random.default_rng(seed)
+    n = n_train + n_test
+    xy = rng.uniform(-extent / 2 + 30, extent / 2 - 30, size=(n, 2))
+    yaw = rng.uniform(-math.pi, math.pi, size=n)
+    area = (extent / 400.0) ** 2  # sequence-workload densities per area
+    scene = Scene(seed, extent, int(250 * area), int(800 * area), int(300 * area), clear_xy=xy)
+    mp = scene.map_points(n_map)
+    scans, poses = [], []
+    for i in range(n):
+        t4 = np.array([xy[i, 0], xy[i, 1], 1.8, yaw[i]])
+        scans.append(scene.scan(t4, Lidar(rings=32), seed * 1000 + i))
+        poses.append(pose6(t4))
+    poses = np.array(poses)
+    return ProposalMap(mp, scans[:n_train], poses[:n_train], scans[n_train:], poses[n_train:])
+
+
+def proposal_maps(seed=100, n_maps=16, n_train=400, n_test=25, extent=200.0,
+                  n_map=1_250_000, threads=None):
+    """Maps for the learned initial-pose proposals: 200x200 m tiles of the sequence-workload
+    generator (same densities of buildings, poles and tree blobs), each with 32-ring scans
+    from seeded poses split into training and held-out test scans. The ray casts run in C
+    (outside the GIL), so maps are generated in parallel threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    threads = threads or min(n_maps, os.cpu_count() or 1)
+    with ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(lambda m: _proposal_map(seed + m, n_train, n_test, extent, n_map),
+                           range(n_maps)))
+
+
 def queue_scans(seed=22, n_scans=64, lo=2000, hi=40000, n_map=200_000):
     """A queue of scans of uneven size on one single-workload map: 128-ring scans (dense
     band) from seeded poses, each subsampled to a log-uniform size in [lo, hi] (capped by

@@ -309,9 +309,12 @@ int ndt_learned_pose_search(ndt_ctx* ctx, ndt_pnet* net, int32_t map_id, const n
                             int32_t* used_fallback);
 
 /* The network's GEMM: D[m x n] (f32, row-major) = A[m x k] B[n x k]^T with A, B bf16
- * row-major (device), k a multiple of 64; synchronous (checks the kernel's wait limits). */
+ * row-major (device), k a multiple of 64; synchronous (checks the kernel's wait limits).
+ * splits > 1 (split-K, at most k / 64): D holds `splits` partial products one after the
+ * other (d_d + z * m * n covers k-blocks [z k/64/splits, (z+1) k/64/splits)); their sum is
+ * the product. */
 int ndt_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
-                  void* stream);
+                  int32_t splits, void* stream);
 
 /* 27-cell hash neighbour query (graph_hash_query_inline, ndt_graph_kernels.cu:47-104;
  * voxel_hash_query_kernel, voxel_hash.cu:136-210) for host query points; idx is

@@ -8,14 +8,16 @@ from cuda_ndt_matcher_gb300 import capi
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (256, 512, 576), (64, 512, 256),
-                                   (256, 64, 512), (300, 200, 128), (256, 512, 36864)])
-def test_gemm_bf16_matches_torch(gpu, m, n, k):
+@pytest.mark.parametrize("m,n,k,splits", [(128, 128, 64, 1), (256, 512, 576, 1),
+                                          (64, 512, 256, 1), (256, 64, 512, 1),
+                                          (300, 200, 128, 1), (256, 512, 36864, 1),
+                                          (256, 512, 36864, 16), (256, 512, 4096, 7)])
+def test_gemm_bf16_matches_torch(gpu, m, n, k, splits):
     import torch
     g = torch.Generator(device="cpu").manual_seed(m * 7 + n * 3 + k)
     a = torch.randn(m, k, generator=g).to(torch.bfloat16).cuda()
     b = torch.randn(n, k, generator=g).to(torch.bfloat16).cuda()
-    d = capi.gemm_bf16(a, b)
+    d = capi.gemm_bf16(a, b, splits)
     ref = a.float() @ b.float().T
     torch.testing.assert_close(d, ref, rtol=1e-3, atol=1e-3 * float(ref.abs().max()))
 
@@ -53,4 +55,47 @@ def test_pnet_training_reduces_loss(gpu):
     loss = net.train(300)
     assert np.all(np.isfinite(loss))
     assert loss[-50:].mean() < loss[:20].mean() - 0.3, (loss[:20].mean(), loss[-50:].mean())
+    net.close()
+
+
+def _success(pose, truth):
+    dyaw = (pose[5] - truth[5] + np.pi) % (2 * np.pi) - np.pi
+    return np.linalg.norm(pose[:2] - truth[:2]) < 0.2 and abs(dyaw) < np.radians(1.0)
+
+
+def test_learned_proposals_gain_over_random_particles(gpu):
+    """What the trained network adds. Held-out scans on the training maps, coarse poses off by
+    U(+-5 m) in x, y with an unknown heading: with the same budget of 16 NDT refinements per
+    query, the network's proposals succeed (error < 0.2 m and < 1 deg) far more often than 16
+    random particles drawn over the same range."""
+    from cuda_ndt_matcher_gb300 import synth
+    maps = synth.proposal_maps(seed=300, n_maps=8, n_train=250, n_test=15)
+    net = capi.PNet(seed=11)
+    ctx = capi.Context(cuda_graph=1)
+    mids = []
+    for m in maps:
+        mid = net.add_map(m.map_points)
+        mids.append(mid)
+        ctx.set_target(m.map_points)
+        conv = ctx.align_batch(m.train_scans, m.train_poses)
+        for s, r in zip(m.train_scans, conv):
+            net.add_scan(mid, s, r["pose"])
+    net.train(6000)
+    rng = np.random.default_rng(5)
+    ok_learned = ok_random = n = 0
+    for m, mid in zip(maps, mids):
+        ctx.set_target(m.map_points)
+        coarse = []
+        for t in m.test_poses:
+            c = t.copy()
+            c[:2] += rng.uniform(-5, 5, 2)
+            c[5] = rng.uniform(-np.pi, np.pi)
+            coarse.append(c)
+        learned = ctx.learned_pose_search(net, mid, m.test_scans, coarse)
+        rand = ctx.initial_pose_search(m.test_scans, coarse, num_particles=16, xy_range=5.0,
+                                       yaw_range=np.pi, seed=9)
+        ok_learned += sum(_success(e["pose"], t) for e, t in zip(learned, m.test_poses))
+        ok_random += sum(_success(e["pose"], t) for e, t in zip(rand, m.test_poses))
+        n += len(m.test_poses)
+    assert ok_learned / n >= ok_random / n + 0.1, (ok_learned / n, ok_random / n)
     net.close()
