@@ -1,12 +1,18 @@
 // ndt_api.cu — the C ABI of libndt_gb300.so (declared in include/ndt_gb300.h).
 //
-// A context owns one CUDA stream, the device voxel map, grow-only device buffers and pinned
-// host staging buffers. An alignment call packs the host scans into pinned memory, copies
-// them with one cudaMemcpyAsync, launches the Newton kernel (one cluster per alignment,
-// longest scans first) and the NVTL kernel on the final poses, copies the per-alignment
-// records back and synchronises once.
+// A context owns one CUDA stream, the device voxel map, grow-only device buffers, pinned
+// host staging buffers and a few host threads. An alignment call packs the host scans into
+// pinned memory with those threads, copying each packed chunk to the device while the next
+// is packed, launches the Newton kernel (one cluster per alignment, longest scans first) and
+// the NVTL kernel on the final poses (as a CUDA graph when configured), copies the
+// per-alignment records back and synchronises once.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -84,7 +90,77 @@ static void gauss_params(double res, double outlier, double* d1, double* d2) {
 
 using namespace ndtgb;
 
+// A few host threads for staging copies: run(n, f) calls f(0 .. n-1) across the workers and
+// the calling thread and returns when every call is done. Workers start on first use and
+// stop with the owning context.
+class HostPool {
+public:
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto& w : workers_) w.join();
+    }
+    void run(uint64_t n, const std::function<void(uint64_t)>& f) {
+        if (n == 0) return;
+        start();
+        if (workers_.empty() || n == 1) {
+            for (uint64_t i = 0; i < n; ++i) f(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &f;
+            n_ = n;
+            next_.store(0);
+            active_ = workers_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return active_ == 0; });
+        fn_ = nullptr;
+    }
+
+private:
+    void drain() {
+        for (uint64_t i; (i = next_.fetch_add(1)) < n_;) (*fn_)(i);
+    }
+    void start() {
+        if (started_) return;
+        started_ = true;
+        const unsigned hw = std::thread::hardware_concurrency();
+        const unsigned nt = hw > 1 ? std::min(7u, hw - 1) : 0u;
+        for (unsigned t = 0; t < nt; ++t) workers_.emplace_back([this] { loop(); });
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+            if (quit_) return;
+            seen = gen_;
+            lk.unlock();
+            drain();
+            lk.lock();
+            if (--active_ == 0) done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(uint64_t)>* fn_ = nullptr;
+    uint64_t n_ = 0, gen_ = 0;
+    std::atomic<uint64_t> next_{0};
+    size_t active_ = 0;
+    bool quit_ = false, started_ = false;
+};
+
 struct ndt_ctx {
+    HostPool pool;
     ndt_config cfg{};
     int device = 0;
     int num_sms = 0;
@@ -114,6 +190,30 @@ struct ndt_ctx {
     uint64_t map_gen = 0, cfg_gen = 0;
     std::vector<double> t_start_ms, t_finish_ms;           // last call, by result index
 };
+
+// Packs host scans into the pinned staging buffer with the context's host threads and copies
+// them to the device in chunks of about 16 MB: each chunk's copy is issued as soon as that
+// chunk is packed, so the DMA overlaps the packing of the next one.
+static void stage_scans(ndt_ctx* c, const ndt_scan* scans, uint64_t m,
+                        const std::vector<uint64_t>& offset, uint64_t total) {
+    if (total == 0) return;
+    char* hp = (char*)c->h_pts.p;
+    const uint64_t chunk_pts = (16ull << 20) / 12;
+    uint64_t i0 = 0;
+    while (i0 < m) {
+        uint64_t i1 = i0, pts = 0;
+        while (i1 < m && (pts < chunk_pts || i1 == i0)) pts += scans[i1++].num_points;
+        c->pool.run(i1 - i0, [&](uint64_t k) {
+            const uint64_t i = i0 + k;
+            std::memcpy(hp + offset[i] * 12, scans[i].xyz, scans[i].num_points * 12);
+        });
+        const uint64_t o0 = offset[i0], o1 = i1 < m ? offset[i1] : total;
+        cudaMemcpyAsync((char*)c->d_in.p + o0 * 12, hp + o0 * 12, (o1 - o0) * 12,
+                        cudaMemcpyHostToDevice, c->stream);
+        i0 = i1;
+    }
+    c->stats.h2d_bytes += total * 12;
+}
 
 static void drop_graphs(ndt_ctx* c) {
     for (auto& g : c->graphs)
@@ -650,21 +750,17 @@ int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* o
     if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
         return rc;
     std::vector<AlignJob> jobs(m);
-    std::vector<uint64_t> ns(m);
+    std::vector<uint64_t> ns(m), offset(m);
     uint64_t off = 0;
-    char* hp = (char*)c->h_pts.p;
     for (uint64_t i = 0; i < m; ++i) {
-        std::memcpy(hp + off * 12, scans[i].xyz, scans[i].num_points * 12);
-        jobs[i].offset = off;
+        jobs[i].offset = offset[i] = off;
         jobs[i].n = (uint32_t)scans[i].num_points;
         jobs[i].slot = (uint32_t)i;
         for (int k = 0; k < 6; ++k) jobs[i].pose[k] = scans[i].initial_pose[k];
         ns[i] = scans[i].num_points;
         off += scans[i].num_points;
     }
-    if (total)
-        cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
-    c->stats.h2d_bytes += total * 12;
+    stage_scans(c, scans, m, offset, total);
     return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
 }
 
@@ -756,11 +852,10 @@ static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, 
     if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
         return rc;
     std::vector<AlignJob> jobs(nq * np);
-    std::vector<uint64_t> ns(nq * np);
+    std::vector<uint64_t> ns(nq * np), qoff(nq);
     uint64_t off = 0;
-    char* hp = (char*)c->h_pts.p;
     for (uint64_t q = 0; q < nq; ++q) {
-        std::memcpy(hp + off * 12, queries[q].xyz, queries[q].num_points * 12);
+        qoff[q] = off;
         for (uint64_t k = 0; k < np; ++k) {
             AlignJob& j = jobs[q * np + k];
             j.offset = off;
@@ -771,8 +866,7 @@ static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, 
         }
         off += queries[q].num_points;
     }
-    cudaMemcpyAsync(c->d_in.p, c->h_pts.p, total * 12, cudaMemcpyHostToDevice, c->stream);
-    c->stats.h2d_bytes += total * 12;
+    stage_scans(c, queries, nq, qoff, total);
     std::vector<ndt_result> local;
     ndt_result* res = particles;
     if (!res) {
