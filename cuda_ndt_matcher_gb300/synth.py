@@ -303,3 +303,35 @@ def queue_scans(seed=22, n_scans=64, lo=2000, hi=40000, n_map=200_000):
         truth.append(t6)
         guesses.append(g)
     return SearchWorkload(mp, scans, np.array(truth), np.array(guesses))
+
+
+def large_map(seed=7, extent=2000.0, n_points=50_000_000, outlier_frac=0.05):
+    """The large-map stress workload: the sequence generator scaled to extent x extent
+    (same densities of buildings, poles and tree blobs) with a fraction of uniform outliers
+    over the box [-extent/2, extent/2]^2 x [-5, 30] m, shuffled into the surface points."""
+    area = (extent / 400.0) ** 2
+    scene = Scene(seed, extent, int(250 * area), int(800 * area), int(300 * area))
+    n_out = int(round(n_points * outlier_frac))
+    pts = scene.map_points(n_points - n_out)
+    rng = np.random.default_rng(seed)
+    out = np.empty((n_out, 3), np.float32)
+    out[:, 0] = rng.uniform(-extent / 2, extent / 2, n_out)
+    out[:, 1] = rng.uniform(-extent / 2, extent / 2, n_out)
+    out[:, 2] = rng.uniform(-5.0, 30.0, n_out)
+    allp = np.concatenate([pts, out])
+    return np.ascontiguousarray(allp[rng.permutation(len(allp))])
+
+
+def crop_scan(map_points, pose, n, radius=60.0, sigma=0.02, seed=0):
+    """A dense scan without ray casting: n map points within `radius` of the pose's
+    position (sampled without replacement), moved into the sensor frame of `pose`
+    (R = Rz(yaw)), with N(0, sigma^2) noise."""
+    rng = np.random.default_rng(seed)
+    d = map_points[:, :2] - np.asarray(pose[:2], np.float32)
+    idx = np.nonzero((d * d).sum(1) < radius * radius)[0]
+    idx = rng.choice(idx, min(n, len(idx)), replace=False)
+    q = map_points[np.sort(idx)].astype(np.float64) - np.asarray(pose[:3])
+    c, s = math.cos(pose[5]), math.sin(pose[5])
+    local = np.stack([c * q[:, 0] + s * q[:, 1], -s * q[:, 0] + c * q[:, 1], q[:, 2]], 1)
+    local += rng.normal(0, sigma, local.shape)
+    return np.ascontiguousarray(local.astype(np.float32))
