@@ -63,11 +63,27 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def rank_scan_indices(batch, rank, world):
+    """Replicas: every rank aligns its own `batch` scans of the sequence (disjoint shards,
+    no collective on the data path); the map is replicated."""
+    return [2 + rank * batch + i for i in range(batch)]
+
+
+def max_over_ranks(values, device):
+    """Timing of a multi-rank step: the slowest rank's, reduced on the given device (the
+    torch.distributed backend's: cuda for nccl, cpu for gloo)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 def make_workload(args, rank, world):
     from cuda_ndt_matcher_gb300 import synth
     n_traj = max(1000, args.batch * world + 8)
     seq = synth.Sequence(seed=args.seed, n_map=args.map_points, n_scans=n_traj)
-    ks = [2 + rank * args.batch + i for i in range(args.batch)]
+    ks = rank_scan_indices(args.batch, rank, world)
     scans = [seq.scan(k) for k in ks]
     poses = np.stack([seq.guess(k) for k in ks])
     truth = np.stack([seq.true_pose(k) for k in ks])
@@ -533,9 +549,7 @@ def run_ours(args):
     st_e2e = ctx.stats()
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([dev_ms, wall], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, wall = float(t[0]), float(t[1])
+        dev_ms, wall = max_over_ranks([dev_ms, wall], "cuda")
 
     aligns = B * args.steps * world
     value = aligns / (dev_ms / 1000.0)
