@@ -313,6 +313,49 @@ def learned_bench(steps=20000):
     return res
 
 
+def tile_stream_bench(pts, scans, guesses, events=40):
+    """Tiles of 100 x 100 m streamed over the large map at 2 m: a 5 x 5 tile window slides
+    east one tile column at a time. Each event uploads one tile, drops the one leaving the
+    window and commits a background rebuild, while a batch of dense scans is aligned on the
+    current map. Reported: rebuild time per commit (device), wall time per event (upload +
+    commit + aligning the batch + waiting for the rebuild) and the tile rate that wall time
+    sustains."""
+    from cuda_ndt_matcher_gb300 import capi
+    tx = np.floor(pts[:, 0] / 100.0).astype(np.int64)
+    ty = np.floor(pts[:, 1] / 100.0).astype(np.int64)
+    tid = (tx + 10) * 32 + (ty + 10)
+    order = np.argsort(tid, kind="stable")
+    bounds = np.searchsorted(tid[order], np.arange(32 * 32 + 1))
+    tile = lambda i, j: pts[order[bounds[(i + 10) * 32 + (j + 10)]:bounds[(i + 10) * 32 + (j + 10) + 1]]]
+    ctx = capi.Context(resolution=2.0, cuda_graph=1)
+    window = [(i, j) for i in range(-7, -2) for j in range(-2, 3)]
+    for (i, j) in window:
+        ctx.tile_put((i + 10) * 32 + (j + 10), tile(i, j))
+    ctx.tiles_commit(wait=True)
+    ev = [(i, j) for i in range(-2, -2 + events // 5 + 1) for j in range(-2, 3)][:events]
+    build_ms, wall = [], []
+    for k, (i, j) in enumerate(ev):
+        t0 = time.perf_counter()
+        ctx.tile_put((i + 10) * 32 + (j + 10), tile(i, j))
+        old = (i - 5, j)
+        ctx.tile_remove((old[0] + 10) * 32 + (old[1] + 10))
+        ctx.tiles_commit(wait=False)
+        ctx.align_batch(scans, guesses)        # alignment continues on the current map
+        while ctx.tiles_status()["pending"]:
+            time.sleep(0.0002)
+        ctx.map_info()                         # switch to the rebuilt map
+        wall.append(time.perf_counter() - t0)
+        build_ms.append(ctx.tiles_status()["build_ms"])
+    st = ctx.tiles_status()
+    ctx.close()
+    return {"tile_m": 100, "window_tiles": 25, "points_in_window": int(st["points"]),
+            "events": len(ev), "rebuild_ms_mean": float(np.mean(build_ms)),
+            "rebuild_ms_max": float(np.max(build_ms)),
+            "event_wall_ms_mean": float(np.mean(wall) * 1e3),
+            "sustained_tiles_per_s": float(1.0 / np.mean(wall)),
+            "aligned_per_event": len(scans)}
+
+
 def large_map_bench(n_points=50_000_000, n_scans=16):
     """Large-map stress: 50M points over 2 x 2 km (sequence generator densities, 5% uniform
     outliers) built at 1, 2 and 3 m. Per resolution:
@@ -377,6 +420,8 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
         wall = time.perf_counter() - t0
         st = ctx.stats()
         err = [float(np.linalg.norm(r["pose"][:2] - p[:2])) for r, p in zip(res_al, poses)]
+        if res == 2.0:
+            out["tile_streaming"] = tile_stream_bench(pts, scans, guesses)
         out["resolutions"][f"{res:g}m"] = {
             "voxels": int(info.num_voxels), "build_ms": float(info.build_ms),
             "build_gbs": nbytes / (info.build_ms / 1e3) / 1e9,

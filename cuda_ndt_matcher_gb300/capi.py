@@ -24,7 +24,8 @@ STATUS = {0: "Converged", 1: "MaxIterations", 2: "NoCorrespondences", 3: "Singul
 EXPORTS = [
     "ndt_config_default", "ndt_ctx_create", "ndt_ctx_destroy", "ndt_ctx_configure",
     "ndt_ctx_stream",
-    "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_map_voxels",
+    "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_tile_put",
+    "ndt_tile_remove", "ndt_tiles_commit", "ndt_tiles_status", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
     "ndt_autotune", "ndt_eval_batch", "ndt_batch_timings", "ndt_initial_pose_search",
     "ndt_pnet_config_default", "ndt_pnet_create", "ndt_pnet_destroy", "ndt_pnet_get_config",
@@ -146,6 +147,12 @@ def load(build_if_missing=True):
         "ndt_set_target": (C.c_int, [P, P, C.c_uint64]),
         "ndt_set_target_device": (C.c_int, [P, P, C.c_uint64]),
         "ndt_map_info_get": (C.c_int, [P, C.POINTER(MapInfo)]),
+        "ndt_tile_put": (C.c_int, [P, C.c_uint64, P, C.c_uint64]),
+        "ndt_tile_remove": (C.c_int, [P, C.c_uint64]),
+        "ndt_tiles_commit": (C.c_int, [P, C.c_int32]),
+        "ndt_tiles_status": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_float)]),
         "ndt_map_voxels": (C.c_int, [P, P, P, P, P, P, C.c_uint64]),
         "ndt_align": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(Result)]),
         "ndt_align_multi_pose": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
@@ -263,6 +270,24 @@ class Context:
     def set_target(self, points):
         p = as_xyz(points)
         check(self.lib.ndt_set_target(self.h, p.ctypes.data, len(p)))
+
+    def tile_put(self, tile_id, points):
+        p = as_xyz(points)
+        check(self.lib.ndt_tile_put(self.h, tile_id, p.ctypes.data, len(p)))
+
+    def tile_remove(self, tile_id):
+        check(self.lib.ndt_tile_remove(self.h, tile_id))
+
+    def tiles_commit(self, wait=True):
+        check(self.lib.ndt_tiles_commit(self.h, 1 if wait else 0))
+
+    def tiles_status(self):
+        nt, npnt = C.c_uint64(), C.c_uint64()
+        pend, rc, ms = C.c_int32(), C.c_int32(), C.c_float()
+        check(self.lib.ndt_tiles_status(self.h, C.byref(nt), C.byref(npnt), C.byref(pend),
+                                        C.byref(rc), C.byref(ms)))
+        return {"tiles": nt.value, "points": npnt.value, "pending": bool(pend.value),
+                "last_rc": rc.value, "build_ms": ms.value}
 
     def set_target_device(self, ptr, n):
         check(self.lib.ndt_set_target_device(self.h, ptr, n))

@@ -189,7 +189,39 @@ struct ndt_ctx {
     std::vector<GraphEntry> graphs;
     uint64_t map_gen = 0, cfg_gen = 0;
     std::vector<double> t_start_ms, t_finish_ms;           // last call, by result index
+    // map tiles and the background rebuild into the standby map
+    struct Tile {
+        uint64_t id;
+        DevBuf pts;
+        uint64_t n;
+    };
+    std::vector<Tile> tiles;
+    Map map_b;
+    BuildScratch bs_b;
+    DevBuf d_gather, d_status_b;
+    cudaStream_t bstream = nullptr;
+    std::thread builder;
+    std::atomic<int> build_state{0};  // 0 idle, 1 running, 2 finished
+    int build_rc = 0;
+    float build_ms_b = 0.f;
+    std::string build_err;
 };
+
+// Finishes a background rebuild: joins its thread and, when it succeeded, makes the standby
+// map the active one (alignment work on the old map has completed: every call synchronises).
+static void tiles_settle(ndt_ctx* c, bool wait) {
+    if (!c->builder.joinable()) return;
+    if (!wait && c->build_state.load() != 2) return;
+    c->builder.join();
+    c->build_state.store(0);
+    if (c->build_rc == 0) {
+        std::swap(c->map, c->map_b);
+        c->map_b.valid = false;
+        c->map_gen++;
+        c->stats.build_launches++;
+        c->stats.build_ms += c->build_ms_b;
+    }
+}
 
 // Packs host scans into the pinned staging buffer with the context's host threads and copies
 // them to the device in chunks of about 16 MB: each chunk's copy is issued as soon as that
@@ -319,12 +351,15 @@ int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
     cudaEventCreate(&x->ev1);
     cudaEventCreate(&x->ev2);
     cudaEventCreate(&x->ev3);
+    cudaStreamCreateWithFlags(&x->bstream, cudaStreamNonBlocking);
     int rc = dev_reserve(x->d_status, 16);
+    if (!rc) rc = dev_reserve(x->d_status_b, 16);
     if (rc) {
         delete x;
         return rc;
     }
     cudaMemsetAsync(x->d_status.p, 0, 16, x->stream);
+    cudaMemsetAsync(x->d_status_b.p, 0, 16, x->stream);
     gauss_params((double)c.resolution, c.outlier_ratio, &x->d1, &x->d2);
     *out = x;
     return NDT_OK;
@@ -334,6 +369,16 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     if (!c) return NDT_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->builder.joinable()) c->builder.join();
+    for (auto& t : c->tiles) dev_free(t.pts);
+    for (DevBuf* b : {&c->map_b.slots, &c->map_b.slot_icov, &c->map_b.slot_vidx, &c->map_b.grid,
+                      &c->map_b.vox_coord, &c->map_b.vox_mean, &c->map_b.vox_cov,
+                      &c->map_b.vox_icov, &c->map_b.vox_count, &c->bs_b.keys_a, &c->bs_b.keys_b,
+                      &c->bs_b.vals_a, &c->bs_b.vals_b, &c->bs_b.tmp, &c->bs_b.seg_ids,
+                      &c->bs_b.seg_starts, &c->bs_b.seg_valid, &c->bs_b.seg_rank,
+                      &c->bs_b.seg_rec, &c->bs_b.small, &c->d_gather, &c->d_status_b})
+        dev_free(*b);
+    if (c->bstream) cudaStreamDestroy(c->bstream);
     drop_graphs(c);
     for (DevBuf* b : {&c->map.slots, &c->map.slot_icov, &c->map.slot_vidx, &c->map.grid,
                       &c->map.vox_coord,
@@ -357,6 +402,7 @@ void* ndt_ctx_stream(ndt_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int ndt_ctx_configure(ndt_ctx* c, const ndt_config* cfg) {
     if (!c || !cfg) return NDT_ERR_INVALID_ARGUMENT;
+    tiles_settle(c, true);  // a running rebuild reads the configuration
     const ndt_config& n = *cfg;
     if (!config_ok(n) || n.device != c->cfg.device) {
         set_error("invalid configuration");
@@ -418,6 +464,7 @@ int ndt_stats_reset(ndt_ctx* c) {
 }
 
 static int set_target_dev(ndt_ctx* c, const float* d_xyz, uint64_t n) {
+    tiles_settle(c, true);
     c->map.valid = false;
     c->map_gen++;  // captured batches bake the map in
     float ms = 0.f;
@@ -462,8 +509,110 @@ int ndt_set_target_device(ndt_ctx* c, const float* d_xyz, uint64_t n) {
     return set_target_dev(c, d_xyz, n);
 }
 
+int ndt_tile_put(ndt_ctx* c, uint64_t tile_id, const float* xyz, uint64_t n) {
+    if (!c || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
+    if (n == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    cudaSetDevice(c->device);
+    ndt_ctx::Tile* t = nullptr;
+    for (auto& x : c->tiles)
+        if (x.id == tile_id) t = &x;
+    if (!t) {
+        c->tiles.push_back(ndt_ctx::Tile{tile_id, DevBuf{}, 0});
+        t = &c->tiles.back();
+    }
+    int rc = dev_reserve(t->pts, n * 12);
+    if (rc) return rc;
+    t->n = n;
+    cudaMemcpyAsync(t->pts.p, xyz, n * 12, cudaMemcpyHostToDevice, c->bstream);
+    c->stats.h2d_bytes += n * 12;
+    return cuda_fail(cudaStreamSynchronize(c->bstream), "tile upload");
+}
+
+int ndt_tile_remove(ndt_ctx* c, uint64_t tile_id) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < c->tiles.size(); ++i)
+        if (c->tiles[i].id == tile_id) {
+            // a running rebuild has already gathered its points: the buffer can go
+            tiles_settle(c, true);
+            dev_free(c->tiles[i].pts);
+            c->tiles.erase(c->tiles.begin() + (long)i);
+            return NDT_OK;
+        }
+    set_error("no such tile");
+    return NDT_ERR_INVALID_ARGUMENT;
+}
+
+int ndt_tiles_commit(ndt_ctx* c, int32_t wait) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    tiles_settle(c, true);  // one rebuild at a time
+    uint64_t total = 0;
+    for (auto& t : c->tiles) total += t.n;
+    if (total == 0) {
+        set_error("no tiles to build a map from");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    cudaSetDevice(c->device);
+    int rc = dev_reserve(c->d_gather, total * 12);
+    if (rc) return rc;
+    uint64_t off = 0;
+    for (auto& t : c->tiles) {  // device-side gather of the resident tiles, in put order
+        cudaMemcpyAsync((char*)c->d_gather.p + off * 12, t.pts.p, t.n * 12,
+                        cudaMemcpyDeviceToDevice, c->bstream);
+        off += t.n;
+    }
+    c->build_state.store(1);
+    const ndt_config cfg = c->cfg;
+    c->builder = std::thread([c, total, cfg]() {
+        cudaSetDevice(c->device);
+        float ms = 0.f;
+        int r = build_map(c->map_b, c->bs_b, (const float*)c->d_gather.p, (size_t)total, cfg,
+                          (uint32_t*)c->d_status_b.p, c->bstream, &ms);
+        uint32_t st = 0;
+        if (!r) {
+            cudaMemcpyAsync(&st, c->d_status_b.p, 4, cudaMemcpyDeviceToHost, c->bstream);
+            r = cuda_fail(cudaStreamSynchronize(c->bstream), "tile rebuild");
+        }
+        if (!r && st) {
+            uint32_t zero = 0;
+            cudaMemcpyAsync(c->d_status_b.p, &zero, 4, cudaMemcpyHostToDevice, c->bstream);
+            cudaStreamSynchronize(c->bstream);
+            set_error("device reported status " + std::to_string(st) + " during a tile rebuild");
+            r = NDT_ERR_DEVICE;
+        }
+        c->build_rc = r;
+        c->build_ms_b = ms;
+        c->build_err = r ? std::string(ndt_last_error_string()) : std::string();
+        c->build_state.store(2);
+    });
+    if (wait) {
+        tiles_settle(c, true);
+        if (c->build_rc) {
+            set_error(c->build_err);
+            return c->build_rc;
+        }
+    }
+    return NDT_OK;
+}
+
+int ndt_tiles_status(ndt_ctx* c, uint64_t* num_tiles, uint64_t* num_points, int32_t* pending,
+                     int32_t* last_rc, float* build_ms) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    uint64_t n = 0;
+    for (auto& t : c->tiles) n += t.n;
+    if (num_tiles) *num_tiles = c->tiles.size();
+    if (num_points) *num_points = n;
+    if (pending) *pending = c->build_state.load() == 1 ? 1 : 0;
+    if (last_rc) *last_rc = c->build_state.load() == 1 ? 0 : c->build_rc;
+    if (build_ms) *build_ms = c->build_ms_b;
+    return NDT_OK;
+}
+
 int ndt_map_info_get(ndt_ctx* c, ndt_map_info* out) {
     if (!c || !out) return NDT_ERR_INVALID_ARGUMENT;
+    tiles_settle(c, false);
     if (!c->map.valid) {
         set_error("No target set. Call set_target() first.");
         return NDT_ERR_NO_TARGET;
@@ -475,6 +624,7 @@ int ndt_map_info_get(ndt_ctx* c, ndt_map_info* out) {
 int ndt_map_voxels(ndt_ctx* c, int32_t* coords, float* means, float* covs, float* icovs,
                    uint32_t* counts, uint64_t capacity) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    tiles_settle(c, false);
     if (!c->map.valid) {
         set_error("No target set. Call set_target() first.");
         return NDT_ERR_NO_TARGET;
@@ -719,6 +869,7 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
 }
 
 static int need_target(ndt_ctx* c) {
+    tiles_settle(c, false);
     if (!c->map.valid) {
         set_error("No target set. Call set_target() first.");
         return NDT_ERR_NO_TARGET;

@@ -159,6 +159,24 @@ void* ndt_ctx_stream(ndt_ctx* ctx);
 int ndt_set_target(ndt_ctx* ctx, const float* xyz, uint64_t num_points);
 int ndt_set_target_device(ndt_ctx* ctx, const float* d_xyz, uint64_t num_points);
 int ndt_map_info_get(ndt_ctx* ctx, ndt_map_info* out);
+
+/* Map tiles streamed in and out (the map module's tile loading and the dual matcher's
+ * rebuild-and-swap, src/cuda_ndt_matcher/src/map_module.rs:192-360,
+ * src/cuda_ndt_matcher/src/dual_ndt_manager.rs). Tiles (host points, uploaded once) stay in
+ * device memory under a caller-chosen id; ndt_tile_put adds or replaces one,
+ * ndt_tile_remove drops one. ndt_tiles_commit rebuilds the voxel map from the resident tiles
+ * (concatenated on the device in put order) into a standby map, on the context's second
+ * stream and a background host thread, while alignment calls keep using the active map.
+ * The first alignment (or map query) call after the rebuild has finished switches to the
+ * new map. wait = 1 waits for the rebuild and switches before returning. A failed rebuild
+ * leaves the active map in place; ndt_tiles_status reports it. */
+int ndt_tile_put(ndt_ctx* ctx, uint64_t tile_id, const float* xyz, uint64_t num_points);
+int ndt_tile_remove(ndt_ctx* ctx, uint64_t tile_id);
+int ndt_tiles_commit(ndt_ctx* ctx, int32_t wait);
+/* pending: 1 while a rebuild runs; last_rc: result of the last finished rebuild;
+ * build_ms: its device time. */
+int ndt_tiles_status(ndt_ctx* ctx, uint64_t* num_tiles, uint64_t* num_points, int32_t* pending,
+                     int32_t* last_rc, float* build_ms);
 /* VoxelGrid accessors (means_flat / inv_covariances_flat, voxel_grid/mod.rs:428-453):
  * valid voxels in ascending coordinate-Morton order; any output pointer may be NULL. */
 int ndt_map_voxels(ndt_ctx* ctx, int32_t* coords, float* means, float* covs, float* icovs,
