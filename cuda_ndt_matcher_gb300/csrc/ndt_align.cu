@@ -967,8 +967,8 @@ __device__ __forceinline__ void warp_sum_acc(const float* acc, int lane, double*
     }
 }
 
-// REGCAP: registers per thread the launch bounds allow (128: the default; 80: more resident
-// CTAs per SM at the price of a few spills; the autotuner picks)
+// REGCAP: registers per thread the launch bounds allow (128: the default; 80 and 64: more
+// resident CTAs per SM at the price of some spills; the autotuner picks)
 template <int THREADS, bool CPU_SEM, int REGCAP>
 __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_align(const AlignParams P) {
@@ -1157,10 +1157,16 @@ int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s) {
     }
     AlignParams q = p;
     q.cluster = K;
-    const bool dense = shape.regcap == 80;
+    const int R = shape.regcap;
     switch (shape.threads) {
-        case 128: return dense ? launch_t<128, 80>(q, K, s) : launch_t<128, 128>(q, K, s);
-        case 256: return dense ? launch_t<256, 80>(q, K, s) : launch_t<256, 128>(q, K, s);
+        case 128:
+            return R == 64 ? launch_t<128, 64>(q, K, s)
+                           : (R == 80 ? launch_t<128, 80>(q, K, s) : launch_t<128, 128>(q, K, s));
+        case 256:
+            return R == 48   ? launch_t<256, 48>(q, K, s)
+                   : R == 64 ? launch_t<256, 64>(q, K, s)
+                   : R == 80 ? launch_t<256, 80>(q, K, s)
+                             : launch_t<256, 128>(q, K, s);
         case 512: return launch_t<512, 128>(q, K, s);
         default:
             set_error("threads per CTA must be 128, 256 or 512");

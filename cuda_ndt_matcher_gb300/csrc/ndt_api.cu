@@ -305,7 +305,8 @@ static bool config_ok(const ndt_config& c) {
            c.outlier_ratio < 1.0 &&
            (c.semantics == NDT_SEMANTICS_GPU_GRAPH || c.semantics == NDT_SEMANTICS_CPU) &&
            (K == 0 || K == 1 || K == 2 || K == 4 || K == 8) &&
-           (T == 0 || T == 128 || T == 256 || T == 512) && (R == 0 || R == 80 || R == 128) &&
+           (T == 0 || T == 128 || T == 256 || T == 512) &&
+           (R == 0 || R == 48 || R == 64 || R == 80 || R == 128) &&
            (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
            (c.cuda_graph == 0 || c.cuda_graph == 1);
 }
@@ -1194,7 +1195,8 @@ int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const 
     std::vector<ndt_result> tmp(m);
     ndt_stats saved = c->stats;
     const int Ks[4] = {1, 2, 4, 8};
-    const int TC[5][2] = {{128, 128}, {128, 80}, {256, 128}, {256, 80}, {512, 128}};
+    const int TC[8][2] = {{128, 128}, {128, 80}, {128, 64}, {256, 128},
+                          {256, 80},  {256, 64}, {256, 48}, {512, 128}};
     LaunchShape best{0, 0, 128};
     double best_ms = 1e300;
     int tried = 0;

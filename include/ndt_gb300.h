@@ -74,7 +74,8 @@ typedef struct ndt_config {
     int32_t cluster_size;          /* CTAs per alignment; 0 = autotuned */
     int32_t threads_per_cta;       /* 0 = autotuned */
     int32_t hash_capacity_factor;  /* capacity = next pow2 >= factor * V; 2 = reference */
-    int32_t max_registers;         /* Newton-kernel register cap (80 or 128); 0 = autotuned */
+    int32_t max_registers;         /* Newton-kernel register cap (64, 80 or 128; 48 also at
+                                      256 threads; 128 only at 512); 0 = autotuned */
     int32_t cell_index;            /* NDT_CELL_INDEX_*: how kernels find a cell's voxel */
     int32_t cuda_graph;            /* 1: batches run as captured CUDA graphs (replayed while
                                       the batch shape repeats); 0: direct launches */
