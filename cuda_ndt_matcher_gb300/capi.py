@@ -53,7 +53,8 @@ class Config(C.Structure):
                 ("device", C.c_int32), ("cluster_size", C.c_int32),
                 ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
                 ("max_registers", C.c_int32), ("cell_index", C.c_int32),
-                ("cuda_graph", C.c_int32)]
+                ("cuda_graph", C.c_int32), ("use_line_search", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class Result(C.Structure):

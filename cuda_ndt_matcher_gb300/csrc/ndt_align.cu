@@ -35,6 +35,8 @@ constexpr int NACC = 34;          // f32 per-thread accumulators
 constexpr int NRED = NACC + 1;    // + correspondence count
 constexpr int MAX_WARPS = 16;
 constexpr int NFR = 52;           // per-iteration frame: R,t hi (12), R,t lo (12), A_k (27)
+// line-search candidate sums: score, G[3], G p^T [3x3], correspondence count (14 used)
+constexpr int LS_VALS = 16, LS_USED = 14;
 
 // accumulator offsets: score, G[3], G p^T [3x3], M[6 sym], (M J_k)[a][k] [3x3], J^T M J [6]
 constexpr int A_SC = 0, A_G = 1, A_GP = 4, A_M = 13, A_HTR = 19, A_HRR = 28;
@@ -69,6 +71,14 @@ struct AlignShared {
     double prev[3], prev2[3];
     int last_corr;
     int osc, max_osc;
+    // graph-path line search: direction, start pose, phi(0), phi'(0), candidate step lengths,
+    // poses, frames (every rank), A_k at each candidate pose, per-candidate sums
+    double ls_delta[6], ls_orig[6], ls_phi0, ls_dphi0, ls_best, ls_best_alpha;
+    int ls_more;  // the selection needs another round of candidates
+    double ls_alpha[LS_MAX], ls_pose[LS_MAX][6], ls_phi[LS_MAX], ls_dphi[LS_MAX];
+    double ls_Ad[LS_MAX][27], ls_trig[LS_MAX][16];
+    float ls_fr[LS_MAX][NFR];
+    double ls_part[LS_MAX][LS_VALS], ls_tot[LS_MAX][LS_VALS];
 };
 
 __device__ __forceinline__ int sym3(int a, int b) {
@@ -112,7 +122,8 @@ __device__ const uint32_t FRAME_TERMS[90] = {
 // sin/cos of roll, pitch, yaw; every lane then evaluates up to three of the 90 table
 // entries. Outputs: the f32 frame of the point work (R and t as hi/lo pairs, A_k in f32) and
 // A_k, B_kl in FP64 for assembling g and H at this pose. `small` applies the CPU path's
-// |angle| < 1e-5 rule (sin = 0, cos = 1) to A_k and B_kl (angular.rs), not to R.
+// |angle| < 1e-5 rule (sin = 0, cos = 1) to A_k and B_kl (angular.rs), not to R. With Bd
+// null the B_kl entries are skipped (a line-search candidate needs the gradient only).
 __device__ __noinline__ void make_frame_warp(const double* pose, bool small, float* fr,
                                              double* trig, double* Ad, double* Bd, int lane) {
     if (lane < 3) {
@@ -133,7 +144,8 @@ __device__ __noinline__ void make_frame_warp(const double* pose, bool small, flo
         trig[14] = 1.0;
     }
     __syncwarp();
-    for (int e = lane; e < 90; e += 32) {
+    const int nterms = Bd ? 90 : 36;
+    for (int e = lane; e < nterms; e += 32) {
         const uint32_t w = __ldg(FRAME_TERMS + e);
         const double* f = e < 9 ? trig : trig + 8;
         const double t0 = f[w & 7u] * f[(w >> 3) & 7u] * f[(w >> 6) & 7u];
@@ -561,13 +573,10 @@ __device__ __noinline__ void solve_warp(const double* H, const double* g, SolveS
 // ------------------------------------------------------------------------------------
 // Per-point work
 // ------------------------------------------------------------------------------------
-template <bool CPU_SEM>
-__device__ __forceinline__ void point_terms(const MapView& m, float px, float py, float pz,
-                                            const float* fr, int max_nb, float d1f, float d2f,
-                                            float* acc, int& ncorr, uint32_t* nbl,
-                                            int nbl_stride) {
-    const float pv[3] = {px, py, pz};
-    float qh[3], ql[3];
+// q = R p + t as an unevaluated sum qh + ql, from the frame's hi/lo R and t (TwoProd and
+// TwoSum), so q - mean keeps f32 precision however far the map lies from the origin
+__device__ __forceinline__ void transform_point(const float* fr, const float* pv, float* qh,
+                                                float* ql) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         float hi = fr[9 + i], lo = fr[21 + i];
@@ -586,37 +595,39 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
         ql[i] = lo - (s - hi);
         qh[i] = s;
     }
+}
+
+// Neighbour search of the point q = qh + ql: the 27 cells in the reference's order (dx outer,
+// dy, dz inner); the slots of the accepted voxels (centroid within one resolution, at most
+// max_nb) are listed in shared memory (nbl[k * nbl_stride]), so the search runs with all
+// lanes busy and the pair work runs once per listed voxel rather than once per cell.
+// Returns the number listed.
+__device__ __forceinline__ int search_point(const MapView& m, const float* qh, const float* ql,
+                                            int max_nb, uint32_t* nbl, int nbl_stride) {
     int32_t gc[3];
     cell_of_sum(m, qh, ql, gc);
-    // ---- search: the 27 cells in the reference's order (dx outer, dy, dz inner); the slots
-    // of the accepted voxels (centroid within one resolution, at most max_nb) are listed in
-    // shared memory, so the search runs with all lanes busy and the pair work below runs once
-    // per listed voxel rather than once per cell
     int cnt = 0;
     if (m.grid) {
-        // dense cell index: one 16-byte load per cell gives occupancy and centroid; the
-        // column's three cells (dz = -1, 0, 1) are adjacent entries
-        const uint32_t ux0 = (uint32_t)gc[0] - (uint32_t)m.min_cell[0];
-        const uint32_t uy0 = (uint32_t)gc[1] - (uint32_t)m.min_cell[1];
-        const uint32_t uz0 = (uint32_t)gc[2] - (uint32_t)m.min_cell[2];
+        // dense cell index: the cell's neighbourhood mask names the occupied cells among the
+        // 27, in search order; their {centroid, slot} entries are loaded NB_BATCH at a time
+        // (independent loads in flight together), then tested in order
+        constexpr int NB_BATCH = 4;
+        uint32_t corner;
+        uint32_t bits = nbhd_mask(m, gc, corner);
 #pragma unroll 1
-        for (int c9 = 0; c9 < 9; ++c9) {
-            if (cnt >= max_nb) break;
-            const uint32_t ux = ux0 + (uint32_t)(c9 / 3 - 1), uy = uy0 + (uint32_t)(c9 % 3 - 1);
-            if (!grid_in(m, ux, uy)) continue;
-            const float4* col = m.grid + ((size_t)ux * m.ext[1] + uy) * m.ext[2];
-            float4 e[3];
+        while (bits != 0u && cnt < max_nb) {
+            float4 e[NB_BATCH];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const uint32_t uz = uz0 + (uint32_t)(k - 1);
-                e[k] = uz < m.ext[2] ? __ldg(col + uz)
-                                     : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+            for (int k = 0; k < NB_BATCH; ++k) {
+                const uint32_t b = (uint32_t)(__ffs(bits) - 1);  // 0xFFFFFFFF when empty
+                e[k] = bits != 0u ? __ldg(m.grid + nbhd_index(m, corner, b))
+                                  : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+                bits &= bits - 1u;
             }
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                if (cnt >= max_nb) break;
+            for (int k = 0; k < NB_BATCH; ++k) {
                 const int32_t s = __float_as_int(e[k].w);
-                if (s < 0) continue;
+                if (s < 0 || cnt >= max_nb) break;
                 const float e0 = (qh[0] - e[k].x) + ql[0];
                 const float e1 = (qh[1] - e[k].y) + ql[1];
                 const float e2 = (qh[2] - e[k].z) + ql[2];
@@ -667,6 +678,18 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
         }
     }
     }
+    return cnt;
+}
+
+template <bool CPU_SEM>
+__device__ __forceinline__ void point_terms(const MapView& m, float px, float py, float pz,
+                                            const float* fr, int max_nb, float d1f, float d2f,
+                                            float* acc, int& ncorr, uint32_t* nbl,
+                                            int nbl_stride) {
+    const float pv[3] = {px, py, pz};
+    float qh[3], ql[3];
+    transform_point(fr, pv, qh, ql);
+    const int cnt = search_point(m, qh, ql, max_nb, nbl, nbl_stride);
     if (cnt == 0) return;
     // ---- pairs: S, G, M aggregated over the listed voxels
     float S = 0.f, G0 = 0.f, G1 = 0.f, G2 = 0.f;
@@ -743,6 +766,50 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
         for (int l = k; l < 3; ++l, ++kl)
             acc[A_HRR + kl] = fmaf(J[k][0], MJ[l][0],
                                    fmaf(J[k][1], MJ[l][1], fmaf(J[k][2], MJ[l][2], acc[A_HRR + kl])));
+}
+
+// Line-search terms of one point at a candidate pose (graph semantics; the candidate pass of
+// ndt_graph_linesearch_kernel, ndt_graph_kernels.cu:473-570): score and gradient only, as the
+// accumulators S (a[0]), G (a[1..3]) and G p^T (a[4..12]) of point_terms, same arithmetic.
+__device__ __forceinline__ void point_terms_ls(const MapView& m, float px, float py, float pz,
+                                               const float* fr, int max_nb, float d1f, float d2f,
+                                               float* a, int& ncorr, uint32_t* nbl,
+                                               int nbl_stride) {
+    const float pv[3] = {px, py, pz};
+    float qh[3], ql[3];
+    transform_point(fr, pv, qh, ql);
+    const int cnt = search_point(m, qh, ql, max_nb, nbl, nbl_stride);
+    if (cnt == 0) return;
+    float S = 0.f, G[3] = {0.f, 0.f, 0.f};
+    const float d1d2 = d1f * d2f;
+#pragma unroll 1
+    for (int j = 0; j < cnt; ++j) {
+        const uint32_t s = nbl[j * nbl_stride];
+        const uint4 v = __ldg(m.slots + s);
+        const float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
+        const float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
+        const float x0 = (qh[0] - __uint_as_float(v.y)) + ql[0];
+        const float x1 = (qh[1] - __uint_as_float(v.z)) + ql[1];
+        const float x2 = (qh[2] - __uint_as_float(v.w)) + ql[2];
+        const float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
+        const float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
+        const float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
+        const float sq = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
+        const float e = expf(-0.5f * d2f * sq);
+        const float w = d1d2 * e;
+        S = fmaf(-d1f, e, S);
+        G[0] = fmaf(w, c0, G[0]);
+        G[1] = fmaf(w, c1, G[1]);
+        G[2] = fmaf(w, c2, G[2]);
+    }
+    ncorr += cnt;
+    a[0] += S;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        a[1 + i] += G[i];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) a[4 + 3 * i + b] = fmaf(G[i], pv[b], a[4 + 3 * i + b]);
+    }
 }
 
 // g (6) and H (6x6) in FP64 from the reduced accumulators; lanes of one warp share the work.
@@ -967,6 +1034,120 @@ __device__ __forceinline__ void warp_sum_acc(const float* acc, int lane, double*
     }
 }
 
+// Warp sums of the first `nv` (<= 16) of 16 f32 values, compensated, written as FP64 to
+// out[0..nv): a butterfly over lane distance 16, then recursive halving as in warp_sum_acc,
+// after which lane l holds the sum of value l & 15.
+__device__ __forceinline__ void warp_sum16(const float* v, int lane, int nv, double* out) {
+    float s[16], c[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) two_sum(v[j], __shfl_xor_sync(0xffffffffu, v[j], 16), s[j], c[j]);
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < o; ++j) {
+            const float ss = up ? s[j] : s[j + o], cs = up ? c[j] : c[j + o];
+            const float sk = up ? s[j + o] : s[j], ck = up ? c[j + o] : c[j];
+            const float sr = __shfl_xor_sync(0xffffffffu, ss, o);
+            const float cr = __shfl_xor_sync(0xffffffffu, cs, o);
+            float e;
+            two_sum(sk, sr, s[j], e);
+            c[j] = ck + cr + e;
+        }
+    }
+    if (lane < nv) out[lane] = (double)s[0] + (double)c[0];
+}
+
+// Line-search set-up after the Newton solve (graph path; ndt_graph_solve_kernel,
+// ndt_graph_kernels.cu:388-430): the direction is the raw solve (or -1e-4 g when it failed),
+// reversed when g.delta <= 0; phi(0) = score, phi'(0) = g.delta; candidate step lengths 1,
+// 0.618, 0.618^2, ... formed as an f32 product as the reference forms them; their poses.
+// Lane 0 of the controller warp.
+__device__ __noinline__ void ls_prepare(const AlignParams& P, AlignShared& sh) {
+    double x[6];
+    for (int i = 0; i < 6; ++i) x[i] = sh.solve.ok ? sh.solve.x[i] : -sh.g[i] * 1e-4;
+    double dphi = dot6(sh.g, x);
+    if (dphi <= 0.0) {
+        for (int i = 0; i < 6; ++i) x[i] = -x[i];
+        dphi = -dphi;
+    }
+    for (int i = 0; i < 6; ++i) {
+        sh.ls_delta[i] = x[i];
+        sh.ls_orig[i] = sh.pose[i];
+    }
+    sh.ls_phi0 = sh.tot[A_SC];
+    sh.ls_dphi0 = dphi;
+    sh.ls_best = sh.ls_phi0;  // no candidate above phi(0) yet: no move
+    sh.ls_best_alpha = 0.0;
+    float a = 1.0f;
+    for (int k = 0; k < P.ls_cands; ++k, a *= 0.618f) {
+        sh.ls_alpha[k] = (double)a;
+        for (int i = 0; i < 6; ++i) sh.ls_pose[k][i] = sh.pose[i] + (double)a * x[i];
+    }
+}
+
+// phi(alpha_k) and phi'(alpha_k) = g(alpha_k).delta of candidates c_lo <= k < c_hi from the
+// cluster sums (lane k, as finalize_gH forms the gradient)
+__device__ __forceinline__ void ls_candidates_warp(const AlignParams& P, AlignShared& sh,
+                                                   int lane, int c_lo, int c_hi) {
+    if (lane >= c_lo && lane < c_hi) {
+        const double* t = sh.ls_tot[lane];
+        const double(*A)[9] = reinterpret_cast<const double(*)[9]>(sh.ls_Ad[lane]);
+        double g[6];
+        for (int i = 0; i < 3; ++i) g[i] = t[1 + i];
+        for (int r = 0; r < 3; ++r) {
+            double v = 0.0;
+            for (int q = 0; q < 9; ++q) v += A[r][q] * t[4 + q];
+            g[3 + r] = v;
+        }
+        sh.ls_phi[lane] = t[0];
+        sh.ls_dphi[lane] = dot6(g, sh.ls_delta);
+    }
+}
+
+// Candidate selection and step (ndt_graph_update_kernel, ndt_graph_kernels.cu:626-710): the
+// first candidate meeting the strong Wolfe conditions, else the best score above phi(0), else
+// no move; step length alpha |delta| (no clamp); then the oscillation and convergence rules
+// of the graph path. Applied to candidates c_lo <= k < c_hi on top of the earlier rounds'
+// running best. Lane 0 of the controller warp; returns -1 when the round found no Wolfe
+// candidate and candidates remain, else 1 when the alignment is finished, 0 when it goes on.
+__device__ __noinline__ int ls_decide(const AlignParams& P, AlignShared& sh, AlignOut& o, int it,
+                                      int ncorr, int c_lo, int c_hi) {
+    const double phi0 = sh.ls_phi0, dphi0 = sh.ls_dphi0;
+    double best_alpha = sh.ls_best_alpha, best = sh.ls_best;
+    bool wolfe = false;
+    for (int k = c_lo; k < c_hi; ++k) {
+        const double phi = sh.ls_phi[k], a = sh.ls_alpha[k];
+        const bool armijo = phi >= phi0 + P.ls_mu * a * dphi0;
+        const bool curvature = fabs(sh.ls_dphi[k]) <= P.ls_nu * fabs(dphi0);
+        if (armijo && curvature) {
+            best_alpha = a;
+            wolfe = true;
+            break;
+        }
+        if (phi > best) {
+            best = phi;
+            best_alpha = a;
+        }
+    }
+    if (!wolfe && c_hi < P.ls_cands) {
+        sh.ls_best = best;
+        sh.ls_best_alpha = best_alpha;
+        return -1;
+    }
+    for (int i = 0; i < 6; ++i) sh.pose[i] = sh.ls_orig[i] + best_alpha * sh.ls_delta[i];
+    const double step = best_alpha * sqrt(dot6(sh.ls_delta, sh.ls_delta));
+    osc_update(sh, sh.pose, it);
+    const int conv = step < P.eps;
+    if (conv || it + 1 >= P.max_iter) {
+        const int status = ncorr == 0 ? NDT_STATUS_NO_CORRESPONDENCES
+                                      : (conv ? NDT_STATUS_CONVERGED : NDT_STATUS_MAX_ITERATIONS);
+        write_out(o, sh.pose, phi0, sh.H, it + 1, conv && ncorr > 0, ncorr, sh.max_osc, status);
+        return 1;
+    }
+    return 0;
+}
+
 // REGCAP: registers per thread the launch bounds allow (128: the default; 80 and 64: more
 // resident CTAs per SM at the price of some spills; the autotuner picks)
 template <int THREADS, bool CPU_SEM, int REGCAP>
@@ -985,6 +1166,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     const MapView& m = P.map;
     const float* pts = P.pts + 3 * job.offset;
     const uint32_t n = job.n;
+    // graph path with line search: every iteration adds a candidate pass (two more barriers)
+    const bool line_search = !CPU_SEM && P.ls_cands > 0;
 
     if (tid == 0) {
         for (int i = 0; i < 6; ++i) {
@@ -1075,7 +1258,11 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     point_iters += n;
                     corr_total += (uint64_t)ncorr;
                     AlignOut& o = P.out[jid];
-                    int done = control_step<CPU_SEM>(P, sh, job, o, it, sh.tot[A_SC], ncorr);
+                    int done = 0;
+                    if (line_search)
+                        ls_prepare(P, sh);  // the step is taken after the candidate pass
+                    else
+                        done = control_step<CPU_SEM>(P, sh, job, o, it, sh.tot[A_SC], ncorr);
                     if (done) {
                         o.point_iters = point_iters;
                         o.corr_total = corr_total;
@@ -1083,23 +1270,36 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     sh.done = done;
                 }
                 __syncwarp();
-                make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                if (!line_search) {
+                    make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                    if (lane > 0 && lane < K) {
+                        AlignShared* rs = cluster.map_shared_rank(&sh, lane);
+                        for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
+                        for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
+                        rs->done = sh.done;
+                    }
+                }
                 if (t) {  // controller sub-phase cycles: assembly, solve, step + next frame
                     t[44] = (double)(cb - ca);
                     t[45] = (double)(cc - cb);
                     t[46] = (double)(clock64() - cc);
                     t[47] = sh.solve.sweeps;
                 }
-                if (lane > 0 && lane < K) {
-                    AlignShared* rs = cluster.map_shared_rank(&sh, lane);
-                    for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
-                    for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
-                    rs->done = sh.done;
+            }
+            if (line_search) {  // candidate frames, one warp per candidate, to every rank
+                __syncthreads();
+                for (int c = warp; c < P.ls_cands; c += NW) {
+                    make_frame_warp(sh.ls_pose[c], false, sh.ls_fr[c], sh.ls_trig[c],
+                                    sh.ls_Ad[c], nullptr, lane);
+                    if (lane > 0 && lane < K) {
+                        AlignShared* rs = cluster.map_shared_rank(&sh, lane);
+                        for (int i = 0; i < NFR; ++i) rs->ls_fr[c][i] = sh.ls_fr[c][i];
+                    }
                 }
             }
         }
         unsigned long long t3 = clock64();
-        cluster.sync();  // next pose (or done) visible in every CTA
+        cluster.sync();  // next pose (or done, or the candidate frames) visible in every CTA
         unsigned long long t4 = clock64();
         if (rank == 0 && tid == 0) {
             sh.cyc[0] += t1 - t0;
@@ -1108,6 +1308,95 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             sh.cyc[3] += t4 - t3;
         }
         t0 = t4;
+        if (sh.done) break;
+        // Line search: candidates are scored in rounds (step lengths [0, 1), [1, 3), [3, 8));
+        // after each round rank 0 applies the selection rule to the candidates scored so far,
+        // in order, and stops at the first that meets the strong Wolfe conditions. The rule
+        // never looks past that candidate, so the outcome equals scoring all 8 at once, while
+        // the common full step (alpha = 1 accepted) costs one candidate pass instead of 8.
+        for (int round = 0; line_search; ++round) {
+            const int c_lo = round == 0 ? 0 : (round == 1 ? 1 : 3);
+            const int c_hi = min(round == 0 ? 1 : (round == 1 ? 3 : LS_MAX), P.ls_cands);
+            // candidate pass: score and gradient of each candidate pose of the round over this
+            // rank's points, one candidate after another; FP64 warp sums of each candidate
+            // kept in shared memory, summed over the CTA, then over the cluster by rank 0
+            double* lsw = reinterpret_cast<double*>(nbl_smem + (size_t)P.max_nb * THREADS);
+            for (int c = c_lo; c < c_hi; ++c) {
+                float a[LS_VALS];
+#pragma unroll
+                for (int v = 0; v < LS_VALS; ++v) a[v] = 0.f;
+                int lc = 0;
+                for (uint32_t i = (uint32_t)rank * THREADS + tid; i < n;
+                     i += (uint32_t)K * THREADS) {
+                    float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
+                          pz = __ldg(pts + 3 * (size_t)i + 2);
+                    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
+                    point_terms_ls(m, px, py, pz, sh.ls_fr[c], P.max_nb, P.d1f, P.d2f, a, lc,
+                                   nbl_smem + tid, THREADS);
+                }
+                double* wout = lsw + ((size_t)warp * LS_MAX + c) * LS_VALS;
+                warp_sum16(a, lane, LS_USED - 1, wout);
+                lc = __reduce_add_sync(0xffffffffu, lc);
+                if (lane == 0) wout[LS_USED - 1] = (double)lc;
+            }
+            __syncthreads();
+            const int nk = (c_hi - c_lo) * LS_USED;
+            for (int k = tid; k < nk; k += THREADS) {
+                const int c = c_lo + k / LS_USED, v = k % LS_USED;
+                double s = 0.0;
+                for (int w = 0; w < NW; ++w) s += lsw[((size_t)w * LS_MAX + c) * LS_VALS + v];
+                sh.ls_part[c][v] = s;
+            }
+            const unsigned long long t5 = clock64();
+            cluster.sync();  // candidate partials of every CTA are ready
+            if (rank == 0) {
+                for (int k = tid; k < nk; k += THREADS) {
+                    const int c = c_lo + k / LS_USED, v = k % LS_USED;
+                    double w8[8];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r)
+                        w8[r] = r < K ? cluster.map_shared_rank(&sh.ls_part[c][v], r)[0] : 0.0;
+                    sh.ls_tot[c][v] =
+                        ((w8[0] + w8[1]) + (w8[2] + w8[3])) + ((w8[4] + w8[5]) + (w8[6] + w8[7]));
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    ls_candidates_warp(P, sh, lane, c_lo, c_hi);
+                    __syncwarp();
+                    if (lane == 0) {
+                        AlignOut& o = P.out[jid];
+                        const int r = ls_decide(P, sh, o, it, (int)sh.tot[NACC], c_lo, c_hi);
+                        if (r == 1) {
+                            o.point_iters = point_iters;
+                            o.corr_total = corr_total;
+                        }
+                        sh.ls_more = r < 0;
+                        sh.done = r == 1;
+                    }
+                    __syncwarp();
+                    if (!sh.ls_more) make_frame_warp(sh.pose, false, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                    if (lane > 0 && lane < K) {
+                        AlignShared* rs = cluster.map_shared_rank(&sh, lane);
+                        if (!sh.ls_more) {
+                            for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
+                            for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
+                        }
+                        rs->done = sh.done;
+                        rs->ls_more = sh.ls_more;
+                    }
+                }
+            }
+            const unsigned long long t6 = clock64();
+            cluster.sync();  // another round, or the stepped pose (or done), in every CTA
+            const unsigned long long t7 = clock64();
+            if (rank == 0 && tid == 0) {  // candidate pass as point work, selection as control
+                sh.cyc[0] += t5 - t4;
+                sh.cyc[2] += t6 - t5;
+                sh.cyc[3] += t7 - t6;
+            }
+            t0 = t4 = t7;
+            if (!sh.ls_more) break;
+        }
         if (sh.done) break;
     }
     if (rank == 0 && tid == 0) {
@@ -1134,7 +1423,12 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.num_jobs * K, 1, 1);
     cfg.blockDim = dim3(T, 1, 1);
-    cfg.dynamicSmemBytes = (size_t)T * p.max_nb * sizeof(uint32_t);
+    // [max_nb][T] neighbour lists, then (line search) [T/32][LS_MAX][LS_VALS] FP64 warp sums;
+    // T * max_nb * 4 bytes is a multiple of 8 (T is)
+    cfg.dynamicSmemBytes = (size_t)T * p.max_nb * sizeof(uint32_t) +
+                           (p.ls_cands > 0 && p.semantics != NDT_SEMANTICS_CPU
+                                ? (size_t)(T / 32) * LS_MAX * LS_VALS * sizeof(double)
+                                : 0);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -308,7 +308,9 @@ static bool config_ok(const ndt_config& c) {
            (T == 0 || T == 128 || T == 256 || T == 512) &&
            (R == 0 || R == 48 || R == 64 || R == 80 || R == 128) &&
            (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
-           (c.cuda_graph == 0 || c.cuda_graph == 1);
+           (c.cuda_graph == 0 || c.cuda_graph == 1) &&
+           (c.use_line_search == 0 ||
+            (c.use_line_search == 1 && c.semantics == NDT_SEMANTICS_GPU_GRAPH));
 }
 
 extern "C" {
@@ -373,6 +375,7 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     if (c->builder.joinable()) c->builder.join();
     for (auto& t : c->tiles) dev_free(t.pts);
     for (DevBuf* b : {&c->map_b.slots, &c->map_b.slot_icov, &c->map_b.slot_vidx, &c->map_b.grid,
+                      &c->map_b.nmask,
                       &c->map_b.vox_coord, &c->map_b.vox_mean, &c->map_b.vox_cov,
                       &c->map_b.vox_icov, &c->map_b.vox_count, &c->bs_b.keys_a, &c->bs_b.keys_b,
                       &c->bs_b.vals_a, &c->bs_b.vals_b, &c->bs_b.tmp, &c->bs_b.seg_ids,
@@ -382,6 +385,7 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     if (c->bstream) cudaStreamDestroy(c->bstream);
     drop_graphs(c);
     for (DevBuf* b : {&c->map.slots, &c->map.slot_icov, &c->map.slot_vidx, &c->map.grid,
+                      &c->map.nmask,
                       &c->map.vox_coord,
                       &c->map.vox_mean, &c->map.vox_cov, &c->map.vox_icov, &c->map.vox_count,
                       &c->bs.keys_a, &c->bs.keys_b, &c->bs.vals_a, &c->bs.vals_b, &c->bs.tmp,
@@ -744,6 +748,9 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         p.eps = (double)sqrtf(ef * ef);
     }
     p.status = (uint32_t*)c->d_status.p;
+    p.ls_cands = (c->cfg.use_line_search && !cpu) ? LS_MAX : 0;
+    p.ls_mu = LS_MU;
+    p.ls_nu = LS_NU;
     p.trace = nullptr;
     if (c->trace) {
         size_t tb = (size_t)nj * p.max_iter * TRACE_REC * sizeof(double);

@@ -45,12 +45,38 @@ struct MapView {
     // slot -1 for an empty cell
     const float4* grid;
     uint32_t ext[3];
+    // neighbourhood masks over the dense index's box grown by one cell on every side:
+    // nmask[((ux + 1) * (ext[1] + 2) + uy + 1) * (ext[2] + 2) + uz + 1] has bit
+    // 9 (dx + 1) + 3 (dy + 1) + (dz + 1) set when local cell (ux + dx, uy + dy, uz + dz) holds
+    // a voxel; ascending bits are the reference's 27-cell search order (dx outer, dz inner)
+    const uint32_t* nmask;
 };
 
 // Column (ux, uy) of local cells lies inside the dense index. Local coordinates are unsigned
 // (cell - min cell, wrapped), so a cell below the box reads as a huge value.
 __device__ __forceinline__ bool grid_in(const MapView& m, uint32_t ux, uint32_t uy) {
     return ux < m.ext[0] && uy < m.ext[1];
+}
+
+// Occupied neighbours of cell gc (dense index only): the neighbourhood mask (0 when gc lies
+// more than one cell outside the box), and in `corner` the dense-index position of cell
+// gc - (1, 1, 1), from which nbhd_index finds each neighbour. Positions are computed modulo
+// 2^32: the corner of a cell in the outer ring lies outside the box, but every neighbour
+// whose bit is set lies inside it, so its position comes out exact.
+__device__ __forceinline__ uint32_t nbhd_mask(const MapView& m, const int32_t* gc,
+                                              uint32_t& corner) {
+    const uint32_t mx = (uint32_t)gc[0] - (uint32_t)m.min_cell[0] + 1u;
+    const uint32_t my = (uint32_t)gc[1] - (uint32_t)m.min_cell[1] + 1u;
+    const uint32_t mz = (uint32_t)gc[2] - (uint32_t)m.min_cell[2] + 1u;
+    const uint32_t E1 = m.ext[1] + 2u, E2 = m.ext[2] + 2u;
+    corner = ((mx - 2u) * m.ext[1] + (my - 2u)) * m.ext[2] + (mz - 2u);
+    if (mx >= m.ext[0] + 2u || my >= E1 || mz >= E2) return 0u;
+    return __ldg(m.nmask + ((size_t)mx * E1 + my) * E2 + mz);
+}
+
+// Dense-index position of neighbour b (bit b of the mask) of the cell whose corner is given.
+__device__ __forceinline__ uint32_t nbhd_index(const MapView& m, uint32_t corner, uint32_t b) {
+    return corner + (b / 9u) * (m.ext[1] * m.ext[2]) + (b / 3u % 3u) * m.ext[2] + b % 3u;
 }
 
 // Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).

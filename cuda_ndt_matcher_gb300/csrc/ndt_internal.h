@@ -32,7 +32,7 @@ int cuda_fail(cudaError_t e, const char* what);
 
 // Device-resident voxel map.
 struct Map {
-    DevBuf slots, slot_icov, slot_vidx, grid;
+    DevBuf slots, slot_icov, slot_vidx, grid, nmask;
     DevBuf vox_coord, vox_mean, vox_cov, vox_icov, vox_count;
     MapView view{};
     ndt_map_info info{};
@@ -112,7 +112,16 @@ struct AlignParams {
     double step_size;
     double eps;
     uint32_t* status;
+    int32_t ls_cands;      // graph-path line search: candidates per iteration (0: off)
+    double ls_mu, ls_nu;   // strong Wolfe constants
 };
+
+// Line search of the graph path: at most 8 candidates (GRAPH_MAX_LS_CANDIDATES,
+// ndt_graph_common.cuh:18); Armijo and curvature constants of PipelineV2Config::default
+// (full_gpu_pipeline_v2.rs:101-113)
+constexpr int LS_MAX = 8;
+constexpr double LS_MU = 1e-4;
+constexpr double LS_NU = 0.9;
 
 struct LaunchShape {
     int cluster;

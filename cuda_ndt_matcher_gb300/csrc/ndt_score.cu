@@ -110,30 +110,43 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
         const int32_t gx = gc[0], gy = gc[1], gz = gc[2];
         float best = -INFINITY, sum = 0.f;
         int cnt = 0;
-#pragma unroll 1
-        for (int c = 0; c < 27; ++c) {
-            int dx, dy, dz;
-            offset27(c, dx, dy, dz);
-            float mx, my, mz;
-            const int32_t s = find_cell(m, (int32_t)((uint32_t)gx + (uint32_t)dx),
-                                        (int32_t)((uint32_t)gy + (uint32_t)dy),
-                                        (int32_t)((uint32_t)gz + (uint32_t)dz), &mx, &my, &mz);
-            if (s < 0) continue;
-            {
-                float e0 = (qx - mx) + ql[0], e1 = (qy - my) + ql[1], e2 = (qz - mz) + ql[2];
-                if (fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2) continue;
-            }
-            float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
-            float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
-            float x0 = (qx - mx) + ql[0], x1 = (qy - my) + ql[1], x2 = (qz - mz) + ql[2];
-            float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
-            float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
-            float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
-            float md = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
-            float s0 = -d1 * expf(-d2 * md * 0.5f);
+        // one voxel with centroid (mx, my, mz) in slot s: radius test, then its score term
+        auto visit = [&](int32_t s, float mx, float my, float mz) {
+            const float x0 = (qx - mx) + ql[0], x1 = (qy - my) + ql[1], x2 = (qz - mz) + ql[2];
+            if (fmaf(x0, x0, fmaf(x1, x1, x2 * x2)) > m.r2) return;
+            const float4 ca = __ldg(m.slot_icov + 2 * (size_t)s);
+            const float4 cb = __ldg(m.slot_icov + 2 * (size_t)s + 1);
+            const float c0 = fmaf(ca.x, x0, fmaf(ca.y, x1, ca.z * x2));
+            const float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
+            const float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
+            const float md = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
+            const float s0 = -d1 * expf(-d2 * md * 0.5f);
             best = fmaxf(best, s0);
             sum += s0;
             cnt++;
+        };
+        if (m.grid) {  // occupied neighbours only, in the same order, from the mask
+            uint32_t corner;
+            uint32_t bits = nbhd_mask(m, gc, corner);
+#pragma unroll 1
+            while (bits != 0u) {
+                const uint32_t b = (uint32_t)(__ffs(bits) - 1);
+                bits &= bits - 1u;
+                const float4 e = __ldg(m.grid + nbhd_index(m, corner, b));
+                visit(__float_as_int(e.w), e.x, e.y, e.z);
+            }
+        } else {
+#pragma unroll 1
+            for (int c = 0; c < 27; ++c) {
+                int dx, dy, dz;
+                offset27(c, dx, dy, dz);
+                float mx, my, mz;
+                const int32_t s = find_cell(m, (int32_t)((uint32_t)gx + (uint32_t)dx),
+                                            (int32_t)((uint32_t)gy + (uint32_t)dy),
+                                            (int32_t)((uint32_t)gz + (uint32_t)dz), &mx, &my,
+                                            &mz);
+                if (s >= 0) visit(s, mx, my, mz);
+            }
         }
         if (cnt) {
             nv += (double)best;

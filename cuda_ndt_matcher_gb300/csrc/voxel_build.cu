@@ -659,6 +659,30 @@ __global__ void k_grid_fill(MapView m, float4* __restrict__ grid) {
                             __int_as_float((int32_t)s));
 }
 
+// Neighbourhood masks (layout in MapView::nmask): one thread per cell of the box grown by
+// one cell on every side gathers the occupancy of its 27 neighbours from the dense index.
+__global__ void k_grid_mask(const float4* __restrict__ grid, uint32_t e0, uint32_t e1,
+                            uint32_t e2, uint32_t* __restrict__ nmask) {
+    const uint32_t E1 = e1 + 2u, E2 = e2 + 2u;
+    const uint64_t total = (uint64_t)(e0 + 2u) * E1 * E2;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t mz = (uint32_t)(i % E2);
+        const uint32_t my = (uint32_t)((i / E2) % E1);
+        const uint32_t mx = (uint32_t)(i / ((uint64_t)E2 * E1));
+        uint32_t bits = 0u;
+#pragma unroll 1
+        for (uint32_t b = 0; b < 27u; ++b) {
+            // neighbour (local) = grown-box cell - 1 + (offset - 1)
+            const uint32_t nx = mx + b / 9u - 2u, ny = my + b / 3u % 3u - 2u, nz = mz + b % 3u - 2u;
+            if (nx >= e0 || ny >= e1 || nz >= e2) continue;  // wrapped negatives are huge
+            const float w = __ldg(&grid[((size_t)nx * e1 + ny) * e2 + nz].w);
+            if (__float_as_int(w) >= 0) bits |= 1u << b;
+        }
+        nmask[i] = bits;
+    }
+}
+
 static uint32_t bit_width(uint32_t x) {
     uint32_t b = 0;
     while (b < 32 && (x >> b)) ++b;
@@ -792,11 +816,19 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
         cells *= v.ext[a];
     }
     v.grid = nullptr;
+    v.nmask = nullptr;
+    const uint64_t mcells = (uint64_t)(v.ext[0] + 2) * (v.ext[1] + 2) * (v.ext[2] + 2);
     if (cfg.cell_index == NDT_CELL_INDEX_AUTO && cells * 16 <= DENSE_GRID_MAX_BYTES) {
-        if ((rc = dev_reserve(map.grid, (size_t)cells * 16))) return rc;
+        if ((rc = dev_reserve(map.grid, (size_t)cells * 16)) ||
+            (rc = dev_reserve(map.nmask, (size_t)mcells * 4)))
+            return rc;
         cudaMemsetAsync(map.grid.p, 0xFF, (size_t)cells * 16, s);
         k_grid_fill<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (float4*)map.grid.p);
+        const unsigned mblocks = (unsigned)std::min<uint64_t>((mcells + 255) / 256, 152ull * 64);
+        k_grid_mask<<<mblocks, 256, 0, s>>>((const float4*)map.grid.p, v.ext[0], v.ext[1],
+                                            v.ext[2], (uint32_t*)map.nmask.p);
         v.grid = (const float4*)map.grid.p;
+        v.nmask = (const uint32_t*)map.nmask.p;
     }
     cudaEventRecord(e1, s);
     uint32_t hprobe = 0;
@@ -821,7 +853,8 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
         info.max_coord[a] = hmm[3 + a];
     }
     info.build_ms = ms;
-    info.dense_grid_mib = v.grid ? (float)((double)cells * 16.0 / (1024.0 * 1024.0)) : 0.f;
+    info.dense_grid_mib =
+        v.grid ? (float)(((double)cells * 16.0 + (double)mcells * 4.0) / (1024.0 * 1024.0)) : 0.f;
     map.valid = true;
     return 0;
 }

@@ -179,17 +179,18 @@ class NdtScanMatcher:
         return NdtScanMatcherBuilder()
 
     def _init(self, config):
-        if config.use_line_search or config.regularization_enabled:
-            raise NotImplementedError(
-                "line search and GNSS regularisation are outside this library's scope")
+        if config.regularization_enabled:
+            raise NotImplementedError("GNSS regularisation is outside this library's scope")
         self.config = config
         self._ctx = capi.Context(
             resolution=config.resolution, max_iterations=config.max_iterations,
             trans_epsilon=config.trans_epsilon, step_size=config.step_size,
             outlier_ratio=config.outlier_ratio,
             min_points_per_voxel=config.min_points_per_voxel,
-            semantics=self._semantics(config.use_gpu), cluster_size=config.cluster_size,
-            threads_per_cta=config.threads_per_cta, device=config.device)
+            semantics=(capi.SEMANTICS_GPU_GRAPH if config.use_line_search
+                       else self._semantics(config.use_gpu)),
+            cluster_size=config.cluster_size, threads_per_cta=config.threads_per_cta,
+            device=config.device, use_line_search=int(config.use_line_search))
         self._has_target = False
 
     @staticmethod
@@ -197,7 +198,13 @@ class NdtScanMatcher:
         return capi.SEMANTICS_GPU_GRAPH if use_gpu else capi.SEMANTICS_CPU
 
     def _with(self, use_gpu):
+        """Selects the path: the graph kernels (align_gpu) or NdtOptimizer::align. With
+        use_line_search the graph path runs its parallel line search; the CPU path's
+        More-Thuente search (solver.rs:268-280) is not built, so that combination raises."""
         want = self._semantics(use_gpu)
+        if want == capi.SEMANTICS_CPU and self.config.use_line_search:
+            raise NotImplementedError(
+                "the CPU path's More-Thuente line search is not built; use the GPU path")
         if self._ctx.cfg.semantics != want:
             self._ctx.configure(semantics=want)
 

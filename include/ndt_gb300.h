@@ -79,6 +79,13 @@ typedef struct ndt_config {
     int32_t cell_index;            /* NDT_CELL_INDEX_*: how kernels find a cell's voxel */
     int32_t cuda_graph;            /* 1: batches run as captured CUDA graphs (replayed while
                                       the batch shape repeats); 0: direct launches */
+    int32_t use_line_search;       /* NdtScanMatcherConfig::use_line_search (ndt.rs:69, default
+                                      false): the graph path's parallel line search, 8 step
+                                      candidates 0.618^k under the strong Wolfe conditions
+                                      (ndt_graph_kernels.cu:388-430,473-570,626-710) instead
+                                      of the clamped step; graph semantics only (the CPU
+                                      path's More-Thuente search is not built) */
+    int32_t reserved;              /* 0 */
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */

@@ -1143,6 +1143,41 @@ void or_align_gpu_sem_trace(const or_grid* g, const float* src, size_t n,
     align_gpu_sem_impl(g, src, n, pose_in, cfg, out, trace);
 }
 
+/* Parallel line search of the graph path (ndt_graph_kernels.cu:388-430 set-up,
+ * :473-570 candidate scores and gradients, :626-710 selection): candidates alpha_k =
+ * 0.618^k (an f32 product chain) along the reversed-if-needed Newton direction dl, each
+ * scored with the graph neighbour rule at pose + alpha_k dl; the first candidate meeting the
+ * strong Wolfe conditions (phi_k >= phi0 + mu alpha_k dphi0 and |dphi_k| <= nu |dphi0|) wins,
+ * else the highest phi_k above phi0, else alpha = 0. No step clamp applies. Updates pose and
+ * returns the step length alpha |dl|. */
+static double line_search_gpu_sem(const or_grid* g, const float* src, size_t n, double* pose,
+                                  const double* dl, double phi0, double dphi0, double dn,
+                                  double d1, double d2, const or_config* cfg) {
+    int nc = cfg->ls_candidates < 8 ? cfg->ls_candidates : 8;
+    double best_alpha = 0.0, best = phi0;
+    float a32 = 1.0f;
+    for (int k = 0; k < nc; ++k, a32 *= 0.618f) {
+        double a = (double)a32, trial[6], sc, gr[6], H[36];
+        int32_t ncorr;
+        for (int i = 0; i < 6; ++i) trial[i] = pose[i] + a * dl[i];
+        or_derivatives_gpu_sem(g, src, n, trial, d1, d2, cfg->max_neighbors, &sc, gr, H, &ncorr);
+        double dphi = 0.0;
+        for (int i = 0; i < 6; ++i) dphi += gr[i] * dl[i];
+        int armijo = sc >= phi0 + cfg->ls_mu * a * dphi0;
+        int curvature = fabs(dphi) <= cfg->ls_nu * fabs(dphi0);
+        if (armijo && curvature) {
+            best_alpha = a;
+            break;
+        }
+        if (sc > best) {
+            best = sc;
+            best_alpha = a;
+        }
+    }
+    for (int i = 0; i < 6; ++i) pose[i] += best_alpha * dl[i];
+    return best_alpha * dn;
+}
+
 static void align_gpu_sem_impl(const or_grid* g, const float* src, size_t n,
                                const double* pose_in, const or_config* cfg, or_result* out,
                                double* trace) {
@@ -1181,14 +1216,21 @@ static void align_gpu_sem_impl(const or_grid* g, const float* src, size_t n,
             for (int i = 0; i < 6; ++i) dl[i] = -gr[i] * 1e-4;
         double dphi = 0.0;
         for (int i = 0; i < 6; ++i) dphi += gr[i] * dl[i];
-        if (dphi <= 0.0)
+        if (dphi <= 0.0) {
             for (int i = 0; i < 6; ++i) dl[i] = -dl[i];
+            dphi = -dphi;
+        }
         double dn = 0.0;
         for (int i = 0; i < 6; ++i) dn += dl[i] * dl[i];
         dn = sqrt(dn);
-        double step = dn > cfg->step_size ? cfg->step_size : dn;
-        double scale = dn > 1e-10 ? step / dn : 0.0;
-        for (int i = 0; i < 6; ++i) pose[i] += scale * dl[i];
+        double step;
+        if (cfg->ls_candidates > 0) {
+            step = line_search_gpu_sem(g, src, n, pose, dl, sc, dphi, dn, d1, d2, cfg);
+        } else {
+            step = dn > cfg->step_size ? cfg->step_size : dn;
+            double scale = dn > 1e-10 ? step / dn : 0.0;
+            for (int i = 0; i < 6; ++i) pose[i] += scale * dl[i];
+        }
         if (it >= 1) {
             double cv[3], pv[3];
             for (int a = 0; a < 3; ++a) {

@@ -54,7 +54,9 @@ typedef struct {
     double step_size;
     double outlier_ratio;
     int32_t min_correspondences;  /* 10 in OptimizationConfig::default() */
-    int32_t pad;
+    int32_t ls_candidates;        /* graph path line search: 0 off, else candidates (<= 8) */
+    double ls_mu;                 /* Armijo constant (PipelineV2Config::armijo_mu, 1e-4) */
+    double ls_nu;                 /* curvature constant (PipelineV2Config::wolfe_nu, 0.9) */
 } or_config;
 
 /* derivatives/types.rs:61-75 */

@@ -39,13 +39,18 @@ class OrConfig(C.Structure):
     _fields_ = [("resolution", C.c_double), ("max_iterations", C.c_int32),
                 ("max_neighbors", C.c_int32), ("trans_epsilon", C.c_double),
                 ("step_size", C.c_double), ("outlier_ratio", C.c_double),
-                ("min_correspondences", C.c_int32), ("pad", C.c_int32)]
+                ("min_correspondences", C.c_int32), ("ls_candidates", C.c_int32),
+                ("ls_mu", C.c_double), ("ls_nu", C.c_double)]
 
 
 def config(resolution=2.0, max_iterations=30, max_neighbors=8, trans_epsilon=0.01,
-           step_size=0.1, outlier_ratio=0.55, min_correspondences=10):
+           step_size=0.1, outlier_ratio=0.55, min_correspondences=10, ls_candidates=0,
+           ls_mu=1e-4, ls_nu=0.9):
+    """ls_candidates > 0 turns on the graph path's parallel line search (the reference
+    pipeline uses 8 candidates, Armijo 1e-4, curvature 0.9: full_gpu_pipeline_v2.rs:101-113,
+    566-567)."""
     return OrConfig(resolution, max_iterations, max_neighbors, trans_epsilon, step_size,
-                    outlier_ratio, min_correspondences, 0)
+                    outlier_ratio, min_correspondences, ls_candidates, ls_mu, ls_nu)
 
 
 def lib():

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts():
     assert C.sizeof(capi.Result) == 6 * 8 + 3 * 8 + 36 * 8 + 6 * 4
-    assert C.sizeof(capi.Config) == 80
+    assert C.sizeof(capi.Config) == 88
     assert C.sizeof(capi.Scan) == 8 + 8 + 48
     assert C.sizeof(capi.ParticleConfig) == 4 + 4 + 4 * 8 + 8
     assert C.sizeof(capi.PoseEstimate) == 12 * 8 + 3 * 8 + 4 * 4
@@ -51,6 +51,18 @@ def test_config_defaults_mirror_reference():
     assert cfg.min_points_per_voxel == 6 and abs(cfg.eigenvalue_ratio - 0.01) < 1e-9
     assert cfg.max_neighbors == 8 and cfg.min_correspondences == 10
     assert cfg.hash_capacity_factor == 2
+    assert cfg.use_line_search == 0  # NdtScanMatcherConfig::default, ndt.rs:99
+
+
+def test_line_search_only_on_the_graph_path():
+    """The configuration is checked before any device call: line search with the CPU path's
+    semantics (More-Thuente, not built) is an invalid argument, on any machine."""
+    with pytest.raises(capi.NdtError) as e:
+        capi.Context(semantics=capi.SEMANTICS_CPU, use_line_search=1)
+    assert e.value.code == -1
+    with pytest.raises(capi.NdtError) as e:
+        capi.Context(use_line_search=2)
+    assert e.value.code == -1
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device error path")

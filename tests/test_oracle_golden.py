@@ -235,6 +235,22 @@ def test_oracle_aligns_single_case(oracle, single_cases, semantics):
             assert r["status"] in (0, 1) and (r["converged"] or r["iterations"] == 30)
 
 
+def test_oracle_line_search(oracle, single_cases):
+    """Graph path with the 8-candidate line search: converges to the same optimum as the
+    clamped-step path, in no more iterations than the 30 allowed, with full Newton steps
+    (no 0.1 m clamp) where they satisfy the Wolfe conditions."""
+    for case in single_cases:
+        grid = oracle.Grid(case.map_points, 2.0)
+        plain = grid.align(case.scan, case.guess)
+        ls, tr = grid.align_trace(case.scan, case.guess, ls_candidates=8)
+        assert ls["converged"], ls["iterations"]
+        assert np.abs(ls["pose"][:3] - plain["pose"][:3]).max() < 0.02
+        assert np.linalg.norm(ls["pose"][:2] - case.true_pose[:2]) < 0.1
+        steps = np.linalg.norm(np.diff(np.vstack([tr[:, 3:9], ls["pose"][None]]), axis=0)[:, :3],
+                               axis=1)
+        assert steps.max() > 0.1  # a full step beyond the clamp was taken
+
+
 def test_half_cube_scenarios(oracle):
     """Ports of src/ndt_cuda/src/ndt.rs:1490-1600 (within 2 m, positive score/NVTL)."""
     m = synth.half_cubic_pcd() + np.array([100, 100, 0], np.float32)
