@@ -20,10 +20,15 @@
 //      src/ndt_cuda/src/optimization/newton.rs:160-176 for the CPU semantics, with an FP64
 //      Cholesky fast path when H is definite and well conditioned), applies the reference's
 //      step control and convergence test, and broadcasts the next pose through DSMEM.
-// Only hardware cluster barriers are used: no global-memory spin waits.
+// k_ndt_align uses only hardware cluster barriers: no global-memory spin waits. The
+// work-queue variant k_ndt_queue (below) splits iterations into chunks claimed by a
+// persistent grid; its only waits are bounded polls for work.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <map>
+#include <mutex>
 
 #include "ndt_internal.h"
 
@@ -31,8 +36,6 @@ namespace cg = cooperative_groups;
 
 namespace ndtgb {
 
-constexpr int NACC = 34;          // f32 per-thread accumulators
-constexpr int NRED = NACC + 1;    // + correspondence count
 constexpr int MAX_WARPS = 16;
 constexpr int NFR = 52;           // per-iteration frame: R,t hi (12), R,t lo (12), A_k (27)
 // line-search candidate sums: score, G[3], G p^T [3x3], correspondence count (14 used)
@@ -681,10 +684,14 @@ __device__ __forceinline__ int search_point(const MapView& m, const float* qh, c
     return cnt;
 }
 
+// Per-point terms into the accumulators: acc[0 .. A_HTR) in registers, the 15 trailing ones
+// (J^T M J blocks A_HTR.., A_HRR..) in the thread's shared-memory column sacc[k * nbl_stride]
+// (they change once per point; keeping them out of registers leaves the search and pair
+// work room without spilling to local memory)
 template <bool CPU_SEM>
 __device__ __forceinline__ void point_terms(const MapView& m, float px, float py, float pz,
                                             const float* fr, int max_nb, float d1f, float d2f,
-                                            float* acc, int& ncorr, uint32_t* nbl,
+                                            float* acc, float* sacc, int& ncorr, uint32_t* nbl,
                                             int nbl_stride) {
     const float pv[3] = {px, py, pz};
     float qh[3], ql[3];
@@ -751,7 +758,7 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
 #pragma unroll
         for (int b = 0; b < 3; ++b) acc[A_GP + 3 * a + b] = fmaf(G[a], pv[b], acc[A_GP + 3 * a + b]);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) acc[A_HTR + 3 * a + k] += MJ[k][a];
+        for (int k = 0; k < 3; ++k) sacc[(3 * a + k) * nbl_stride] += MJ[k][a];
     }
     acc[A_M + 0] += M0;
     acc[A_M + 1] += M1;
@@ -763,9 +770,10 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int l = k; l < 3; ++l, ++kl)
-            acc[A_HRR + kl] = fmaf(J[k][0], MJ[l][0],
-                                   fmaf(J[k][1], MJ[l][1], fmaf(J[k][2], MJ[l][2], acc[A_HRR + kl])));
+        for (int l = k; l < 3; ++l, ++kl) {
+            float& h = sacc[(A_HRR - A_HTR + kl) * nbl_stride];
+            h = fmaf(J[k][0], MJ[l][0], fmaf(J[k][1], MJ[l][1], fmaf(J[k][2], MJ[l][2], h)));
+        }
 }
 
 // Line-search terms of one point at a candidate pose (graph semantics; the candidate pass of
@@ -1155,7 +1163,11 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_align(const AlignParams P) {
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
-    extern __shared__ uint32_t nbl_smem[];  // [max_nb][THREADS] accepted slots per thread
+    // dynamic shared memory: [max_nb][THREADS] accepted slots per thread, then the trailing
+    // NACC - A_HTR accumulators [NACC - A_HTR][THREADS], then the line search's warp sums
+    extern __shared__ uint32_t nbl_smem[];
+    float* const sacc =
+        reinterpret_cast<float*>(nbl_smem + (size_t)P.max_nb * THREADS) + threadIdx.x;
     cg::cluster_group cluster = cg::this_cluster();
     const int K = P.cluster;
     const int rank = (int)cluster.block_rank();
@@ -1197,15 +1209,19 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         const float* fr = sh.fr;
         float acc[NACC];
 #pragma unroll
-        for (int i = 0; i < NACC; ++i) acc[i] = 0.f;
+        for (int i = 0; i < A_HTR; ++i) acc[i] = 0.f;
+#pragma unroll
+        for (int k = 0; k < NACC - A_HTR; ++k) sacc[k * THREADS] = 0.f;
         int nc = 0;
         for (uint32_t i = (uint32_t)rank * THREADS + tid; i < n; i += (uint32_t)K * THREADS) {
             float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                   pz = __ldg(pts + 3 * (size_t)i + 2);
             if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-            point_terms<CPU_SEM>(m, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, nc,
+            point_terms<CPU_SEM>(m, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
                                  nbl_smem + tid, THREADS);
         }
+#pragma unroll
+        for (int k = 0; k < NACC - A_HTR; ++k) acc[A_HTR + k] = sacc[k * THREADS];
         warp_sum_acc(acc, lane, sh.warp_part[warp]);
         nc = __reduce_add_sync(0xffffffffu, nc);
         if (lane == 0) sh.warp_part[warp][NACC] = (double)nc;
@@ -1320,7 +1336,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             // candidate pass: score and gradient of each candidate pose of the round over this
             // rank's points, one candidate after another; FP64 warp sums of each candidate
             // kept in shared memory, summed over the CTA, then over the cluster by rank 0
-            double* lsw = reinterpret_cast<double*>(nbl_smem + (size_t)P.max_nb * THREADS);
+            double* lsw = reinterpret_cast<double*>(
+                nbl_smem + (size_t)(P.max_nb + NACC - A_HTR) * THREADS);
             for (int c = c_lo; c < c_hi; ++c) {
                 float a[LS_VALS];
 #pragma unroll
@@ -1408,6 +1425,365 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Work-queue Newton kernel
+//
+// In k_ndt_align a cluster owns one alignment for all its iterations, so a batch runs in
+// waves: alignments that need many iterations and start late set the batch's makespan, and
+// the cluster's other warps idle while rank 0 runs the FP64 step. Here the unit of work is a
+// chunk of one alignment's points for one iteration. A persistent grid of CTAs (all resident)
+// claims chunks of any open alignment, oldest alignment first; each chunk's sums go to global
+// memory in FP64, and the CTA that finishes the last chunk of an iteration runs that
+// alignment's Newton step (the same controller code) and publishes the next frame. Other
+// alignments' chunks keep every SM busy meanwhile, and the last alignments of a batch spread
+// over the whole GPU.
+//
+// Claims: QJob.gen_claim packs the alignment's iteration (high word) and the chunks claimed
+// so far (low word), so one atomicAdd both claims a chunk and names its iteration. The
+// controller resets it to (iteration + 1, 0) after writing the frame, behind a fence; readers
+// fence after a claim and read shared state through L2 (__ldcg), since L1 is not coherent
+// across SMs. A chunk's partial sums are written behind a fence before its done counter is
+// incremented; the controller, after the increment that completes the iteration, fences and
+// sums the partials in chunk order, so results do not depend on which CTA ran which chunk.
+// No CTA ever waits for another; a CTA that finds nothing to claim polls, and gives up with a
+// status bit after 2 s without work (every alignment ends within max_iterations steps).
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+// Initial state of every alignment: controller state at the initial pose, the first frame,
+// the chunk count; one warp per alignment.
+template <bool CPU_SEM>
+__global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
+    __shared__ double s_trig[4][16];
+    __shared__ double s_pose[4][6];
+    __shared__ float s_fr[4][NFR];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t j = blockIdx.x * 4 + w;
+    if (j >= P.num_jobs) return;
+    const AlignJob job = P.jobs[j];
+    QCtl* q = P.qctl + j;
+    if (lane < 6) s_pose[w][lane] = job.pose[lane];
+    __syncwarp();
+    make_frame_warp(s_pose[w], CPU_SEM, s_fr[w], s_trig[w], q->Ad, q->Bd, lane);
+    for (int i = lane; i < NFR; i += 32) P.qframe[(size_t)j * NFR + i] = s_fr[w][i];
+    if (lane < 6) q->pose[lane] = q->best_pose[lane] = job.pose[lane];
+    if (lane < 3) q->prev[lane] = q->prev2[lane] = job.pose[lane];
+    for (int i = lane; i < 36; i += 32) q->last_H[i] = 0.0;
+    if (lane == 0) {
+        q->best_score = -INFINITY;
+        q->last_corr = q->osc = q->max_osc = q->n_eigen = q->have_w = 0;
+        q->point_iters = q->corr_total = 0;
+        q->cyc_chunks = q->cyc_ctl = 0;
+        q->t_start = 0;
+        P.qjobs[j].gen_claim = 0ull;
+        P.qjobs[j].done = 0u;
+        P.qjobs[j].nchunks = job.n ? (job.n + (uint32_t)P.qchunk - 1u) / (uint32_t)P.qchunk : 1u;
+    }
+}
+
+// Newton step of alignment `job` after its iteration `it` (warp 0 of the CTA that finished
+// the iteration's last chunk): state from global memory, sums of the chunk partials in chunk
+// order, then the controller of k_ndt_align, then the next frame (or the outputs) published.
+template <bool CPU_SEM>
+__device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh, int job,
+                                           uint32_t it, int lane) {
+    const unsigned long long c0 = clock64();
+    QCtl* q = P.qctl + job;
+    if (lane < 6) {
+        sh.pose[lane] = __ldcg(q->pose + lane);
+        sh.best_pose[lane] = __ldcg(q->best_pose + lane);
+    }
+    if (lane < 3) {
+        sh.prev[lane] = __ldcg(q->prev + lane);
+        sh.prev2[lane] = __ldcg(q->prev2 + lane);
+    }
+    for (int i = lane; i < 36; i += 32) {
+        sh.last_H[i] = __ldcg(q->last_H + i);
+        sh.solve.W[i] = __ldcg(q->W + i);
+    }
+    for (int i = lane; i < 27; i += 32) sh.Ad[i] = __ldcg(q->Ad + i);
+    for (int i = lane; i < 54; i += 32) sh.Bd[i] = __ldcg(q->Bd + i);
+    if (lane == 0) {
+        sh.best_score = __ldcg(&q->best_score);
+        sh.last_corr = __ldcg(&q->last_corr);
+        sh.osc = __ldcg(&q->osc);
+        sh.max_osc = __ldcg(&q->max_osc);
+        sh.n_eigen = __ldcg(&q->n_eigen);
+        sh.solve.have_w = __ldcg(&q->have_w);
+    }
+    const uint32_t nch = P.qjobs[job].nchunks;
+    const double* part = P.qpart + (size_t)P.qpart_off[job] * NRED;
+    for (int k = lane; k < NRED; k += 32) {
+        double s = 0.0;
+        for (uint32_t c = 0; c < nch; ++c) s += __ldcg(part + (size_t)c * NRED + k);
+        sh.tot[k] = s;
+    }
+    __syncwarp();
+    finalize_gH(sh.tot, sh.Ad, sh.Bd, sh.g, sh.H, lane);
+    __syncwarp();
+    solve_warp<CPU_SEM>(sh.H, sh.g, sh.solve, lane);
+    const AlignJob jb = P.jobs[job];
+    int done = 0;
+    if (lane == 0) {
+        sh.n_eigen += sh.solve.path;
+        if (P.trace && (int)it < P.max_iter) {
+            double* t = P.trace + ((size_t)job * P.max_iter + it) * TRACE_REC;
+            t[0] = it;
+            t[1] = sh.tot[A_SC];
+            t[2] = sh.tot[NACC];
+            for (int i = 0; i < 6; ++i) {
+                t[3 + i] = sh.pose[i];
+                t[9 + i] = sh.g[i];
+                t[36 + i] = sh.solve.x[i];
+            }
+            int u = 0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i; j < 6; ++j) t[15 + u++] = sh.H[i * 6 + j];
+            t[42] = sh.solve.path;
+            t[43] = sh.solve.ok;
+            t[44] = t[45] = t[46] = 0.0;
+            t[47] = sh.solve.sweeps;
+        }
+        const int ncorr = (int)sh.tot[NACC];
+        const uint64_t pi = __ldcg(&q->point_iters) + jb.n;
+        const uint64_t ct = __ldcg(&q->corr_total) + (uint64_t)ncorr;
+        __stcg(&q->point_iters, pi);
+        __stcg(&q->corr_total, ct);
+        AlignOut& o = P.out[job];
+        done = control_step<CPU_SEM>(P, sh, jb, o, (int)it, sh.tot[A_SC], ncorr);
+        if (done) {
+            o.point_iters = pi;
+            o.corr_total = ct;
+        }
+    }
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (!done) make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+    __syncwarp();
+    if (!done) {
+        if (lane < 6) {
+            __stcg(q->pose + lane, sh.pose[lane]);
+            __stcg(q->best_pose + lane, sh.best_pose[lane]);
+        }
+        if (lane < 3) {
+            __stcg(q->prev + lane, sh.prev[lane]);
+            __stcg(q->prev2 + lane, sh.prev2[lane]);
+        }
+        for (int i = lane; i < 36; i += 32) {
+            __stcg(q->last_H + i, sh.last_H[i]);
+            __stcg(q->W + i, sh.solve.W[i]);
+        }
+        for (int i = lane; i < 27; i += 32) __stcg(q->Ad + i, sh.Ad[i]);
+        for (int i = lane; i < 54; i += 32) __stcg(q->Bd + i, sh.Bd[i]);
+        for (int i = lane; i < NFR; i += 32) __stcg(P.qframe + (size_t)job * NFR + i, sh.fr[i]);
+        if (lane == 0) {
+            __stcg(&q->best_score, sh.best_score);
+            __stcg(&q->last_corr, sh.last_corr);
+            __stcg(&q->osc, sh.osc);
+            __stcg(&q->max_osc, sh.max_osc);
+            __stcg(&q->n_eigen, sh.n_eigen);
+            __stcg(&q->have_w, sh.solve.have_w);
+        }
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) {
+        const unsigned long long cyc = __ldcg(&q->cyc_ctl) + (clock64() - c0);
+        __stcg(&q->cyc_ctl, cyc);
+        if (done) {
+            AlignOut& o = P.out[job];
+            o.cycles[0] = __ldcg(&q->cyc_chunks);
+            o.cycles[1] = 0;
+            o.cycles[2] = cyc;
+            o.cycles[3] = 0;
+            o.n_eigen = sh.n_eigen;
+            o.t_start = __ldcg(&q->t_start);
+            o.t_end = global_ns();
+            __threadfence();
+            atomicExch(&P.qjobs[job].gen_claim, (unsigned long long)QDONE << 32);
+            atomicAdd(P.qcount, 1u);
+        } else {
+            P.qjobs[job].done = 0u;
+            __threadfence();
+            atomicExch(&P.qjobs[job].gen_claim, (unsigned long long)(it + 1u) << 32);
+        }
+    }
+    __syncwarp();
+}
+
+template <int THREADS, bool CPU_SEM, int REGCAP>
+__global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
+    k_ndt_queue(const AlignParams P) {
+    constexpr int NW = THREADS / 32;
+    __shared__ AlignShared sh;
+    __shared__ int s_job, s_lw, s_flag;
+    __shared__ uint32_t s_chunk, s_gen;
+    // dynamic shared memory as in k_ndt_align: neighbour lists, then the trailing accumulators
+    extern __shared__ uint32_t nbl_smem[];
+    float* const sacc =
+        reinterpret_cast<float*>(nbl_smem + (size_t)P.max_nb * THREADS) + threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const MapView& m = P.map;
+    const uint32_t B = P.num_jobs;
+    uint64_t idle_since = 0;  // thread 0
+    if (tid == 0) s_lw = 0;
+    for (;;) {
+        __syncthreads();  // the previous chunk (and controller) is finished with shared memory
+        if (warp == 0) {
+            // claim: scan the alignments from the first one not known to be finished, 32 at
+            // a time, and try the claimable ones in order
+            int job = -1, first_open = -1;
+            uint32_t chunk = 0, gen = 0;
+            for (uint32_t base = (uint32_t)s_lw; base < B && job < 0; base += 32) {
+                const uint32_t j = base + lane;
+                bool open = false, ok = false;
+                uint32_t nch = 0;
+                if (j < B) {
+                    const unsigned long long w = ld_volatile(&P.qjobs[j].gen_claim);
+                    nch = P.qjobs[j].nchunks;
+                    open = (uint32_t)(w >> 32) != QDONE;
+                    ok = open && (uint32_t)w < nch;
+                }
+                const unsigned om = __ballot_sync(0xffffffffu, open);
+                if (first_open < 0 && om) first_open = (int)base + __ffs(om) - 1;
+                unsigned okm = __ballot_sync(0xffffffffu, ok);
+                while (okm != 0u && job < 0) {
+                    const int src = __ffs(okm) - 1;
+                    okm &= okm - 1u;
+                    unsigned long long old = 0ull;
+                    if (lane == src) old = atomicAdd(&P.qjobs[j].gen_claim, 1ull);
+                    old = __shfl_sync(0xffffffffu, old, src);
+                    const uint32_t ns = __shfl_sync(0xffffffffu, nch, src);
+                    if ((uint32_t)(old >> 32) != QDONE && (uint32_t)old < ns) {
+                        job = (int)base + src;
+                        chunk = (uint32_t)old;
+                        gen = (uint32_t)(old >> 32);
+                    }
+                }
+            }
+            __threadfence();  // acquire: the frame of the claimed iteration is published
+            if (lane == 0) {
+                s_lw = first_open >= 0 ? first_open : (int)B;
+                s_job = job;
+                s_chunk = chunk;
+                s_gen = gen;
+            }
+        }
+        __syncthreads();
+        const int job = s_job;
+        if (job < 0) {
+            // nothing claimable: every alignment finished, or the open ones wait for their
+            // Newton step
+            if (tid == 0) {
+                int stop = s_lw >= (int)B;
+                if (!stop) {
+                    const uint64_t now = global_ns();
+                    if (idle_since == 0) {
+                        idle_since = now;
+                    } else if (now - idle_since > 2000000000ull) {
+                        atomicOr(P.status, ST_QUEUE_STALL);
+                        stop = 1;
+                    }
+                }
+                s_flag = stop;
+            }
+            __syncthreads();
+            if (s_flag) break;
+            __nanosleep(500);
+            continue;
+        }
+        if (tid == 0) idle_since = 0;
+        const unsigned long long c0 = clock64();
+        const uint32_t chunk = s_chunk, gen = s_gen;
+        const AlignJob& jb = P.jobs[job];
+        if (tid < NFR) sh.fr[tid] = __ldcg(P.qframe + (size_t)job * NFR + tid);
+        if (tid == 0 && gen == 0 && chunk == 0) __stcg(&P.qctl[job].t_start, global_ns());
+        __syncthreads();
+        const float* pts = P.pts + 3 * jb.offset;
+        const uint32_t first = chunk * (uint32_t)P.qchunk;
+        const uint32_t last = min(jb.n, first + (uint32_t)P.qchunk);
+        float acc[NACC];
+#pragma unroll
+        for (int i = 0; i < A_HTR; ++i) acc[i] = 0.f;
+#pragma unroll
+        for (int k = 0; k < NACC - A_HTR; ++k) sacc[k * THREADS] = 0.f;
+        int nc = 0;
+        for (uint32_t i = first + tid; i < last; i += THREADS) {
+            float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
+                  pz = __ldg(pts + 3 * (size_t)i + 2);
+            if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
+            point_terms<CPU_SEM>(m, px, py, pz, sh.fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
+                                 nbl_smem + tid, THREADS);
+        }
+#pragma unroll
+        for (int k = 0; k < NACC - A_HTR; ++k) acc[A_HTR + k] = sacc[k * THREADS];
+        warp_sum_acc(acc, lane, sh.warp_part[warp]);
+        nc = __reduce_add_sync(0xffffffffu, nc);
+        if (lane == 0) sh.warp_part[warp][NACC] = (double)nc;
+        __syncthreads();
+        double* part = P.qpart + ((size_t)P.qpart_off[job] + chunk) * NRED;
+        for (int k = tid; k < NRED; k += THREADS) {
+            double s = 0.0;
+            for (int w = 0; w < NW; ++w) s += sh.warp_part[w][k];
+            __stcg(part + k, s);
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t prev = atomicAdd(&P.qjobs[job].done, 1u);
+            s_flag = prev + 1u == P.qjobs[job].nchunks;
+            atomicAdd(&P.qctl[job].cyc_chunks, (unsigned long long)(clock64() - c0));
+        }
+        __syncthreads();
+        if (!s_flag) continue;
+        __threadfence();  // acquire: every chunk's partials of this iteration are visible
+        if (warp == 0) queue_control<CPU_SEM>(P, sh, job, gen, lane);
+    }
+}
+
+template <int T, bool SEM, int CAP>
+static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t chunks,
+                                  cudaStream_t s) {
+    auto kern = k_ndt_queue<T, SEM, CAP>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // persistent grid: every CTA resident (the kernel's CTAs never wait for each other, so
+    // residency is a matter of speed only), at most one CTA per chunk of the batch
+    static std::mutex mu;
+    static std::map<std::pair<int, size_t>, int> cache;  // (device, smem) -> CTAs
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int ctas = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find({dev, smem});
+        if (it != cache.end()) {
+            ctas = it->second;
+        } else {
+            int per_sm = 0, sms = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem);
+            if (e != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+                return e;
+            ctas = std::max(1, per_sm * sms);
+            cache[{dev, smem}] = ctas;
+        }
+    }
+    k_queue_init<SEM><<<(p.num_jobs + 3) / 4, 128, 0, s>>>(p);
+    const unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)ctas, std::max(1u, chunks));
+    kern<<<grid, T, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <int T, int CAP>
+static int launch_queue_t(const AlignParams& p, uint32_t chunks, cudaStream_t s) {
+    const size_t smem = (size_t)T * (p.max_nb + NACC - A_HTR) * sizeof(uint32_t);
+    const cudaError_t e = p.semantics == NDT_SEMANTICS_CPU
+                              ? launch_queue_k<T, true, CAP>(p, smem, chunks, s)
+                              : launch_queue_k<T, false, CAP>(p, smem, chunks, s);
+    return cuda_fail(e, "work-queue align launch");
+}
+
 template <int T, bool SEM, int CAP>
 static cudaError_t launch_k(cudaLaunchConfig_t& cfg, const AlignParams& p, int K) {
     cudaFuncSetAttribute(k_ndt_align<T, SEM, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1423,9 +1799,9 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.num_jobs * K, 1, 1);
     cfg.blockDim = dim3(T, 1, 1);
-    // [max_nb][T] neighbour lists, then (line search) [T/32][LS_MAX][LS_VALS] FP64 warp sums;
-    // T * max_nb * 4 bytes is a multiple of 8 (T is)
-    cfg.dynamicSmemBytes = (size_t)T * p.max_nb * sizeof(uint32_t) +
+    // [max_nb][T] neighbour lists, [NACC - A_HTR][T] accumulators, then (line search)
+    // [T/32][LS_MAX][LS_VALS] FP64 warp sums; the first two are multiples of 8 bytes (T is)
+    cfg.dynamicSmemBytes = (size_t)T * (p.max_nb + NACC - A_HTR) * sizeof(uint32_t) +
                            (p.ls_cands > 0 && p.semantics != NDT_SEMANTICS_CPU
                                 ? (size_t)(T / 32) * LS_MAX * LS_VALS * sizeof(double)
                                 : 0);
@@ -1452,6 +1828,23 @@ int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s) {
     AlignParams q = p;
     q.cluster = K;
     const int R = shape.regcap;
+    if (shape.queue > 0) {
+        if (p.ls_cands > 0 || !p.qjobs) {
+            set_error("the work-queue kernel takes no line search and needs its buffers");
+            return NDT_ERR_INVALID_ARGUMENT;
+        }
+        q.qchunk = shape.threads * shape.queue;
+        switch (shape.threads) {
+            case 128: return launch_queue_t<128, 64>(q, p.qchunks_total, s);
+            case 256:
+                return R == 80 ? launch_queue_t<256, 80>(q, p.qchunks_total, s)
+                               : launch_queue_t<256, 64>(q, p.qchunks_total, s);
+            case 512: return launch_queue_t<512, 128>(q, p.qchunks_total, s);
+            default:
+                set_error("threads per CTA must be 128, 256 or 512");
+                return NDT_ERR_INVALID_ARGUMENT;
+        }
+    }
     switch (shape.threads) {
         case 128:
             return R == 64 ? launch_t<128, 64>(q, K, s)

@@ -174,11 +174,12 @@ struct ndt_ctx {
     bool profile = false;
     bool trace = false;
     DevBuf d_trace;
+    DevBuf d_qjobs, d_qctl, d_qframe, d_qpart, d_qoff;  // work-queue kernel
     std::vector<double> h_trace;       // last call's records, by job order
     std::vector<uint32_t> trace_slot;  // job index -> caller's result index
     int trace_iters = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
-    LaunchShape forced{0, 0, 0};                           // set only while autotuning
+    LaunchShape forced{0, 0, 0, 0};                        // set only while autotuning
     std::map<std::pair<int, int>, LaunchShape> tuned;      // (log2 jobs, log2 max points)
     // captured batches, most recently used last; a key holds everything the captured
     // launches bake in (sizes, launch shape, buffer addresses, map and parameter versions)
@@ -266,6 +267,10 @@ static int check_status(ndt_ctx* c, uint32_t st) {
         set_error("hash probe exceeded its bound");
         return NDT_ERR_PROBE_LIMIT;
     }
+    if (st & ST_QUEUE_STALL) {
+        set_error("work-queue Newton kernel found no work for 2 s with alignments open");
+        return NDT_ERR_DEVICE;
+    }
     set_error("device reported status " + std::to_string(st));
     return NDT_ERR_DEVICE;
 }
@@ -310,7 +315,11 @@ static bool config_ok(const ndt_config& c) {
            (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
            (c.cuda_graph == 0 || c.cuda_graph == 1) &&
            (c.use_line_search == 0 ||
-            (c.use_line_search == 1 && c.semantics == NDT_SEMANTICS_GPU_GRAPH));
+            (c.use_line_search == 1 && c.semantics == NDT_SEMANTICS_GPU_GRAPH)) &&
+           c.work_queue >= -1 && c.work_queue <= 16 &&
+           (c.work_queue <= 0 || (T != 128 || R == 0 || R == 64)) &&
+           (c.work_queue <= 0 || (T != 512 || R == 0 || R == 128)) &&
+           (c.work_queue <= 0 || (T != 256 || R == 0 || R == 64 || R == 80));
 }
 
 extern "C" {
@@ -392,7 +401,8 @@ int ndt_ctx_destroy(ndt_ctx* c) {
                       &c->bs.seg_ids, &c->bs.seg_starts, &c->bs.seg_valid, &c->bs.seg_rank,
                       &c->bs.seg_rec, &c->bs.small, &c->d_in, &c->d_jobs, &c->d_aout,
                       &c->d_sjobs, &c->d_sout, &c->d_part, &c->d_status, &c->d_q, &c->d_qidx,
-                      &c->d_qcnt, &c->d_trace})
+                      &c->d_qcnt, &c->d_trace, &c->d_qjobs, &c->d_qctl, &c->d_qframe,
+                      &c->d_qpart, &c->d_qoff})
         dev_free(*b);
     for (PinBuf* b : {&c->h_pts, &c->h_jobs, &c->h_aout, &c->h_sjobs, &c->h_sout, &c->h_misc})
         pin_free(*b);
@@ -674,11 +684,22 @@ static int log2_bucket(uint64_t v) {
 // (batch size, scan size) bucket, then the default: 512-thread CTAs for large scans, and
 // clusters doubled until the launch covers about three CTAs per SM while keeping at least
 // two points per thread per CTA.
+// The work-queue kernel is used when the configuration asks for it (work_queue > 0) or the
+// autotuner picked it, never with line search.
 static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
-    LaunchShape sh{0, 0, 128};
+    LaunchShape sh{0, 0, 128, 0};
     if (c->forced.cluster > 0) return c->forced;
+    const bool ls = c->cfg.use_line_search && c->cfg.semantics != NDT_SEMANTICS_CPU;
+    if (c->cfg.work_queue > 0 && !ls) {
+        sh.cluster = 1;
+        sh.threads = c->cfg.threads_per_cta > 0 ? c->cfg.threads_per_cta : 256;
+        sh.regcap = c->cfg.max_registers > 0 ? c->cfg.max_registers : (sh.threads == 512 ? 128 : 64);
+        sh.queue = c->cfg.work_queue;
+        return sh;
+    }
     auto it = c->tuned.find({log2_bucket(jobs), log2_bucket(max_n)});
-    if (it != c->tuned.end() && c->cfg.cluster_size <= 0 && c->cfg.threads_per_cta <= 0)
+    if (it != c->tuned.end() && c->cfg.cluster_size <= 0 && c->cfg.threads_per_cta <= 0 &&
+        !(it->second.queue > 0 && (ls || c->cfg.work_queue < 0)))
         return it->second;
     sh.threads = c->cfg.threads_per_cta > 0
                      ? c->cfg.threads_per_cta
@@ -759,6 +780,50 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         p.trace = (double*)c->d_trace.p;
     }
     LaunchShape shape = choose_shape(c, nj, max_n);
+    // work-queue kernel: chunk counts and partial-sum offsets per alignment (host, in the
+    // pinned job block), per-alignment state and the partials (device)
+    size_t qob = 0;
+    uint32_t* hq = nullptr;
+    if (shape.queue > 0) {
+        const uint32_t chunk = (uint32_t)(shape.threads * shape.queue);
+        qob = (size_t)nj * sizeof(uint32_t);
+        if ((rc = pin_reserve(c->h_jobs, jb + sjb + qob))) return rc;
+        hj = (AlignJob*)c->h_jobs.p;  // the block may have moved: refill it
+        hs = (ScoreJob*)((char*)c->h_jobs.p + jb);
+        for (uint32_t j = 0; j < nj; ++j) {
+            hj[j] = jobs[j];
+            ScoreJob s{};
+            s.offset = jobs[j].offset;
+            s.n = jobs[j].n;
+            s.pose_src = 1;
+            s.out_index = j;
+            hs[j] = s;
+        }
+        hq = (uint32_t*)((char*)c->h_jobs.p + jb + sjb);
+        uint64_t total = 0;
+        for (uint32_t j = 0; j < nj; ++j) {
+            hq[j] = (uint32_t)total;
+            total += jobs[j].n ? (jobs[j].n + chunk - 1) / chunk : 1;
+        }
+        if (total > 0xFFFFFFFFull) {
+            set_error("too many chunks in one batch");
+            return NDT_ERR_CAPACITY;
+        }
+        if ((rc = dev_reserve(c->d_qjobs, (size_t)nj * sizeof(QJob))) ||
+            (rc = dev_reserve(c->d_qctl, (size_t)nj * sizeof(QCtl))) ||
+            (rc = dev_reserve(c->d_qframe, (size_t)nj * 52 * sizeof(float))) ||
+            (rc = dev_reserve(c->d_qoff, qob)) ||
+            (rc = dev_reserve(c->d_qpart, (size_t)total * NRED * sizeof(double))))
+            return rc;
+        p.qjobs = (QJob*)c->d_qjobs.p;
+        p.qctl = (QCtl*)c->d_qctl.p;
+        p.qframe = (float*)c->d_qframe.p;
+        p.qpart = (double*)c->d_qpart.p;
+        p.qpart_off = (const uint32_t*)c->d_qoff.p;
+        p.qcount = (uint32_t*)c->d_status.p + 2;  // word 2 of the status block
+        p.qchunks_total = (uint32_t)total;
+        c->stats.h2d_bytes += qob;
+    }
     AlignOut* ho = (AlignOut*)c->h_aout.p;
     ScoreOut* hso = (ScoreOut*)((char*)c->h_aout.p + ob);
     uint32_t* hst = (uint32_t*)((char*)c->h_aout.p + ob + sob);
@@ -767,6 +832,10 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
     auto enqueue = [&](unsigned evf) -> int {
         cudaMemcpyAsync(c->d_jobs.p, hj, jb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
+        if (shape.queue > 0) {
+            cudaMemcpyAsync(c->d_qoff.p, hq, qob, cudaMemcpyHostToDevice, st);
+            cudaMemsetAsync(p.qcount, 0, 4, st);
+        }
         cudaEventRecordWithFlags(c->ev0, st, evf);
         int r = launch_align(p, shape, st);
         if (r) return r;
@@ -784,6 +853,9 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
     if (c->cfg.cuda_graph && !c->trace) {
         const std::vector<uint64_t> key = {
             nj, max_n, (uint64_t)shape.cluster, (uint64_t)shape.threads, (uint64_t)shape.regcap,
+            (uint64_t)shape.queue, (uint64_t)(uintptr_t)c->d_qjobs.p,
+            (uint64_t)(uintptr_t)c->d_qctl.p, (uint64_t)(uintptr_t)c->d_qframe.p,
+            (uint64_t)(uintptr_t)c->d_qpart.p, (uint64_t)(uintptr_t)c->d_qoff.p,
             c->map_gen, c->cfg_gen, (uint64_t)(uintptr_t)d_pts, (uint64_t)(uintptr_t)c->d_jobs.p,
             (uint64_t)(uintptr_t)c->d_aout.p, (uint64_t)(uintptr_t)c->d_sjobs.p,
             (uint64_t)(uintptr_t)c->d_sout.p, (uint64_t)(uintptr_t)c->d_part.p,
@@ -1204,34 +1276,43 @@ int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const 
     const int Ks[4] = {1, 2, 4, 8};
     const int TC[8][2] = {{128, 128}, {128, 80}, {128, 64}, {256, 128},
                           {256, 80},  {256, 64}, {256, 48}, {512, 128}};
-    LaunchShape best{0, 0, 128};
+    // work-queue candidates: (threads, registers, points per thread per chunk)
+    const int QC[6][3] = {{256, 64, 2}, {256, 64, 4}, {256, 64, 8},
+                          {256, 80, 4}, {128, 64, 4}, {512, 128, 2}};
+    const bool ls = c->cfg.use_line_search && c->cfg.semantics != NDT_SEMANTICS_CPU;
+    std::vector<LaunchShape> cands;
+    if (c->cfg.work_queue <= 0 || ls)
+        for (int K : Ks)
+            for (const auto& tc : TC) cands.push_back(LaunchShape{K, tc[0], tc[1], 0});
+    if (c->cfg.work_queue >= 0 && !ls)
+        for (const auto& qc : QC) cands.push_back(LaunchShape{1, qc[0], qc[1], qc[2]});
+    LaunchShape best{0, 0, 128, 0};
     double best_ms = 1e300;
     int tried = 0;
-    for (int K : Ks) {
-        for (const auto& tc : TC) {
-            c->forced = LaunchShape{K, tc[0], tc[1]};
-            rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());  // warm
-            if (rc) break;
-            double before = c->stats.align_kernel_ms;
-            for (int r = 0; r < repeats && !rc; ++r)
-                rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());
-            if (rc) break;
-            double ms = (c->stats.align_kernel_ms - before) / repeats;
-            tried++;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = c->forced;
-            }
-        }
+    for (const LaunchShape& cand : cands) {
+        c->forced = cand;
+        rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());  // warm
         if (rc) break;
+        double before = c->stats.align_kernel_ms;
+        for (int r = 0; r < repeats && !rc; ++r)
+            rc = ndt_align_batch_device(c, d_xyz, offsets, poses, m, tmp.data());
+        if (rc) break;
+        double ms = (c->stats.align_kernel_ms - before) / repeats;
+        tried++;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c->forced;
+        }
     }
-    c->forced = LaunchShape{0, 0, 0};
+    c->forced = LaunchShape{0, 0, 0, 0};
     c->stats = saved;
     if (rc) return rc;
     c->tuned[{log2_bucket(m), log2_bucket(max_n)}] = best;
     out->cluster_size = best.cluster;
     out->threads_per_cta = best.threads;
     out->registers = best.regcap;
+    out->work_queue = best.queue;
+    out->reserved = 0;
     out->kernel_ms = best_ms;
     out->aligns_per_s = best_ms > 0 ? 1000.0 * (double)m / best_ms : 0.0;
     out->candidates = tried;

@@ -114,6 +114,39 @@ struct AlignParams {
     uint32_t* status;
     int32_t ls_cands;      // graph-path line search: candidates per iteration (0: off)
     double ls_mu, ls_nu;   // strong Wolfe constants
+    // work-queue kernel (k_ndt_queue): per-alignment claim words, controller state, frames,
+    // per-chunk partial sums (offsets by alignment), counters {alignments finished}
+    struct QJob* qjobs;
+    struct QCtl* qctl;
+    float* qframe;
+    double* qpart;
+    const uint32_t* qpart_off;
+    uint32_t* qcount;
+    int32_t qchunk;        // points per chunk (set by the launch from the shape)
+    uint32_t qchunks_total;  // chunks of one iteration of every alignment
+};
+
+// Newton-kernel sums per iteration: 34 f32 per-thread accumulators (score, gradient and
+// Hessian terms), reduced in FP64, plus the correspondence count.
+constexpr int NACC = 34;
+constexpr int NRED = NACC + 1;
+
+// Work-queue kernel state, one per alignment (global memory).
+struct QJob {
+    unsigned long long gen_claim;  // iteration << 32 | chunks claimed (iteration QDONE: finished)
+    uint32_t done;                 // chunks of the current iteration finished
+    uint32_t nchunks;
+};
+constexpr uint32_t QDONE = 0xFFFFFFFFu;
+// Controller state of an alignment between iterations (FP64; read and written only by the
+// controller of the alignment's current iteration).
+struct QCtl {
+    double pose[6], best_pose[6], best_score, last_H[36], prev[3], prev2[3];
+    double W[36];
+    double Ad[27], Bd[54];
+    uint64_t point_iters, corr_total, t_start;
+    unsigned long long cyc_chunks, cyc_ctl;
+    int32_t last_corr, osc, max_osc, n_eigen, have_w, pad;
 };
 
 // Line search of the graph path: at most 8 candidates (GRAPH_MAX_LS_CANDIDATES,
@@ -126,7 +159,8 @@ constexpr double LS_NU = 0.9;
 struct LaunchShape {
     int cluster;
     int threads;
-    int regcap;  // 128 (default) or 80 (denser residency for 128/256-thread CTAs)
+    int regcap;  // 128 (default); 80, 64, 48: denser residency for 128/256-thread CTAs
+    int queue;   // > 0: work-queue kernel, chunks of `queue` points per thread (cluster 1)
 };
 
 int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s);

@@ -85,7 +85,12 @@ typedef struct ndt_config {
                                       (ndt_graph_kernels.cu:388-430,473-570,626-710) instead
                                       of the clamped step; graph semantics only (the CPU
                                       path's More-Thuente search is not built) */
-    int32_t reserved;              /* 0 */
+    int32_t work_queue;            /* Newton-kernel form: n > 0 the work-queue kernel (a
+                                      persistent grid claiming chunks of n points per thread
+                                      of any alignment's iteration); -1 one thread-block
+                                      cluster per alignment; 0 autotuned (cluster kernel
+                                      until tuned). Line search always uses the cluster
+                                      kernel. */
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
@@ -204,14 +209,14 @@ int ndt_align_batch(ndt_ctx* ctx, const ndt_scan* scans, uint64_t num_scans, ndt
 int ndt_align_batch_device(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
                            const double* poses_in, uint64_t num_scans, ndt_result* out);
 
-/* Autotuner for the Newton kernel's launch shape (points per CTA = scan size / cluster
- * size; threads per CTA): times every (cluster size 1, 2, 4, 8) x (128, 256, 512 threads)
- * candidate, each with a 128- and an 80-register instance where the CTA size allows more
- * than one resident CTA per SM, on the given device-resident batch (as ndt_align_batch_device takes it),
- * `repeats` timed runs each, and records the fastest for batches of this size class (log2
- * of the scan count and of the largest scan). Later calls in that class use it unless the
- * configuration fixes cluster_size / threads_per_cta. No counterpart in the reference,
- * whose launch shapes are constants. */
+/* Autotuner for the Newton kernel's launch shape: times the cluster kernel at every
+ * (cluster size 1, 2, 4, 8) x (threads per CTA, register cap) candidate and the work-queue
+ * kernel at its (threads, registers, points per thread per chunk) candidates (unless the
+ * configuration fixes the form, or line search is on) on the given device-resident batch
+ * (as ndt_align_batch_device takes it), `repeats` timed runs each, and records the fastest
+ * for batches of this size class (log2 of the scan count and of the largest scan). Later
+ * calls in that class use it unless the configuration fixes cluster_size /
+ * threads_per_cta. No counterpart in the reference, whose launch shapes are constants. */
 typedef struct ndt_tune_result {
     int32_t cluster_size;
     int32_t threads_per_cta;
@@ -219,6 +224,9 @@ typedef struct ndt_tune_result {
     double aligns_per_s;           /* batch size / kernel_ms */
     int32_t candidates;
     int32_t registers;             /* register cap of the winning kernel instance */
+    int32_t work_queue;            /* points per thread per chunk of the winner if it is the
+                                      work-queue kernel, else 0 */
+    int32_t reserved;
 } ndt_tune_result;
 int ndt_autotune(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
                  const double* poses_in, uint64_t num_scans, int32_t repeats,
