@@ -35,9 +35,11 @@ sys.path.insert(0, ROOT)
 METRIC = "scan aligns/s (20k pts, 5M-pt map); init-pose est/s, learned vs plain"
 FLOP_PER_POINT_ITER = 165
 FLOP_PER_PAIR = 65
-# DRAM bytes (read + write) of one k_ndt_align launch of the default workload (256 scans,
-# 5M-point map, seed 2), from one ncu capture of this bench (profiles/k_ndt_align_seq5M_b256.md)
-NCU_ALIGN_TRAFFIC = {(256, 5_000_000, 2): 73.3e6}
+# DRAM bytes (read + write) of one Newton-kernel launch of the default workload (256 scans,
+# 5M-point map, seed 2), from one ncu capture of this bench per kernel form
+# (profiles/k_ndt_align_seq5M_b256.md, profiles/k_ndt_queue_seq5M_b256.md)
+NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
+                     ("k_ndt_queue", 256, 5_000_000, 2): 75.6e6}
 
 
 def parse():
@@ -53,8 +55,9 @@ def parse():
     ap.add_argument("--extras", type=int, default=1,
                     help="also run the initial-pose search and the uneven-queue workloads")
     ap.add_argument("--shape", default="",
-                    help="fixed Newton-kernel launch shape CLUSTER,THREADS,REGISTERS "
-                         "(e.g. 8,256,80) instead of the autotuner")
+                    help="fixed Newton-kernel launch shape CLUSTER,THREADS,REGISTERS[,QUEUE] "
+                         "(e.g. 8,256,64 for the cluster kernel, 1,256,64,4 for the work-queue "
+                         "kernel with 4 points per thread per chunk) instead of the autotuner")
     return ap.parse_args()
 
 
@@ -548,9 +551,12 @@ def run_ours(args):
         capi.check(ctx.lib.ndt_align_batch(ctx.h, scan_arr, B, res_e2e))
 
     if args.shape:
-        K, T, R = (int(v) for v in args.shape.split(","))
-        ctx.configure(cluster_size=K, threads_per_cta=T, max_registers=R)
-        tune = {"cluster_size": K, "threads_per_cta": T, "registers": R,
+        vals = [int(v) for v in args.shape.split(",")]
+        K, T, R = vals[:3]
+        Q = vals[3] if len(vals) > 3 else 0
+        ctx.configure(cluster_size=K, threads_per_cta=T, max_registers=R,
+                      work_queue=Q if Q > 0 else -1)
+        tune = {"cluster_size": K, "threads_per_cta": T, "registers": R, "work_queue": Q,
                 "chosen_by": "--shape"}
     else:
         # launch shape for this batch class, chosen by the library's autotuner (untimed)
@@ -621,6 +627,7 @@ def run_ours(args):
         extra["queue"] = queue_bench(10)
         extra["learned_init_pose"] = learned_bench()
         extra["large_map"] = large_map_bench()
+    kname = "k_ndt_queue" if tune["work_queue"] else "k_ndt_align"
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "aligns/s", "n_gpus": world,
@@ -638,14 +645,15 @@ def run_ours(args):
                        "launch_shape": {"cluster_size": tune["cluster_size"],
                                         "threads_per_cta": tune["threads_per_cta"],
                                         "registers": tune["registers"],
+                                        "work_queue_points_per_thread": tune["work_queue"],
                                         "chosen_by": tune["chosen_by"]}},
             "e2e": {"value": e2e, "unit": "aligns/s",
                     "h2d_bytes_per_step": int(st_e2e["h2d_bytes"] // max(args.steps, 1)),
                     "d2h_bytes_per_step": int(st_e2e["d2h_bytes"] // max(args.steps, 1))},
-            "roofline": {"bound": "fp32", "kernel": "k_ndt_align", "achieved": achieved,
+            "roofline": {"bound": "fp32", "kernel": kname, "achieved": achieved,
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None,
-                         "traffic": NCU_ALIGN_TRAFFIC.get((B, args.map_points, args.seed)),
+                         "traffic": NCU_ALIGN_TRAFFIC.get((kname, B, args.map_points, args.seed)),
                          "traffic_unit": "bytes per launch (ncu dram read + write)",
                          "peak_source": f"derived: SMs x 128 FP32 lanes x 2 x sm_max_mhz "
                                         f"({src} MEASURED_PEAKS.json clock)",
