@@ -1452,8 +1452,31 @@ __device__ __forceinline__ unsigned long long ld_volatile(const unsigned long lo
     return *reinterpret_cast<const volatile unsigned long long*>(p);
 }
 
+// Claim word of an alignment: iteration (16 bits; QDONE once finished), the iteration's chunk
+// count (16 bits) and the chunks claimed so far (32 bits). One atomicAdd claims a chunk and
+// returns all three consistently.
+__device__ __forceinline__ unsigned long long qword(uint32_t gen, uint32_t nch) {
+    return ((unsigned long long)gen << 48) | ((unsigned long long)nch << 32);
+}
+__device__ __forceinline__ uint32_t qw_gen(unsigned long long w) { return (uint32_t)(w >> 48); }
+__device__ __forceinline__ uint32_t qw_nch(unsigned long long w) {
+    return (uint32_t)(w >> 32) & 0xFFFFu;
+}
+
+// Chunks of iteration `it` of an alignment with n points: n / qchunk for its first
+// QSPLIT_ITER iterations, then four times as many, a quarter the size. The alignments that
+// run long are the ones that finish a batch, on an otherwise idle GPU: smaller chunks spread
+// each of their iterations over more SMs. The rule depends on the iteration alone, so every
+// run sums an alignment's chunks over the same tree (results are identical run to run). At
+// most QMAXCH.
+constexpr uint32_t QSPLIT_ITER = 10;
+__device__ __forceinline__ uint32_t queue_chunks(const AlignParams& P, uint32_t n, uint32_t it) {
+    const uint32_t size = it < QSPLIT_ITER ? (uint32_t)P.qchunk : (uint32_t)P.qchunk / 4u;
+    return min(n ? (n + size - 1u) / size : 1u, QMAXCH);
+}
+
 // Initial state of every alignment: controller state at the initial pose, the first frame,
-// the chunk count; one warp per alignment.
+// the claim word of iteration 0; one warp per alignment.
 template <bool CPU_SEM>
 __global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
     __shared__ double s_trig[4][16];
@@ -1477,15 +1500,15 @@ __global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
         q->point_iters = q->corr_total = 0;
         q->cyc_chunks = q->cyc_ctl = 0;
         q->t_start = 0;
-        P.qjobs[j].gen_claim = 0ull;
+        P.qjobs[j].gen_claim = qword(0u, queue_chunks(P, job.n, 0u));
         P.qjobs[j].done = 0u;
-        P.qjobs[j].nchunks = job.n ? (job.n + (uint32_t)P.qchunk - 1u) / (uint32_t)P.qchunk : 1u;
     }
 }
 
 // Newton step of alignment `job` after its iteration `it` (warp 0 of the CTA that finished
-// the iteration's last chunk): state from global memory, sums of the chunk partials in chunk
-// order, then the controller of k_ndt_align, then the next frame (or the outputs) published.
+// the iteration's last chunk, once the CTA has summed the chunk partials into sh.tot):
+// state from global memory, the controller of k_ndt_align, then the next frame and claim
+// word (or the outputs) published.
 template <bool CPU_SEM>
 __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh, int job,
                                            uint32_t it, int lane) {
@@ -1513,23 +1536,19 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
         sh.n_eigen = __ldcg(&q->n_eigen);
         sh.solve.have_w = __ldcg(&q->have_w);
     }
-    const uint32_t nch = P.qjobs[job].nchunks;
-    const double* part = P.qpart + (size_t)P.qpart_off[job] * NRED;
-    for (int k = lane; k < NRED; k += 32) {
-        double s = 0.0;
-        for (uint32_t c = 0; c < nch; ++c) s += __ldcg(part + (size_t)c * NRED + k);
-        sh.tot[k] = s;
-    }
     __syncwarp();
+    const unsigned long long c1 = clock64();
     finalize_gH(sh.tot, sh.Ad, sh.Bd, sh.g, sh.H, lane);
     __syncwarp();
     solve_warp<CPU_SEM>(sh.H, sh.g, sh.solve, lane);
+    const unsigned long long c2 = clock64();
     const AlignJob jb = P.jobs[job];
     int done = 0;
+    double* t = nullptr;
     if (lane == 0) {
         sh.n_eigen += sh.solve.path;
         if (P.trace && (int)it < P.max_iter) {
-            double* t = P.trace + ((size_t)job * P.max_iter + it) * TRACE_REC;
+            t = P.trace + ((size_t)job * P.max_iter + it) * TRACE_REC;
             t[0] = it;
             t[1] = sh.tot[A_SC];
             t[2] = sh.tot[NACC];
@@ -1543,7 +1562,8 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
                 for (int j = i; j < 6; ++j) t[15 + u++] = sh.H[i * 6 + j];
             t[42] = sh.solve.path;
             t[43] = sh.solve.ok;
-            t[44] = t[45] = t[46] = 0.0;
+            t[44] = (double)(c1 - c0);  // state load
+            t[45] = (double)(c2 - c1);  // assembly + solve
             t[47] = sh.solve.sweeps;
         }
         const int ncorr = (int)sh.tot[NACC];
@@ -1589,7 +1609,9 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
     __threadfence();
     __syncwarp();
     if (lane == 0) {
-        const unsigned long long cyc = __ldcg(&q->cyc_ctl) + (clock64() - c0);
+        const unsigned long long c3 = clock64();
+        if (t) t[46] = (double)(c3 - c2);  // step + next frame + state store
+        const unsigned long long cyc = __ldcg(&q->cyc_ctl) + (c3 - c0);
         __stcg(&q->cyc_ctl, cyc);
         if (done) {
             AlignOut& o = P.out[job];
@@ -1601,12 +1623,13 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
             o.t_start = __ldcg(&q->t_start);
             o.t_end = global_ns();
             __threadfence();
-            atomicExch(&P.qjobs[job].gen_claim, (unsigned long long)QDONE << 32);
+            atomicExch(&P.qjobs[job].gen_claim, qword(QDONE, 0u));
             atomicAdd(P.qcount, 1u);
         } else {
+            const uint32_t nch = queue_chunks(P, jb.n, it + 1u);
             P.qjobs[job].done = 0u;
             __threadfence();
-            atomicExch(&P.qjobs[job].gen_claim, (unsigned long long)(it + 1u) << 32);
+            atomicExch(&P.qjobs[job].gen_claim, qword(it + 1u, nch));
         }
     }
     __syncwarp();
@@ -1618,7 +1641,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
     __shared__ int s_job, s_lw, s_flag;
-    __shared__ uint32_t s_chunk, s_gen;
+    __shared__ uint32_t s_chunk, s_gen, s_nch;
     // dynamic shared memory as in k_ndt_align: neighbour lists, then the trailing accumulators
     extern __shared__ uint32_t nbl_smem[];
     float* const sacc =
@@ -1634,16 +1657,14 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             // claim: scan the alignments from the first one not known to be finished, 32 at
             // a time, and try the claimable ones in order
             int job = -1, first_open = -1;
-            uint32_t chunk = 0, gen = 0;
+            uint32_t chunk = 0, gen = 0, nchunks = 0;
             for (uint32_t base = (uint32_t)s_lw; base < B && job < 0; base += 32) {
                 const uint32_t j = base + lane;
                 bool open = false, ok = false;
-                uint32_t nch = 0;
                 if (j < B) {
                     const unsigned long long w = ld_volatile(&P.qjobs[j].gen_claim);
-                    nch = P.qjobs[j].nchunks;
-                    open = (uint32_t)(w >> 32) != QDONE;
-                    ok = open && (uint32_t)w < nch;
+                    open = qw_gen(w) != QDONE;
+                    ok = open && (uint32_t)w < qw_nch(w);
                 }
                 const unsigned om = __ballot_sync(0xffffffffu, open);
                 if (first_open < 0 && om) first_open = (int)base + __ffs(om) - 1;
@@ -1654,11 +1675,11 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     unsigned long long old = 0ull;
                     if (lane == src) old = atomicAdd(&P.qjobs[j].gen_claim, 1ull);
                     old = __shfl_sync(0xffffffffu, old, src);
-                    const uint32_t ns = __shfl_sync(0xffffffffu, nch, src);
-                    if ((uint32_t)(old >> 32) != QDONE && (uint32_t)old < ns) {
+                    if (qw_gen(old) != QDONE && (uint32_t)old < qw_nch(old)) {
                         job = (int)base + src;
                         chunk = (uint32_t)old;
-                        gen = (uint32_t)(old >> 32);
+                        gen = qw_gen(old);
+                        nchunks = qw_nch(old);
                     }
                 }
             }
@@ -1668,6 +1689,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                 s_job = job;
                 s_chunk = chunk;
                 s_gen = gen;
+                s_nch = nchunks;
             }
         }
         __syncthreads();
@@ -1695,14 +1717,15 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         }
         if (tid == 0) idle_since = 0;
         const unsigned long long c0 = clock64();
-        const uint32_t chunk = s_chunk, gen = s_gen;
+        const uint32_t chunk = s_chunk, gen = s_gen, nchunks = s_nch;
         const AlignJob& jb = P.jobs[job];
         if (tid < NFR) sh.fr[tid] = __ldcg(P.qframe + (size_t)job * NFR + tid);
         if (tid == 0 && gen == 0 && chunk == 0) __stcg(&P.qctl[job].t_start, global_ns());
         __syncthreads();
         const float* pts = P.pts + 3 * jb.offset;
-        const uint32_t first = chunk * (uint32_t)P.qchunk;
-        const uint32_t last = min(jb.n, first + (uint32_t)P.qchunk);
+        const uint32_t csize = (jb.n + nchunks - 1u) / nchunks;  // this iteration's chunk size
+        const uint32_t first = min(jb.n, chunk * csize);
+        const uint32_t last = min(jb.n, first + csize);
         float acc[NACC];
 #pragma unroll
         for (int i = 0; i < A_HTR; ++i) acc[i] = 0.f;
@@ -1732,12 +1755,34 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         __syncthreads();
         if (tid == 0) {
             const uint32_t prev = atomicAdd(&P.qjobs[job].done, 1u);
-            s_flag = prev + 1u == P.qjobs[job].nchunks;
+            s_flag = prev + 1u == nchunks;
             atomicAdd(&P.qctl[job].cyc_chunks, (unsigned long long)(clock64() - c0));
         }
         __syncthreads();
         if (!s_flag) continue;
         __threadfence();  // acquire: every chunk's partials of this iteration are visible
+        // the iteration's sums, by the whole CTA in a fixed order: thread (value k, segment s)
+        // sums a contiguous run of chunks, then the segments are added in order
+        {
+            constexpr int NSEG = (THREADS / NRED) < MAX_WARPS ? (THREADS / NRED) : MAX_WARPS;
+            const uint32_t seg = (nchunks + NSEG - 1u) / NSEG;
+            const double* part0 = P.qpart + (size_t)P.qpart_off[job] * NRED;
+            if (tid < NSEG * NRED) {
+                const int k = tid % NRED, s = tid / NRED;
+                const uint32_t c_lo = min(nchunks, (uint32_t)s * seg);
+                const uint32_t c_hi = min(nchunks, c_lo + seg);
+                double v = 0.0;
+                for (uint32_t c = c_lo; c < c_hi; ++c) v += __ldcg(part0 + (size_t)c * NRED + k);
+                sh.warp_part[s][k] = v;
+            }
+            __syncthreads();
+            if (tid < NRED) {
+                double v = 0.0;
+                for (int s = 0; s < NSEG; ++s) v += sh.warp_part[s][tid];
+                sh.tot[tid] = v;
+            }
+            __syncthreads();
+        }
         if (warp == 0) queue_control<CPU_SEM>(P, sh, job, gen, lane);
     }
 }
@@ -1769,9 +1814,13 @@ static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t ch
             cache[{dev, smem}] = ctas;
         }
     }
-    k_queue_init<SEM><<<(p.num_jobs + 3) / 4, 128, 0, s>>>(p);
-    const unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)ctas, std::max(1u, chunks));
-    kern<<<grid, T, smem, s>>>(p);
+    // at most one CTA per chunk of the batch at the quarter chunk size
+    const unsigned grid =
+        (unsigned)std::min<uint64_t>((uint64_t)ctas, 4ull * std::max(1u, chunks));
+    AlignParams q = p;
+    q.qgrid = grid;
+    k_queue_init<SEM><<<(q.num_jobs + 3) / 4, 128, 0, s>>>(q);
+    kern<<<grid, T, smem, s>>>(q);
     return cudaGetLastError();
 }
 

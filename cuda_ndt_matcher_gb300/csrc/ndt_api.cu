@@ -800,10 +800,15 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
             hs[j] = s;
         }
         hq = (uint32_t*)((char*)c->h_jobs.p + jb + sjb);
-        uint64_t total = 0;
+        // partial-sum slots per alignment: its chunk count at the quarter chunk size (the
+        // most an iteration uses), capped at the 16-bit count of the claim word
+        const uint32_t small = chunk / 4;
+        uint64_t total = 0, full = 0;
         for (uint32_t j = 0; j < nj; ++j) {
             hq[j] = (uint32_t)total;
-            total += jobs[j].n ? (jobs[j].n + chunk - 1) / chunk : 1;
+            const uint64_t n = jobs[j].n;
+            total += std::min<uint64_t>(n ? (n + small - 1) / small : 1, QMAXCH);
+            full += std::min<uint64_t>(n ? (n + chunk - 1) / chunk : 1, QMAXCH);
         }
         if (total > 0xFFFFFFFFull) {
             set_error("too many chunks in one batch");
@@ -821,7 +826,7 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         p.qpart = (double*)c->d_qpart.p;
         p.qpart_off = (const uint32_t*)c->d_qoff.p;
         p.qcount = (uint32_t*)c->d_status.p + 2;  // word 2 of the status block
-        p.qchunks_total = (uint32_t)total;
+        p.qchunks_total = (uint32_t)full;
         c->stats.h2d_bytes += qob;
     }
     AlignOut* ho = (AlignOut*)c->h_aout.p;

@@ -122,8 +122,10 @@ struct AlignParams {
     double* qpart;
     const uint32_t* qpart_off;
     uint32_t* qcount;
-    int32_t qchunk;        // points per chunk (set by the launch from the shape)
-    uint32_t qchunks_total;  // chunks of one iteration of every alignment
+    int32_t qchunk;        // points per chunk (set by the launch from the shape); chunks of a
+                           // quarter of it near the end of a batch
+    uint32_t qchunks_total;  // chunks of one iteration of every alignment (at full size)
+    uint32_t qgrid;          // CTAs of the launch (set by the launch)
 };
 
 // Newton-kernel sums per iteration: 34 f32 per-thread accumulators (score, gradient and
@@ -133,11 +135,14 @@ constexpr int NRED = NACC + 1;
 
 // Work-queue kernel state, one per alignment (global memory).
 struct QJob {
-    unsigned long long gen_claim;  // iteration << 32 | chunks claimed (iteration QDONE: finished)
+    // iteration << 48 | the iteration's chunk count << 32 | chunks claimed (iteration QDONE:
+    // the alignment is finished)
+    unsigned long long gen_claim;
     uint32_t done;                 // chunks of the current iteration finished
-    uint32_t nchunks;
+    uint32_t pad;
 };
-constexpr uint32_t QDONE = 0xFFFFFFFFu;
+constexpr uint32_t QDONE = 0xFFFFu;
+constexpr uint32_t QMAXCH = 0xFFFFu;  // chunks per iteration at most (16-bit count)
 // Controller state of an alignment between iterations (FP64; read and written only by the
 // controller of the alignment's current iteration).
 struct QCtl {
