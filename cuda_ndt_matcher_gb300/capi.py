@@ -27,6 +27,7 @@ EXPORTS = [
     "ndt_set_target", "ndt_set_target_device", "ndt_map_info_get", "ndt_tile_put",
     "ndt_tile_remove", "ndt_tiles_commit", "ndt_tiles_status", "ndt_map_voxels",
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
+    "ndt_batch_submit", "ndt_batch_poll", "ndt_batch_wait",
     "ndt_autotune", "ndt_eval_batch", "ndt_batch_timings", "ndt_initial_pose_search",
     "ndt_pnet_config_default", "ndt_pnet_create", "ndt_pnet_destroy", "ndt_pnet_get_config",
     "ndt_pnet_add_map", "ndt_pnet_add_scan", "ndt_pnet_train", "ndt_pnet_propose",
@@ -159,6 +160,9 @@ def load(build_if_missing=True):
         "ndt_align": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(Result)]),
         "ndt_align_multi_pose": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
         "ndt_align_batch": (C.c_int, [P, P, C.c_uint64, P]),
+        "ndt_batch_submit": (C.c_int, [P, P, C.c_uint64, C.POINTER(C.c_uint64)]),
+        "ndt_batch_poll": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int32)]),
+        "ndt_batch_wait": (C.c_int, [P, C.c_uint64, P]),
         "ndt_align_batch_device": (C.c_int, [P, P, P, P, C.c_uint64, P]),
         "ndt_autotune": (C.c_int, [P, P, P, P, C.c_uint64, C.c_int32, C.POINTER(TuneResult)]),
         "ndt_eval_batch": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P, P]),
@@ -326,7 +330,8 @@ class Context:
                                             len(poses), res))
         return [result_dict(r) for r in res]
 
-    def align_batch(self, scans, poses):
+    @staticmethod
+    def _scan_array(scans, poses):
         scans = [as_xyz(s) for s in scans]
         m = len(scans)
         arr = (Scan * m)()
@@ -335,9 +340,30 @@ class Context:
             arr[i].num_points = len(s)
             for k in range(6):
                 arr[i].initial_pose[k] = float(pose[k])
+        return arr, m, scans
+
+    def align_batch(self, scans, poses):
+        arr, m, keep = self._scan_array(scans, poses)
         res = (Result * m)()
         check(self.lib.ndt_align_batch(self.h, arr, m, res))
         return [result_dict(r) for r in res]
+
+    def batch_submit(self, scans, poses):
+        """Queues a batch (AsyncBatchPipeline::submit); returns (ticket, number of scans)."""
+        arr, m, keep = self._scan_array(scans, poses)
+        t = C.c_uint64()
+        check(self.lib.ndt_batch_submit(self.h, arr, m, C.byref(t)))
+        return t.value, m
+
+    def batch_poll(self, ticket):
+        ready = C.c_int32()
+        check(self.lib.ndt_batch_poll(self.h, ticket[0], C.byref(ready)))
+        return bool(ready.value)
+
+    def batch_wait(self, ticket):
+        res = (Result * max(ticket[1], 1))()
+        check(self.lib.ndt_batch_wait(self.h, ticket[0], res))
+        return [result_dict(r) for r in res[:ticket[1]]]
 
     def align_batch_raw(self, scan_array, results):
         """Hot-path form: prebuilt (Scan * m) and (Result * m) arrays, no conversion."""

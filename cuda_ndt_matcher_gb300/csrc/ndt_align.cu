@@ -1706,6 +1706,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     } else if (now - idle_since > 2000000000ull) {
                         atomicOr(P.status, ST_QUEUE_STALL);
                         stop = 1;
+                    } else if (blockIdx.x >= gridDim.x / 4u && now - idle_since > 20000ull) {
+                        // near the end of a batch: all but a quarter of the grid (one CTA
+                        // per SM) leave after 20 us without work, so a kernel queued on
+                        // another stream (the next asynchronous batch) can take their SMs;
+                        // the quarter that stays serves the remaining iterations
+                        stop = 1;
                     }
                 }
                 s_flag = stop;

@@ -159,9 +159,34 @@ private:
     bool quit_ = false, started_ = false;
 };
 
+// A batch between its enqueue and its completion.
+struct PendingAlign {
+    std::vector<AlignJob> jobs;        // in launch order (largest scans first)
+    std::vector<uint64_t> n_by_slot;   // points of each of the caller's scans
+    int max_iter = 0;
+    bool cpu = false;
+    size_t ob = 0, sob = 0;            // byte offsets of the score outputs and status word
+    bool active = false;
+};
+
+struct ndt_ctx;
+
+// Asynchronous batches (ndt_batch_submit / ndt_batch_wait): each slot is an internal context
+// with its own stream, buffers and pinned staging, aligning against its owner's map.
+struct AsyncSlot {
+    ndt_ctx* ctx = nullptr;
+    uint64_t ticket = 0;               // 0: free
+    uint64_t m = 0;
+};
+constexpr int MAX_ASYNC_SLOTS = 3;
+
 struct ndt_ctx {
     HostPool pool;
     ndt_config cfg{};
+    PendingAlign pend;
+    AsyncSlot slots[MAX_ASYNC_SLOTS];
+    uint64_t next_ticket = 0;
+    bool borrowed_map = false;         // an async slot: map.view belongs to the owner
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
@@ -208,14 +233,23 @@ struct ndt_ctx {
     std::string build_err;
 };
 
+// Waits for the asynchronous batches in flight (their results stay for ndt_batch_wait): the
+// map they read must not change under them.
+static void async_drain(ndt_ctx* c) {
+    for (auto& s : c->slots)
+        if (s.ticket && s.ctx) cudaStreamSynchronize(s.ctx->stream);
+}
+
 // Finishes a background rebuild: joins its thread and, when it succeeded, makes the standby
-// map the active one (alignment work on the old map has completed: every call synchronises).
+// map the active one (alignment work on the old map has completed: every call synchronises,
+// and asynchronous batches are drained first).
 static void tiles_settle(ndt_ctx* c, bool wait) {
     if (!c->builder.joinable()) return;
     if (!wait && c->build_state.load() != 2) return;
     c->builder.join();
     c->build_state.store(0);
     if (c->build_rc == 0) {
+        async_drain(c);
         std::swap(c->map, c->map_b);
         c->map_b.valid = false;
         c->map_gen++;
@@ -380,6 +414,9 @@ int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
 int ndt_ctx_destroy(ndt_ctx* c) {
     if (!c) return NDT_OK;
     cudaSetDevice(c->device);
+    async_drain(c);
+    for (auto& s : c->slots)
+        if (s.ctx) ndt_ctx_destroy(s.ctx);  // a slot's map is borrowed: its Map owns nothing
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->builder.joinable()) c->builder.join();
     for (auto& t : c->tiles) dev_free(t.pts);
@@ -480,6 +517,7 @@ int ndt_stats_reset(ndt_ctx* c) {
 
 static int set_target_dev(ndt_ctx* c, const float* d_xyz, uint64_t n) {
     tiles_settle(c, true);
+    async_drain(c);  // batches in flight read the map being rebuilt in place
     c->map.valid = false;
     c->map_gen++;  // captured batches bake the map in
     float ms = 0.f;
@@ -563,6 +601,7 @@ int ndt_tile_remove(ndt_ctx* c, uint64_t tile_id) {
 int ndt_tiles_commit(ndt_ctx* c, int32_t wait) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
     tiles_settle(c, true);  // one rebuild at a time
+    async_drain(c);         // the rebuild reuses the standby map's buffers
     uint64_t total = 0;
     for (auto& t : c->tiles) total += t.n;
     if (total == 0) {
@@ -717,10 +756,13 @@ static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
     return sh;
 }
 
-// Core: align jobs whose points are already at d_pts (device, concatenated).
-static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
-                     const std::vector<uint64_t>& n_by_slot, ndt_result* out) {
+// Core: align jobs whose points are already at d_pts (device, concatenated). Enqueues the
+// batch on the context's stream (job tables in, Newton kernel, NVTL scoring, results out)
+// and records what run_align_finish needs in c->pend.
+static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
+                             const std::vector<uint64_t>& n_by_slot) {
     uint32_t nj = (uint32_t)jobs.size();
+    c->pend.active = false;
     if (nj == 0) return NDT_OK;
     std::stable_sort(jobs.begin(), jobs.end(),
                      [](const AlignJob& a, const AlignJob& b) { return a.n > b.n; });
@@ -900,11 +942,36 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
         return rc;
     }
     c->stats.d2h_bytes += ob + sob + 4;
-    if ((rc = cuda_fail(cudaStreamSynchronize(st), "align"))) return rc;
+    PendingAlign& pd = c->pend;
+    pd.jobs = jobs;
+    pd.n_by_slot = n_by_slot;
+    pd.max_iter = p.max_iter;
+    pd.cpu = cpu;
+    pd.ob = ob;
+    pd.sob = sob;
+    pd.active = true;
+    return NDT_OK;
+}
+
+// Waits for the batch run_align_enqueue put on the stream and writes its results (caller's
+// order) to out.
+static int run_align_finish(ndt_ctx* c, ndt_result* out) {
+    PendingAlign& pd = c->pend;
+    if (!pd.active) return NDT_OK;
+    pd.active = false;
+    int rc;
+    const std::vector<AlignJob>& jobs = pd.jobs;
+    const std::vector<uint64_t>& n_by_slot = pd.n_by_slot;
+    const uint32_t nj = (uint32_t)jobs.size();
+    const bool cpu = pd.cpu;
+    const AlignOut* ho = (const AlignOut*)c->h_aout.p;
+    const ScoreOut* hso = (const ScoreOut*)((char*)c->h_aout.p + pd.ob);
+    const uint32_t* hst = (const uint32_t*)((char*)c->h_aout.p + pd.ob + pd.sob);
+    if ((rc = cuda_fail(cudaStreamSynchronize(c->stream), "align"))) return rc;
     if ((rc = check_status(c, *hst))) return rc;
     if (c->trace) {
-        c->trace_iters = p.max_iter;
-        c->h_trace.resize((size_t)nj * p.max_iter * TRACE_REC);
+        c->trace_iters = pd.max_iter;
+        c->h_trace.resize((size_t)nj * pd.max_iter * TRACE_REC);
         cudaMemcpy(c->h_trace.data(), c->d_trace.p, c->h_trace.size() * sizeof(double),
                    cudaMemcpyDeviceToHost);
         c->trace_slot.resize(nj);
@@ -953,6 +1020,12 @@ static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs
     return NDT_OK;
 }
 
+static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
+                     const std::vector<uint64_t>& n_by_slot, ndt_result* out) {
+    const int rc = run_align_enqueue(c, d_pts, jobs, n_by_slot);
+    return rc ? rc : run_align_finish(c, out);
+}
+
 static int need_target(ndt_ctx* c) {
     tiles_settle(c, false);
     if (!c->map.valid) {
@@ -964,16 +1037,16 @@ static int need_target(ndt_ctx* c) {
 
 extern "C" {
 
-int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* out) {
-    if (!c || (!scans && m) || (!out && m)) return NDT_ERR_INVALID_ARGUMENT;
-    int rc = need_target(c);
-    if (rc) return rc;
-    if (m == 0) return NDT_OK;
+}  // extern "C"
+
+// Host scans of a batch: checked, staged into x's pinned buffer and copied to x->d_in on x's
+// stream (copies in flight on return), and described as jobs.
+static int prepare_batch(ndt_ctx* x, const ndt_scan* scans, uint64_t m,
+                         std::vector<AlignJob>& jobs, std::vector<uint64_t>& ns) {
     if (m > 0xFFFFFFull) {
         set_error("too many scans in one batch");
         return NDT_ERR_CAPACITY;
     }
-    cudaSetDevice(c->device);
     uint64_t total = 0;
     for (uint64_t i = 0; i < m; ++i) {
         if (scans[i].num_points && !scans[i].xyz) return NDT_ERR_INVALID_ARGUMENT;
@@ -983,10 +1056,12 @@ int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* o
         }
         total += scans[i].num_points;
     }
-    if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
+    int rc;
+    if ((rc = pin_reserve(x->h_pts, total * 12 + 16)) || (rc = dev_reserve(x->d_in, total * 12 + 16)))
         return rc;
-    std::vector<AlignJob> jobs(m);
-    std::vector<uint64_t> ns(m), offset(m);
+    jobs.assign(m, AlignJob{});
+    ns.assign(m, 0);
+    std::vector<uint64_t> offset(m);
     uint64_t off = 0;
     for (uint64_t i = 0; i < m; ++i) {
         jobs[i].offset = offset[i] = off;
@@ -996,8 +1071,118 @@ int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* o
         ns[i] = scans[i].num_points;
         off += scans[i].num_points;
     }
-    stage_scans(c, scans, m, offset, total);
+    stage_scans(x, scans, m, offset, total);
+    return NDT_OK;
+}
+
+static void stats_add(ndt_stats& a, const ndt_stats& b) {
+    a.align_launches += b.align_launches;
+    a.alignments += b.alignments;
+    a.iterations += b.iterations;
+    a.point_iterations += b.point_iterations;
+    a.correspondences += b.correspondences;
+    a.align_kernel_ms += b.align_kernel_ms;
+    a.score_launches += b.score_launches;
+    a.score_kernel_ms += b.score_kernel_ms;
+    a.build_launches += b.build_launches;
+    a.build_ms += b.build_ms;
+    a.h2d_bytes += b.h2d_bytes;
+    a.d2h_bytes += b.d2h_bytes;
+    a.cycles_points += b.cycles_points;
+    a.cycles_cluster_wait += b.cycles_cluster_wait;
+    a.cycles_control += b.cycles_control;
+    a.cycles_broadcast += b.cycles_broadcast;
+    a.eigen_solves += b.eigen_solves;
+}
+
+static AsyncSlot* find_ticket(ndt_ctx* c, uint64_t ticket) {
+    for (auto& s : c->slots)
+        if (ticket && s.ticket == ticket) return &s;
+    set_error("no asynchronous batch with that ticket");
+    return nullptr;
+}
+
+extern "C" {
+
+int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* out) {
+    if (!c || (!scans && m) || (!out && m)) return NDT_ERR_INVALID_ARGUMENT;
+    int rc = need_target(c);
+    if (rc) return rc;
+    if (m == 0) return NDT_OK;
+    cudaSetDevice(c->device);
+    std::vector<AlignJob> jobs;
+    std::vector<uint64_t> ns;
+    if ((rc = prepare_batch(c, scans, m, jobs, ns))) return rc;
     return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
+}
+
+int ndt_batch_submit(ndt_ctx* c, const ndt_scan* scans, uint64_t m, uint64_t* ticket) {
+    if (!c || !ticket || (!scans && m)) return NDT_ERR_INVALID_ARGUMENT;
+    *ticket = 0;
+    int rc = need_target(c);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    AsyncSlot* s = nullptr;
+    for (auto& x : c->slots)
+        if (x.ticket == 0) {
+            s = &x;
+            break;
+        }
+    if (!s) {
+        set_error("every asynchronous slot holds a batch: wait for one first");
+        return NDT_ERR_CAPACITY;
+    }
+    if (!s->ctx) {
+        if ((rc = ndt_ctx_create(&c->cfg, &s->ctx))) return rc;
+        s->ctx->borrowed_map = true;
+    }
+    ndt_ctx* x = s->ctx;
+    // the owner's map (borrowed, never freed by the slot), parameters and tuned shapes
+    x->cfg = c->cfg;
+    x->cfg_gen = c->cfg_gen;
+    x->d1 = c->d1;
+    x->d2 = c->d2;
+    x->tuned = c->tuned;
+    x->map.view = c->map.view;
+    x->map.info = c->map.info;
+    x->map.valid = true;
+    x->map_gen = c->map_gen;
+    x->trace = false;
+    std::vector<AlignJob> jobs;
+    std::vector<uint64_t> ns;
+    if ((rc = prepare_batch(x, scans, m, jobs, ns))) return rc;
+    if ((rc = run_align_enqueue(x, (const float*)x->d_in.p, jobs, ns))) return rc;
+    s->ticket = ++c->next_ticket;
+    s->m = m;
+    *ticket = s->ticket;
+    return NDT_OK;
+}
+
+int ndt_batch_poll(ndt_ctx* c, uint64_t ticket, int32_t* ready) {
+    if (!c || !ready) return NDT_ERR_INVALID_ARGUMENT;
+    AsyncSlot* s = find_ticket(c, ticket);
+    if (!s) return NDT_ERR_INVALID_ARGUMENT;
+    const cudaError_t e = cudaStreamQuery(s->ctx->stream);
+    *ready = e == cudaSuccess;
+    if (e == cudaErrorNotReady) return NDT_OK;
+    return cuda_fail(e, "batch poll");
+}
+
+int ndt_batch_wait(ndt_ctx* c, uint64_t ticket, ndt_result* out) {
+    if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    AsyncSlot* s = find_ticket(c, ticket);
+    if (!s) return NDT_ERR_INVALID_ARGUMENT;
+    if (s->m && !out) return NDT_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    ndt_ctx* x = s->ctx;
+    const int rc = run_align_finish(x, out);
+    stats_add(c->stats, x->stats);
+    std::memset(&x->stats, 0, sizeof x->stats);
+    c->t_start_ms = x->t_start_ms;
+    c->t_finish_ms = x->t_finish_ms;
+    s->ticket = 0;
+    s->m = 0;
+    return rc;
 }
 
 int ndt_batch_timings(ndt_ctx* c, double* start_ms, double* finish_ms, uint64_t n) {

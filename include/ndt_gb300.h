@@ -202,8 +202,25 @@ int ndt_align(ndt_ctx* ctx, const float* xyz, uint64_t num_points, const double 
 int ndt_align_multi_pose(ndt_ctx* ctx, const float* xyz, uint64_t num_points,
                          const double* poses_in, uint64_t num_poses, ndt_result* out);
 /* NdtScanMatcher::align_parallel_scans (src/ndt_cuda/src/ndt.rs:1224-1321): uneven scans
- * aligned in one launch (one thread-block cluster per alignment). */
+ * aligned in one launch (one thread-block cluster per alignment, or the work-queue kernel). */
 int ndt_align_batch(ndt_ctx* ctx, const ndt_scan* scans, uint64_t num_scans, ndt_result* out);
+
+/* Asynchronous batches: AsyncBatchPipeline::submit / poll / wait
+ * (src/ndt_cuda/src/optimization/async_pipeline.rs:348-615), the double-buffered feed of
+ * the scan queue (src/cuda_ndt_matcher/src/scan_queue.rs). Up to 3 batches in flight per
+ * context, each on its own stream with its own staging and device buffers, aligned against
+ * the context's map as ndt_align_batch would align them (same results).
+ *   - ndt_batch_submit stages the scans (the caller's arrays may be reused on return),
+ *     queues the copies and kernels, and returns a ticket; NDT_ERR_CAPACITY when 3 batches
+ *     wait to be collected.
+ *   - ndt_batch_poll sets *ready to 1 once the batch has finished (non-blocking).
+ *   - ndt_batch_wait blocks until the batch has finished, writes its num_scans results and
+ *     frees the slot; the context's stats and ndt_batch_timings then include it.
+ * Calls that change the map (set_target, tile commits) first wait for the batches in
+ * flight; their results stay available to ndt_batch_wait. */
+int ndt_batch_submit(ndt_ctx* ctx, const ndt_scan* scans, uint64_t num_scans, uint64_t* ticket);
+int ndt_batch_poll(ndt_ctx* ctx, uint64_t ticket, int32_t* ready);
+int ndt_batch_wait(ndt_ctx* ctx, uint64_t ticket, ndt_result* out);
 /* Same, with the scans already resident on the device, concatenated: scan i is
  * d_xyz[3*offsets[i] .. 3*offsets[i+1]); offsets and poses are host arrays. */
 int ndt_align_batch_device(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,
