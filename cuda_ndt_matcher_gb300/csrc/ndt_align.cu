@@ -604,9 +604,10 @@ __device__ __forceinline__ void transform_point(const float* fr, const float* pv
 // dy, dz inner); the slots of the accepted voxels (centroid within one resolution, at most
 // max_nb) are listed in shared memory (nbl[k * nbl_stride]), so the search runs with all
 // lanes busy and the pair work runs once per listed voxel rather than once per cell.
-// Returns the number listed.
-__device__ __forceinline__ int search_point(const MapView& m, const float* qh, const float* ql,
-                                            int max_nb, uint32_t* nbl, int nbl_stride) {
+// Returns the number listed. off27: the CTA's table of neighbour offsets (nbhd_offsets).
+__device__ __forceinline__ int search_point(const MapView& m, const uint32_t* off27,
+                                            const float* qh, const float* ql, int max_nb,
+                                            uint32_t* nbl, int nbl_stride) {
     int32_t gc[3];
     cell_of_sum(m, qh, ql, gc);
     int cnt = 0;
@@ -622,8 +623,8 @@ __device__ __forceinline__ int search_point(const MapView& m, const float* qh, c
             float4 e[NB_BATCH];
 #pragma unroll
             for (int k = 0; k < NB_BATCH; ++k) {
-                const uint32_t b = (uint32_t)(__ffs(bits) - 1);  // 0xFFFFFFFF when empty
-                e[k] = bits != 0u ? __ldg(m.grid + nbhd_index(m, corner, b))
+                const uint32_t b = (uint32_t)(__ffs(bits) - 1) & 31u;  // 31 when empty
+                e[k] = bits != 0u ? __ldg(m.grid + (corner + off27[b]))
                                   : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                 bits &= bits - 1u;
             }
@@ -689,14 +690,15 @@ __device__ __forceinline__ int search_point(const MapView& m, const float* qh, c
 // (they change once per point; keeping them out of registers leaves the search and pair
 // work room without spilling to local memory)
 template <bool CPU_SEM>
-__device__ __forceinline__ void point_terms(const MapView& m, float px, float py, float pz,
+__device__ __forceinline__ void point_terms(const MapView& m, const uint32_t* off27,
+                                            float px, float py, float pz,
                                             const float* fr, int max_nb, float d1f, float d2f,
                                             float* acc, float* sacc, int& ncorr, uint32_t* nbl,
                                             int nbl_stride) {
     const float pv[3] = {px, py, pz};
     float qh[3], ql[3];
     transform_point(fr, pv, qh, ql);
-    const int cnt = search_point(m, qh, ql, max_nb, nbl, nbl_stride);
+    const int cnt = search_point(m, off27, qh, ql, max_nb, nbl, nbl_stride);
     if (cnt == 0) return;
     // ---- pairs: S, G, M aggregated over the listed voxels
     float S = 0.f, G0 = 0.f, G1 = 0.f, G2 = 0.f;
@@ -779,14 +781,15 @@ __device__ __forceinline__ void point_terms(const MapView& m, float px, float py
 // Line-search terms of one point at a candidate pose (graph semantics; the candidate pass of
 // ndt_graph_linesearch_kernel, ndt_graph_kernels.cu:473-570): score and gradient only, as the
 // accumulators S (a[0]), G (a[1..3]) and G p^T (a[4..12]) of point_terms, same arithmetic.
-__device__ __forceinline__ void point_terms_ls(const MapView& m, float px, float py, float pz,
+__device__ __forceinline__ void point_terms_ls(const MapView& m, const uint32_t* off27,
+                                               float px, float py, float pz,
                                                const float* fr, int max_nb, float d1f, float d2f,
                                                float* a, int& ncorr, uint32_t* nbl,
                                                int nbl_stride) {
     const float pv[3] = {px, py, pz};
     float qh[3], ql[3];
     transform_point(fr, pv, qh, ql);
-    const int cnt = search_point(m, qh, ql, max_nb, nbl, nbl_stride);
+    const int cnt = search_point(m, off27, qh, ql, max_nb, nbl, nbl_stride);
     if (cnt == 0) return;
     float S = 0.f, G[3] = {0.f, 0.f, 0.f};
     const float d1d2 = d1f * d2f;
@@ -1163,6 +1166,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_align(const AlignParams P) {
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
+    __shared__ uint32_t s_off27[32];  // neighbour offsets of the dense index
     // dynamic shared memory: [max_nb][THREADS] accepted slots per thread, then the trailing
     // NACC - A_HTR accumulators [NACC - A_HTR][THREADS], then the line search's warp sums
     extern __shared__ uint32_t nbl_smem[];
@@ -1194,6 +1198,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         sh.done = 0;
         sh.solve.have_w = 0;
     }
+    nbhd_offsets(m, s_off27);
     __syncthreads();
     if (warp == 0) make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
     __syncthreads();
@@ -1217,7 +1222,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                   pz = __ldg(pts + 3 * (size_t)i + 2);
             if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-            point_terms<CPU_SEM>(m, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
+            point_terms<CPU_SEM>(m, s_off27, px, py, pz, fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
                                  nbl_smem + tid, THREADS);
         }
 #pragma unroll
@@ -1348,7 +1353,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                           pz = __ldg(pts + 3 * (size_t)i + 2);
                     if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-                    point_terms_ls(m, px, py, pz, sh.ls_fr[c], P.max_nb, P.d1f, P.d2f, a, lc,
+                    point_terms_ls(m, s_off27, px, py, pz, sh.ls_fr[c], P.max_nb, P.d1f, P.d2f, a, lc,
                                    nbl_smem + tid, THREADS);
                 }
                 double* wout = lsw + ((size_t)warp * LS_MAX + c) * LS_VALS;
@@ -1640,6 +1645,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_queue(const AlignParams P) {
     constexpr int NW = THREADS / 32;
     __shared__ AlignShared sh;
+    __shared__ uint32_t s_off27[32];  // neighbour offsets of the dense index
     __shared__ int s_job, s_lw, s_flag;
     __shared__ uint32_t s_chunk, s_gen, s_nch;
     // dynamic shared memory as in k_ndt_align: neighbour lists, then the trailing accumulators
@@ -1651,6 +1657,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     const uint32_t B = P.num_jobs;
     uint64_t idle_since = 0;  // thread 0
     if (tid == 0) s_lw = 0;
+    nbhd_offsets(m, s_off27);  // read after the loop's first barrier
     for (;;) {
         __syncthreads();  // the previous chunk (and controller) is finished with shared memory
         if (warp == 0) {
@@ -1742,7 +1749,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                   pz = __ldg(pts + 3 * (size_t)i + 2);
             if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-            point_terms<CPU_SEM>(m, px, py, pz, sh.fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
+            point_terms<CPU_SEM>(m, s_off27, px, py, pz, sh.fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
                                  nbl_smem + tid, THREADS);
         }
 #pragma unroll

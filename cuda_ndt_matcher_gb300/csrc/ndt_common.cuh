@@ -80,6 +80,15 @@ __device__ __forceinline__ uint32_t nbhd_index(const MapView& m, uint32_t corner
     return corner + (b / 9u) * (m.ext[1] * m.ext[2]) + (b / 3u % 3u) * m.ext[2] + b % 3u;
 }
 
+// The 27 offsets nbhd_index adds to the corner, by mask bit, written once per CTA to a
+// 32-entry shared table (entries 27..31 zero, so any 5-bit index reads in bounds): a search
+// then finds a neighbour with one shared load and an add. The caller synchronises the block
+// before the table is read.
+__device__ __forceinline__ void nbhd_offsets(const MapView& m, uint32_t* off32) {
+    for (int b = threadIdx.x; b < 32; b += blockDim.x)
+        off32[b] = b < 27 ? nbhd_index(m, 0u, (uint32_t)b) : 0u;
+}
+
 // Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).
 __host__ __device__ __forceinline__ uint64_t pack21(int32_t gx, int32_t gy, int32_t gz) {
     uint64_t ux = (uint64_t)(int64_t)(gx + (1 << 20));

@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
     __shared__ float Th[12], Tl[12];
     __shared__ double red[ST / 32][2];
     __shared__ unsigned long long redc[ST / 32][2];
+    __shared__ uint32_t s_off[32];  // neighbour offsets of the dense index
+    nbhd_offsets(m, s_off);         // read after the barrier below
     const ScoreJob job = jobs[blockIdx.y];
     const size_t pidx = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
     const uint32_t first = blockIdx.x * SCHUNK;
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
             while (bits != 0u) {
                 const uint32_t b = (uint32_t)(__ffs(bits) - 1);
                 bits &= bits - 1u;
-                const float4 e = __ldg(m.grid + nbhd_index(m, corner, b));
+                const float4 e = __ldg(m.grid + (corner + s_off[b]));
                 visit(__float_as_int(e.w), e.x, e.y, e.z);
             }
         } else {
