@@ -1452,9 +1452,17 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
 // sums the partials in chunk order, so results do not depend on which CTA ran which chunk.
 // No CTA ever waits for another; a CTA that finds nothing to claim polls, and gives up with a
 // status bit after 2 s without work (every alignment ends within max_iterations steps).
+// Host batches may still be copying in when the kernel starts (P.qarrive): the points are laid
+// out largest alignment first, in copy chunks that start on 768-byte boundaries, and a copy
+// stream writes the count of resident points after each chunk. An alignment's first
+// iteration is claimable once its last point is resident; the chunks' alignment keeps every
+// L1 line a CTA reads inside chunks already copied.
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
     return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+__device__ __forceinline__ uint32_t ld_volatile32(const uint32_t* p) {
+    return *reinterpret_cast<const volatile uint32_t*>(p);
 }
 
 // Claim word of an alignment: iteration (16 bits; QDONE once finished), the iteration's chunk
@@ -1655,7 +1663,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const MapView& m = P.map;
     const uint32_t B = P.num_jobs;
-    uint64_t idle_since = 0;  // thread 0
+    uint64_t idle_since = 0;    // thread 0
+    uint32_t seen_arrive = 0;   // thread 0: last value of the input counter seen
     if (tid == 0) s_lw = 0;
     nbhd_offsets(m, s_off27);  // read after the loop's first barrier
     for (;;) {
@@ -1665,6 +1674,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
             // a time, and try the claimable ones in order
             int job = -1, first_open = -1;
             uint32_t chunk = 0, gen = 0, nchunks = 0;
+            // points resident while the batch is still being copied in (all: ~0)
+            uint32_t arrived = 0xFFFFFFFFu;
+            if (P.qarrive) {
+                arrived = ld_volatile32(P.qarrive);
+                if (arrived >= P.qarrive_total) arrived = 0xFFFFFFFFu;
+            }
             for (uint32_t base = (uint32_t)s_lw; base < B && job < 0; base += 32) {
                 const uint32_t j = base + lane;
                 bool open = false, ok = false;
@@ -1672,6 +1687,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     const unsigned long long w = ld_volatile(&P.qjobs[j].gen_claim);
                     open = qw_gen(w) != QDONE;
                     ok = open && (uint32_t)w < qw_nch(w);
+                    if (ok && arrived != 0xFFFFFFFFu && qw_gen(w) == 0u)
+                        ok = P.jobs[j].offset + P.jobs[j].n <= (uint64_t)arrived;
                 }
                 const unsigned om = __ballot_sync(0xffffffffu, open);
                 if (first_open < 0 && om) first_open = (int)base + __ffs(om) - 1;
@@ -1708,12 +1725,22 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                 int stop = s_lw >= (int)B;
                 if (!stop) {
                     const uint64_t now = global_ns();
+                    bool fed = true;  // every point of the batch is resident
+                    if (P.qarrive) {
+                        const uint32_t a = ld_volatile32(P.qarrive);
+                        fed = a >= P.qarrive_total;
+                        if (a != seen_arrive) {  // input still arriving: not a stall
+                            seen_arrive = a;
+                            idle_since = 0;
+                        }
+                    }
                     if (idle_since == 0) {
                         idle_since = now;
                     } else if (now - idle_since > 2000000000ull) {
                         atomicOr(P.status, ST_QUEUE_STALL);
                         stop = 1;
-                    } else if (blockIdx.x >= gridDim.x / 4u && now - idle_since > 20000ull) {
+                    } else if (fed && blockIdx.x >= gridDim.x / 4u &&
+                               now - idle_since > 20000ull) {
                         // near the end of a batch: all but a quarter of the grid (one CTA
                         // per SM) leave after 20 us without work, so a kernel queued on
                         // another stream (the next asynchronous batch) can take their SMs;

@@ -169,6 +169,16 @@ struct PendingAlign {
     bool active = false;
 };
 
+// Host scans of a batch laid out for copying in: the jobs are in launch order (largest scan
+// first), job j's points go to jobs[j].offset, and the copy runs in chunks of jobs
+// [chunk_job[k], chunk_job[k + 1]) of 1 MB doubling to 16 MB, each starting on a 64-point
+// (768-byte) boundary.
+struct StagePlan {
+    const ndt_scan* scans = nullptr;
+    std::vector<uint32_t> chunk_job;   // first job of each chunk, then the job count
+    uint64_t total = 0;                // end of the last job's points (padding included)
+};
+
 struct ndt_ctx;
 
 // Asynchronous batches (ndt_batch_submit / ndt_batch_wait): each slot is an internal context
@@ -190,10 +200,12 @@ struct ndt_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t cstream = nullptr;  // host batches copied in while the work-queue kernel runs
+    cudaEvent_t ev_in0 = nullptr, ev_in1 = nullptr;  // counter reset / last chunk copied
     Map map;
     BuildScratch bs;
     DevBuf d_in, d_jobs, d_aout, d_sjobs, d_sout, d_part, d_status, d_q, d_qidx, d_qcnt;
-    PinBuf h_pts, h_jobs, h_aout, h_sjobs, h_sout, h_misc;
+    PinBuf h_pts, h_jobs, h_aout, h_sjobs, h_sout, h_misc, h_arrive;
     double d1 = 0, d2 = 0;
     ndt_stats stats{};
     bool profile = false;
@@ -280,6 +292,34 @@ static void stage_scans(ndt_ctx* c, const ndt_scan* scans, uint64_t m,
         i0 = i1;
     }
     c->stats.h2d_bytes += total * 12;
+}
+
+// Copies a planned batch to c->d_in on stream s, chunk by chunk: the context's host threads
+// pack a chunk into the pinned buffer, then its copy is issued (overlapping the packing of the
+// next). With d_arrive, a 4-byte copy after each chunk sets that device word to the points
+// resident so far (c->h_arrive holds one value per chunk and is reserved by the caller).
+static void stage_plan(ndt_ctx* c, const StagePlan& pl, const std::vector<AlignJob>& jobs,
+                       cudaStream_t s, uint32_t* d_arrive) {
+    char* hp = (char*)c->h_pts.p;
+    uint32_t* ha = (uint32_t*)c->h_arrive.p;
+    for (size_t k = 0; k + 1 < pl.chunk_job.size(); ++k) {
+        const uint32_t a = pl.chunk_job[k], b = pl.chunk_job[k + 1];
+        c->pool.run(b - a, [&](uint64_t t) {
+            const AlignJob& jb = jobs[a + t];
+            if (jb.n) std::memcpy(hp + jb.offset * 12, pl.scans[jb.slot].xyz, (size_t)jb.n * 12);
+        });
+        const uint64_t o0 = jobs[a].offset, o1 = jobs[b - 1].offset + jobs[b - 1].n;
+        if (o1 > o0) {
+            cudaMemcpyAsync((char*)c->d_in.p + o0 * 12, hp + o0 * 12, (o1 - o0) * 12,
+                            cudaMemcpyHostToDevice, s);
+            c->stats.h2d_bytes += (o1 - o0) * 12;
+        }
+        if (d_arrive) {
+            ha[k] = (uint32_t)o1;
+            cudaMemcpyAsync(d_arrive, ha + k, 4, cudaMemcpyHostToDevice, s);
+            c->stats.h2d_bytes += 4;
+        }
+    }
 }
 
 static void drop_graphs(ndt_ctx* c) {
@@ -398,6 +438,9 @@ int ndt_ctx_create(const ndt_config* cfg, ndt_ctx** out) {
     cudaEventCreate(&x->ev2);
     cudaEventCreate(&x->ev3);
     cudaStreamCreateWithFlags(&x->bstream, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&x->cstream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&x->ev_in0, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&x->ev_in1, cudaEventDisableTiming);
     int rc = dev_reserve(x->d_status, 16);
     if (!rc) rc = dev_reserve(x->d_status_b, 16);
     if (rc) {
@@ -418,6 +461,7 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     for (auto& s : c->slots)
         if (s.ctx) ndt_ctx_destroy(s.ctx);  // a slot's map is borrowed: its Map owns nothing
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->cstream) cudaStreamSynchronize(c->cstream);
     if (c->builder.joinable()) c->builder.join();
     for (auto& t : c->tiles) dev_free(t.pts);
     for (DevBuf* b : {&c->map_b.slots, &c->map_b.slot_icov, &c->map_b.slot_vidx, &c->map_b.grid,
@@ -441,10 +485,12 @@ int ndt_ctx_destroy(ndt_ctx* c) {
                       &c->d_qcnt, &c->d_trace, &c->d_qjobs, &c->d_qctl, &c->d_qframe,
                       &c->d_qpart, &c->d_qoff})
         dev_free(*b);
-    for (PinBuf* b : {&c->h_pts, &c->h_jobs, &c->h_aout, &c->h_sjobs, &c->h_sout, &c->h_misc})
+    for (PinBuf* b : {&c->h_pts, &c->h_jobs, &c->h_aout, &c->h_sjobs, &c->h_sout, &c->h_misc,
+                      &c->h_arrive})
         pin_free(*b);
-    for (cudaEvent_t ev : {c->ev0, c->ev1, c->ev2, c->ev3})
+    for (cudaEvent_t ev : {c->ev0, c->ev1, c->ev2, c->ev3, c->ev_in0, c->ev_in1})
         if (ev) cudaEventDestroy(ev);
+    if (c->cstream) cudaStreamDestroy(c->cstream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return NDT_OK;
@@ -756,11 +802,15 @@ static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
     return sh;
 }
 
-// Core: align jobs whose points are already at d_pts (device, concatenated). Enqueues the
-// batch on the context's stream (job tables in, Newton kernel, NVTL scoring, results out)
-// and records what run_align_finish needs in c->pend.
+// Core: align jobs whose points are at d_pts (device, concatenated), or, with a plan, host
+// scans that are copied to d_pts (c->d_in) first. Enqueues the batch on the context's stream
+// (job tables in, Newton kernel, NVTL scoring, results out) and records what
+// run_align_finish needs in c->pend. With the work-queue kernel, a planned batch of more than
+// one copy chunk is copied in on c->cstream while the kernel already runs (see k_ndt_queue);
+// otherwise its copies precede the launch on the stream.
 static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
-                             const std::vector<uint64_t>& n_by_slot) {
+                             const std::vector<uint64_t>& n_by_slot,
+                             const StagePlan* plan = nullptr) {
     uint32_t nj = (uint32_t)jobs.size();
     c->pend.active = false;
     if (nj == 0) return NDT_OK;
@@ -874,6 +924,18 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
     AlignOut* ho = (AlignOut*)c->h_aout.p;
     ScoreOut* hso = (ScoreOut*)((char*)c->h_aout.p + ob);
     uint32_t* hst = (uint32_t*)((char*)c->h_aout.p + ob + sob);
+    // host batch copied in during the launch: the kernel reads the resident-point count from
+    // word 3 of the status block (32-bit: the batch holds fewer than 2^32 points)
+    const bool stream_in = plan && shape.queue > 0 && !c->trace &&
+                           plan->chunk_job.size() > 2 && plan->total < 0xFFFFFFFFull;
+    if (plan && !stream_in) stage_plan(c, *plan, jobs, st, nullptr);
+    uint32_t* d_arrive = nullptr;
+    if (stream_in) {
+        if ((rc = pin_reserve(c->h_arrive, plan->chunk_job.size() * 4))) return rc;
+        d_arrive = (uint32_t*)c->d_status.p + 3;
+        p.qarrive = d_arrive;
+        p.qarrive_total = (uint32_t)plan->total;
+    }
     // the batch on the stream: job tables in, Newton kernel, NVTL scoring, results out (the
     // events are graph nodes when captured)
     auto enqueue = [&](unsigned evf) -> int {
@@ -881,12 +943,20 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
         cudaMemcpyAsync(c->d_sjobs.p, hs, sjb, cudaMemcpyHostToDevice, st);
         if (shape.queue > 0) {
             cudaMemcpyAsync(c->d_qoff.p, hq, qob, cudaMemcpyHostToDevice, st);
-            cudaMemsetAsync(p.qcount, 0, 4, st);
+            cudaMemsetAsync(p.qcount, 0, d_arrive ? 8 : 4, st);  // words 2 (and 3)
         }
+        if (d_arrive) cudaEventRecord(c->ev_in0, st);  // the counter is reset
         cudaEventRecordWithFlags(c->ev0, st, evf);
         int r = launch_align(p, shape, st);
         if (r) return r;
         cudaEventRecordWithFlags(c->ev1, st, evf);
+        if (d_arrive) {
+            // the points, while the kernel runs; scoring waits for the last chunk
+            cudaStreamWaitEvent(c->cstream, c->ev_in0, 0);
+            stage_plan(c, *plan, jobs, c->cstream, d_arrive);
+            cudaEventRecord(c->ev_in1, c->cstream);
+            cudaStreamWaitEvent(st, c->ev_in1, 0);
+        }
         r = launch_score(c->map.view, d_pts, (const ScoreJob*)c->d_sjobs.p, nj, max_n,
                          (const AlignOut*)c->d_aout.p, c->d_part.p, (ScoreOut*)c->d_sout.p,
                          (float)c->d1, (float)c->d2, st);
@@ -897,7 +967,7 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
         cudaMemcpyAsync(hst, c->d_status.p, 4, cudaMemcpyDeviceToHost, st);
         return cuda_fail(cudaGetLastError(), "align enqueue");
     };
-    if (c->cfg.cuda_graph && !c->trace) {
+    if (c->cfg.cuda_graph && !c->trace && !stream_in) {
         const std::vector<uint64_t> key = {
             nj, max_n, (uint64_t)shape.cluster, (uint64_t)shape.threads, (uint64_t)shape.regcap,
             (uint64_t)shape.queue, (uint64_t)(uintptr_t)c->d_qjobs.p,
@@ -1021,8 +1091,9 @@ static int run_align_finish(ndt_ctx* c, ndt_result* out) {
 }
 
 static int run_align(ndt_ctx* c, const float* d_pts, std::vector<AlignJob>& jobs,
-                     const std::vector<uint64_t>& n_by_slot, ndt_result* out) {
-    const int rc = run_align_enqueue(c, d_pts, jobs, n_by_slot);
+                     const std::vector<uint64_t>& n_by_slot, ndt_result* out,
+                     const StagePlan* plan = nullptr) {
+    const int rc = run_align_enqueue(c, d_pts, jobs, n_by_slot, plan);
     return rc ? rc : run_align_finish(c, out);
 }
 
@@ -1039,39 +1110,55 @@ extern "C" {
 
 }  // extern "C"
 
-// Host scans of a batch: checked, staged into x's pinned buffer and copied to x->d_in on x's
-// stream (copies in flight on return), and described as jobs.
+// Host scans of a batch: checked, described as jobs in launch order (largest scan first,
+// the caller's order among equal sizes) and laid out in x->d_in for copying in chunks (the
+// copies are issued by run_align_enqueue).
 static int prepare_batch(ndt_ctx* x, const ndt_scan* scans, uint64_t m,
-                         std::vector<AlignJob>& jobs, std::vector<uint64_t>& ns) {
+                         std::vector<AlignJob>& jobs, std::vector<uint64_t>& ns,
+                         StagePlan& plan) {
     if (m > 0xFFFFFFull) {
         set_error("too many scans in one batch");
         return NDT_ERR_CAPACITY;
     }
-    uint64_t total = 0;
     for (uint64_t i = 0; i < m; ++i) {
         if (scans[i].num_points && !scans[i].xyz) return NDT_ERR_INVALID_ARGUMENT;
         if (scans[i].num_points > 0xFFFFFFF0ull) {
             set_error("scan exceeds 2^32 points");
             return NDT_ERR_CAPACITY;
         }
-        total += scans[i].num_points;
     }
-    int rc;
-    if ((rc = pin_reserve(x->h_pts, total * 12 + 16)) || (rc = dev_reserve(x->d_in, total * 12 + 16)))
-        return rc;
+    std::vector<uint32_t> order(m);
+    for (uint64_t i = 0; i < m; ++i) order[i] = (uint32_t)i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        return scans[a].num_points > scans[b].num_points;
+    });
     jobs.assign(m, AlignJob{});
     ns.assign(m, 0);
-    std::vector<uint64_t> offset(m);
-    uint64_t off = 0;
-    for (uint64_t i = 0; i < m; ++i) {
-        jobs[i].offset = offset[i] = off;
-        jobs[i].n = (uint32_t)scans[i].num_points;
-        jobs[i].slot = (uint32_t)i;
-        for (int k = 0; k < 6; ++k) jobs[i].pose[k] = scans[i].initial_pose[k];
+    plan.scans = scans;
+    plan.chunk_job.clear();
+    const uint64_t max_chunk = (16ull << 20) / 12;
+    uint64_t off = 0, in_chunk = 0, chunk = (1ull << 20) / 12;
+    for (uint64_t t = 0; t < m; ++t) {
+        const uint32_t i = order[t];
+        if (t == 0 || in_chunk >= chunk) {
+            if (t) chunk = std::min(2 * chunk, max_chunk);
+            off = (off + 63) & ~63ull;
+            plan.chunk_job.push_back((uint32_t)t);
+            in_chunk = 0;
+        }
+        jobs[t].offset = off;
+        jobs[t].n = (uint32_t)scans[i].num_points;
+        jobs[t].slot = i;
+        for (int k = 0; k < 6; ++k) jobs[t].pose[k] = scans[i].initial_pose[k];
         ns[i] = scans[i].num_points;
         off += scans[i].num_points;
+        in_chunk += scans[i].num_points;
     }
-    stage_scans(x, scans, m, offset, total);
+    plan.chunk_job.push_back((uint32_t)m);
+    plan.total = off;
+    int rc;
+    if ((rc = pin_reserve(x->h_pts, off * 12 + 16)) || (rc = dev_reserve(x->d_in, off * 12 + 16)))
+        return rc;
     return NDT_OK;
 }
 
@@ -1112,8 +1199,9 @@ int ndt_align_batch(ndt_ctx* c, const ndt_scan* scans, uint64_t m, ndt_result* o
     cudaSetDevice(c->device);
     std::vector<AlignJob> jobs;
     std::vector<uint64_t> ns;
-    if ((rc = prepare_batch(c, scans, m, jobs, ns))) return rc;
-    return run_align(c, (const float*)c->d_in.p, jobs, ns, out);
+    StagePlan plan;
+    if ((rc = prepare_batch(c, scans, m, jobs, ns, plan))) return rc;
+    return run_align(c, (const float*)c->d_in.p, jobs, ns, out, &plan);
 }
 
 int ndt_batch_submit(ndt_ctx* c, const ndt_scan* scans, uint64_t m, uint64_t* ticket) {
@@ -1150,8 +1238,9 @@ int ndt_batch_submit(ndt_ctx* c, const ndt_scan* scans, uint64_t m, uint64_t* ti
     x->trace = false;
     std::vector<AlignJob> jobs;
     std::vector<uint64_t> ns;
-    if ((rc = prepare_batch(x, scans, m, jobs, ns))) return rc;
-    if ((rc = run_align_enqueue(x, (const float*)x->d_in.p, jobs, ns))) return rc;
+    StagePlan plan;
+    if ((rc = prepare_batch(x, scans, m, jobs, ns, plan))) return rc;
+    if ((rc = run_align_enqueue(x, (const float*)x->d_in.p, jobs, ns, &plan))) return rc;
     s->ticket = ++c->next_ticket;
     s->m = m;
     *ticket = s->ticket;

@@ -126,6 +126,11 @@ struct AlignParams {
                            // quarter of it near the end of a batch
     uint32_t qchunks_total;  // chunks of one iteration of every alignment (at full size)
     uint32_t qgrid;          // CTAs of the launch (set by the launch)
+    // points copied in while the work-queue kernel runs: the device word counts the points of
+    // the batch resident so far (a prefix of pts, written by the copy stream after each
+    // chunk); an alignment is claimable once its last point is resident. nullptr: all are.
+    const uint32_t* qarrive;
+    uint32_t qarrive_total;  // the word's value once every point is resident
 };
 
 // Newton-kernel sums per iteration: 34 f32 per-thread accumulators (score, gradient and

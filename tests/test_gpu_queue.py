@@ -133,3 +133,43 @@ def test_queue_autotune_and_forms(gpu):
     ls = capi.Context(work_queue=4, use_line_search=1)
     ls.set_target(seq.map)
     assert all(x["converged"] for x in ls.align_batch(scans[:4], list(poses[:4])))
+
+
+def test_queue_streamed_input(gpu):
+    """A host batch of more than one copy chunk is copied in while the work-queue kernel runs
+    (largest scan first; an alignment's first iteration is claimable once its points are
+    resident). Its results are identical to the same batch aligned from device memory (a
+    captured graph, replayed), through the synchronous and the asynchronous calls, run to
+    run; an empty and a one-point scan ride along."""
+    import torch
+    seq = synth.Sequence(seed=11, n_map=1_000_000, n_scans=80, scan_points=0)
+    rng = np.random.default_rng(5)
+    scans, poses = [], []
+    for k in range(80):
+        s = seq.scan(k)
+        m = int(rng.integers(300, min(len(s), 30_000) + 1))
+        scans.append(np.ascontiguousarray(s[np.sort(rng.choice(len(s), m, replace=False))]))
+        poses.append(seq.guess(k))
+    scans[5] = scans[5][:0]
+    scans[9] = scans[9][:1]
+    assert sum(len(s) for s in scans) * 12 > 4 << 20  # copy chunks of 1, 2, 4, ... MB
+    host = capi.Context(work_queue=2)
+    dev = capi.Context(work_queue=2, cuda_graph=1)
+    for c in (host, dev):
+        c.set_target(seq.map)
+    a = host.align_batch(scans, poses)
+    b = host.align_batch(scans, poses)
+    t = host.batch_submit(scans, poses)
+    s1 = host.batch_wait(t)
+    xyz = torch.from_numpy(np.concatenate(scans).astype(np.float32)).cuda()
+    offsets = np.concatenate([[0], np.cumsum([len(s) for s in scans])]).astype(np.uint64)
+    d1 = dev.align_batch_device(xyz.data_ptr(), offsets, poses)
+    d2 = dev.align_batch_device(xyz.data_ptr(), offsets, poses)
+    for i in range(len(scans)):
+        for o in (b, s1, d1, d2):
+            np.testing.assert_array_equal(a[i]["pose"], o[i]["pose"])
+            np.testing.assert_equal(a[i]["score"], o[i]["score"])
+            np.testing.assert_equal(a[i]["nvtl"], o[i]["nvtl"])
+            assert a[i]["iterations"] == o[i]["iterations"], i
+            assert a[i]["status"] == o[i]["status"], i
+    assert sum(r["converged"] for r in a) >= 0.8 * (len(scans) - 2)
