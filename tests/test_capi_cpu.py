@@ -94,3 +94,20 @@ def test_builder_mirrors_reference_names():
     c = b.config
     assert (c.resolution, c.max_iterations, c.trans_epsilon, c.step_size, c.outlier_ratio,
             c.use_gpu) == (1.0, 10, 0.02, 0.2, 0.5, True)
+
+
+def test_reference_kernel_driver_builds():
+    """The host driver of the reference's own graph-path kernels builds and exports its entry
+    points, and the cubins it loads are present (nothing runs without a GPU)."""
+    import shutil
+    import subprocess
+    from oracle import build as ob, ref_graph
+    lib = ob.build_ref_driver()
+    if shutil.which("nm") is None:
+        pytest.skip("nm not available")
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True,
+                         text=True).stdout
+    names = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    assert {"rg_open", "rg_set_map", "rg_align", "rg_eval", "rg_query", "rg_close",
+            "rg_error"} <= names
+    assert ref_graph.available()
