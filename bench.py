@@ -489,6 +489,7 @@ def run_reference(args):
             times.append(dt)
     total = sum(times)
     value = per_step * args.steps / total
+    ref_gpu = reference_gpu_kernels(g, scans, poses)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "aligns/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -501,8 +502,40 @@ def run_reference(args):
                                    "(the Rust reference cannot be built here)"},
         "e2e": {"value": value, "unit": "aligns/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_gpu_kernels": ref_gpu,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernels(grid, scans, poses, n=64):
+    """The reference's own GPU path for comparison: its graph kernels K1-K5 and voxel hash
+    (src/cuda_ffi/csrc, compiled unmodified into sm_103a cubins) driven one alignment at a
+    time by the restated FullGpuPipelineV2::optimize loop, on the first n scans of the
+    workload. The map upload and hash build happen once, before timing (the reference
+    repeats them on every align call)."""
+    try:
+        from oracle import oracle as O, ref_graph
+        if not ref_graph.available():
+            return {"unavailable": "reference cubins not built"}
+        rg = ref_graph.RefGraph()
+        rg.set_map(grid.means, grid.icovs, 2.0)
+        d1, d2 = (float(np.float32(x)) for x in O.gauss_params(2.0, 0.55))
+        n = min(n, len(scans))
+        for k in range(2):  # module load, first allocations
+            rg.align(scans[k], poses[k], d1, d2)
+        t0 = time.perf_counter()
+        iters = 0
+        for k in range(n):
+            iters += rg.align(scans[k], poses[k], d1, d2)["iterations"]
+        dt = time.perf_counter() - t0
+        rg.close()
+        return {"value": n / dt, "unit": "aligns/s", "ms_per_align": 1000 * dt / n,
+                "iterations_per_align": iters / n,
+                "sample": f"{n} of the workload's scans, one align call each: K1, then K2/K3/K5 "
+                          "per iteration with a device sync and a flag read (the reference's "
+                          "host loop), points uploaded per call; voxels of the oracle's build"}
+    except Exception as e:  # no device, or the driver library could not load
+        return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
 def run_ours(args):
