@@ -1477,14 +1477,15 @@ __device__ __forceinline__ uint32_t qw_nch(unsigned long long w) {
 }
 
 // Chunks of iteration `it` of an alignment with n points: n / qchunk for its first
-// QSPLIT_ITER iterations, then four times as many, a quarter the size. The alignments that
+// QSPLIT_ITER iterations, then QSPLIT_DIV times as many, that much smaller. The alignments that
 // run long are the ones that finish a batch, on an otherwise idle GPU: smaller chunks spread
 // each of their iterations over more SMs. The rule depends on the iteration alone, so every
 // run sums an alignment's chunks over the same tree (results are identical run to run). At
 // most QMAXCH.
 constexpr uint32_t QSPLIT_ITER = 10;
 __device__ __forceinline__ uint32_t queue_chunks(const AlignParams& P, uint32_t n, uint32_t it) {
-    const uint32_t size = it < QSPLIT_ITER ? (uint32_t)P.qchunk : (uint32_t)P.qchunk / 4u;
+    const uint32_t size =
+        it < QSPLIT_ITER ? (uint32_t)P.qchunk : max(1u, (uint32_t)P.qchunk / QSPLIT_DIV);
     return min(n ? (n + size - 1u) / size : 1u, QMAXCH);
 }
 
@@ -1670,8 +1671,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     for (;;) {
         __syncthreads();  // the previous chunk (and controller) is finished with shared memory
         if (warp == 0) {
-            // claim: scan the alignments from the first one not known to be finished, 32 at
-            // a time, and try the claimable ones in order
+            // claim, lowest iteration first: alignments that need many iterations form the
+            // batch's tail, so none may fall behind while others run ahead. Pass 0 finds the
+            // lowest iteration (saturated at 255) among the claimable alignments, from the
+            // first one not known to be finished; pass 1 tries the claimable ones at that
+            // iteration in order (from the oldest); if other CTAs took all of their chunks
+            // meanwhile, pass 2 takes any claimable chunk, oldest alignment first.
             int job = -1, first_open = -1;
             uint32_t chunk = 0, gen = 0, nchunks = 0;
             // points resident while the batch is still being copied in (all: ~0)
@@ -1680,30 +1685,50 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                 arrived = ld_volatile32(P.qarrive);
                 if (arrived >= P.qarrive_total) arrived = 0xFFFFFFFFu;
             }
-            for (uint32_t base = (uint32_t)s_lw; base < B && job < 0; base += 32) {
+            // whether alignment j has a chunk to claim; open: not finished; g: its iteration
+            // (saturated at 255)
+            auto claimable = [&](uint32_t j, bool& open, uint32_t& g) -> bool {
+                const unsigned long long w = ld_volatile(&P.qjobs[j].gen_claim);
+                open = qw_gen(w) != QDONE;
+                g = min(qw_gen(w), 255u);
+                bool ok = open && (uint32_t)w < qw_nch(w);
+                if (ok && arrived != 0xFFFFFFFFu && qw_gen(w) == 0u)
+                    ok = P.jobs[j].offset + P.jobs[j].n <= (uint64_t)arrived;
+                return ok;
+            };
+            uint32_t best = 0xFFFFFFFFu;  // min over claimable j of min(iteration, 255) << 24 | j
+#pragma unroll 4
+            for (uint32_t base = (uint32_t)s_lw; base < B; base += 32) {
                 const uint32_t j = base + lane;
-                bool open = false, ok = false;
-                if (j < B) {
-                    const unsigned long long w = ld_volatile(&P.qjobs[j].gen_claim);
-                    open = qw_gen(w) != QDONE;
-                    ok = open && (uint32_t)w < qw_nch(w);
-                    if (ok && arrived != 0xFFFFFFFFu && qw_gen(w) == 0u)
-                        ok = P.jobs[j].offset + P.jobs[j].n <= (uint64_t)arrived;
-                }
+                bool open = false;
+                uint32_t g = 0;
+                if (j < B && claimable(j, open, g)) best = min(best, (g << 24) | j);
                 const unsigned om = __ballot_sync(0xffffffffu, open);
                 if (first_open < 0 && om) first_open = (int)base + __ffs(om) - 1;
-                unsigned okm = __ballot_sync(0xffffffffu, ok);
-                while (okm != 0u && job < 0) {
-                    const int src = __ffs(okm) - 1;
-                    okm &= okm - 1u;
-                    unsigned long long old = 0ull;
-                    if (lane == src) old = atomicAdd(&P.qjobs[j].gen_claim, 1ull);
-                    old = __shfl_sync(0xffffffffu, old, src);
-                    if (qw_gen(old) != QDONE && (uint32_t)old < qw_nch(old)) {
-                        job = (int)base + src;
-                        chunk = (uint32_t)old;
-                        gen = qw_gen(old);
-                        nchunks = qw_nch(old);
+            }
+            best = __reduce_min_sync(0xffffffffu, best);
+            for (int pass = 1; pass <= 2 && job < 0 && best != 0xFFFFFFFFu; ++pass) {
+                const uint32_t gsel = best >> 24;
+                const uint32_t start =
+                    pass == 1 ? ((best & 0xFFFFFFu) & ~31u) : (uint32_t)max(first_open, 0);
+                for (uint32_t base = start; base < B && job < 0; base += 32) {
+                    const uint32_t j = base + lane;
+                    bool ok = false, open = false;
+                    uint32_t g = 0;
+                    if (j < B) ok = claimable(j, open, g) && (pass == 2 || g == gsel);
+                    unsigned okm = __ballot_sync(0xffffffffu, ok);
+                    while (okm != 0u && job < 0) {
+                        const int src = __ffs(okm) - 1;
+                        okm &= okm - 1u;
+                        unsigned long long old = 0ull;
+                        if (lane == src) old = atomicAdd(&P.qjobs[j].gen_claim, 1ull);
+                        old = __shfl_sync(0xffffffffu, old, src);
+                        if (qw_gen(old) != QDONE && (uint32_t)old < qw_nch(old)) {
+                            job = (int)base + src;
+                            chunk = (uint32_t)old;
+                            gen = qw_gen(old);
+                            nchunks = qw_nch(old);
+                        }
                     }
                 }
             }
@@ -1854,9 +1879,9 @@ static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t ch
             cache[{dev, smem}] = ctas;
         }
     }
-    // at most one CTA per chunk of the batch at the quarter chunk size
-    const unsigned grid =
-        (unsigned)std::min<uint64_t>((uint64_t)ctas, 4ull * std::max(1u, chunks));
+    // at most one CTA per chunk of the batch at the late-iteration chunk size
+    const unsigned grid = (unsigned)std::min<uint64_t>(
+        (uint64_t)ctas, (uint64_t)QSPLIT_DIV * std::max(1u, chunks));
     AlignParams q = p;
     q.qgrid = grid;
     k_queue_init<SEM><<<(q.num_jobs + 3) / 4, 128, 0, s>>>(q);

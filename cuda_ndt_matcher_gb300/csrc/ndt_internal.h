@@ -122,8 +122,8 @@ struct AlignParams {
     double* qpart;
     const uint32_t* qpart_off;
     uint32_t* qcount;
-    int32_t qchunk;        // points per chunk (set by the launch from the shape); chunks of a
-                           // quarter of it near the end of a batch
+    int32_t qchunk;        // points per chunk (set by the launch from the shape); chunks of
+                           // 1/QSPLIT_DIV of it in an alignment's late iterations
     uint32_t qchunks_total;  // chunks of one iteration of every alignment (at full size)
     uint32_t qgrid;          // CTAs of the launch (set by the launch)
     // points copied in while the work-queue kernel runs: the device word counts the points of
@@ -148,6 +148,9 @@ struct QJob {
 };
 constexpr uint32_t QDONE = 0xFFFFu;
 constexpr uint32_t QMAXCH = 0xFFFFu;  // chunks per iteration at most (16-bit count)
+// Chunks of an alignment's late iterations are 1/QSPLIT_DIV of the launch's chunk size (the
+// partial-sum slots are sized for them). At the 20k-point bench batch, 2 and 8 were slower.
+constexpr uint32_t QSPLIT_DIV = 4;
 // Controller state of an alignment between iterations (FP64; read and written only by the
 // controller of the alignment's current iteration).
 struct QCtl {
