@@ -1456,7 +1456,10 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
 // out largest alignment first, in copy chunks that start on 768-byte boundaries, and a copy
 // stream writes the count of resident points after each chunk. An alignment's first
 // iteration is claimable once its last point is resident; the chunks' alignment keeps every
-// L1 line a CTA reads inside chunks already copied.
+// L1 line a CTA reads inside chunks already copied. Nothing guarantees that the copies run
+// while the kernel does (a tool may serialise them), so a CTA never waits for input beyond
+// QSTARVE_NS without progress: it leaves, and a continuation launch (P.qresume) queued after
+// the last copy finishes whatever is left from the state in global memory.
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
     return *reinterpret_cast<const volatile unsigned long long*>(p);
@@ -1761,6 +1764,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     }
                     if (idle_since == 0) {
                         idle_since = now;
+                    } else if (!fed && now - idle_since > QSTARVE_NS) {
+                        stop = 1;  // starved of input: the continuation launch finishes
                     } else if (now - idle_since > 2000000000ull) {
                         atomicOr(P.status, ST_QUEUE_STALL);
                         stop = 1;
@@ -1884,7 +1889,7 @@ static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t ch
         (uint64_t)ctas, (uint64_t)QSPLIT_DIV * std::max(1u, chunks));
     AlignParams q = p;
     q.qgrid = grid;
-    k_queue_init<SEM><<<(q.num_jobs + 3) / 4, 128, 0, s>>>(q);
+    if (!q.qresume) k_queue_init<SEM><<<(q.num_jobs + 3) / 4, 128, 0, s>>>(q);
     kern<<<grid, T, smem, s>>>(q);
     return cudaGetLastError();
 }

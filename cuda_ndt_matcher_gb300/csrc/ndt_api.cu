@@ -951,11 +951,18 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
         if (r) return r;
         cudaEventRecordWithFlags(c->ev1, st, evf);
         if (d_arrive) {
-            // the points, while the kernel runs; scoring waits for the last chunk
+            // the points, while the kernel runs; then, after the last chunk, the continuation
+            // launch (it finds nothing left unless the first launch ran out of input) and
+            // scoring
             cudaStreamWaitEvent(c->cstream, c->ev_in0, 0);
             stage_plan(c, *plan, jobs, c->cstream, d_arrive);
             cudaEventRecord(c->ev_in1, c->cstream);
             cudaStreamWaitEvent(st, c->ev_in1, 0);
+            AlignParams pr = p;
+            pr.qarrive = nullptr;
+            pr.qresume = 1;
+            if ((r = launch_align(pr, shape, st))) return r;
+            cudaEventRecordWithFlags(c->ev1, st, evf);
         }
         r = launch_score(c->map.view, d_pts, (const ScoreJob*)c->d_sjobs.p, nj, max_n,
                          (const AlignOut*)c->d_aout.p, c->d_part.p, (ScoreOut*)c->d_sout.p,

@@ -131,7 +131,14 @@ struct AlignParams {
     // chunk); an alignment is claimable once its last point is resident. nullptr: all are.
     const uint32_t* qarrive;
     uint32_t qarrive_total;  // the word's value once every point is resident
+    // 1: this launch continues an earlier one over the same state (no initialisation). With
+    // qarrive set, CTAs that find nothing to claim while input is still arriving leave after
+    // QSTARVE_NS without input progress, so the kernel never depends on copies that another
+    // stream may only run after it (the host then launches the continuation after the last
+    // copy).
+    int32_t qresume;
 };
+constexpr unsigned long long QSTARVE_NS = 2000000ull;
 
 // Newton-kernel sums per iteration: 34 f32 per-thread accumulators (score, gradient and
 // Hessian terms), reduced in FP64, plus the correspondence count.

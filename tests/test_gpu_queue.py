@@ -173,3 +173,39 @@ def test_queue_streamed_input(gpu):
             assert a[i]["iterations"] == o[i]["iterations"], i
             assert a[i]["status"] == o[i]["status"], i
     assert sum(r["converged"] for r in a) >= 0.8 * (len(scans) - 2)
+
+
+_SERIAL_SNIPPET = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from cuda_ndt_matcher_gb300 import capi, synth
+seq = synth.Sequence(seed=11, n_map=1_000_000, n_scans=40, scan_points=6000)
+scans = [seq.scan(k) for k in range(40)]
+poses = [seq.guess(k) for k in range(40)]
+ctx = capi.Context(work_queue=2)
+ctx.set_target(seq.map)
+res = ctx.align_batch(scans, poses)
+print(json.dumps([[float(v).hex() for v in r["pose"]] + [r["iterations"]] for r in res]))
+"""
+
+
+def test_queue_streamed_input_serialised(gpu):
+    """With every launch synchronous (CUDA_LAUNCH_BLOCKING=1), no copy can run while the
+    work-queue kernel waits for input: its CTAs leave after the starvation limit, and the
+    continuation launch queued after the last copy finishes the batch. Results are identical
+    to those of the concurrent run."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for blocking in ("0", "1"):
+        env = dict(os.environ, CUDA_LAUNCH_BLOCKING=blocking)
+        r = subprocess.run([sys.executable, "-c", _SERIAL_SNIPPET, root], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out[blocking] = json.loads(r.stdout.strip().splitlines()[-1])
+    assert sum(len(s) for s in out["0"]) > 0
+    assert out["0"] == out["1"]
