@@ -15,7 +15,9 @@ guesses from constant-velocity prediction + noise). Prints one JSON line.
 - cpu_baseline : the CPU restatement of the reference's CPU path (NdtOptimizer::align)
           on all host cores, on a bounded sample of the same scans.
 --impl reference times that CPU path alone (the reference's own implementation is Rust and
-cannot be built here; the restatement stands in for it).
+cannot be built here; the restatement stands in for it), and reports beside it the
+reference's own GPU kernels (K1-K5, compiled from its sources) driven one alignment at a time
+as its host loop drives them ("reference_gpu_kernels").
 """
 import argparse
 import json
@@ -39,7 +41,7 @@ FLOP_PER_PAIR = 65
 # 5M-point map, seed 2), from one ncu capture of this bench per kernel form
 # (profiles/k_ndt_align_seq5M_b256.md, profiles/k_ndt_queue_seq5M_b256.md)
 NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
-                     ("k_ndt_queue", 256, 5_000_000, 2): 75.6e6}
+                     ("k_ndt_queue", 256, 5_000_000, 2): 107.4e6}
 
 
 def parse():
