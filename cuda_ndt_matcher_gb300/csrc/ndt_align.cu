@@ -74,10 +74,16 @@ struct AlignShared {
     double prev[3], prev2[3];
     int last_corr;
     int osc, max_osc;
-    // graph-path line search: direction, start pose, phi(0), phi'(0), candidate step lengths,
-    // poses, frames (every rank), A_k at each candidate pose, per-candidate sums
+    // line search: direction, start pose, phi(0), phi'(0), candidate step lengths, poses,
+    // frames (every rank), A_k at each candidate pose, per-candidate sums. The graph path
+    // scores up to 8 candidates; the CPU path's More-Thuente search one trial per round.
     double ls_delta[6], ls_orig[6], ls_phi0, ls_dphi0, ls_best, ls_best_alpha;
-    int ls_more;  // the selection needs another round of candidates
+    int ls_more;    // the selection needs another round of candidates
+    int ls_active;  // this iteration scores line-search candidates (every rank)
+    // More-Thuente state (rank 0): interval ends and their values (on psi while mt_open),
+    // the trial step, iterations after the first trial, the first trial pending
+    double mt_al, mt_fl, mt_gl, mt_au, mt_fu, mt_gu, mt_at;
+    int mt_open, mt_iter, mt_first;
     double ls_alpha[LS_MAX], ls_pose[LS_MAX][6], ls_phi[LS_MAX], ls_dphi[LS_MAX];
     double ls_Ad[LS_MAX][27], ls_trig[LS_MAX][16];
     float ls_fr[LS_MAX][NFR];
@@ -778,9 +784,12 @@ __device__ __forceinline__ void point_terms(const MapView& m, const uint32_t* of
         }
 }
 
-// Line-search terms of one point at a candidate pose (graph semantics; the candidate pass of
-// ndt_graph_linesearch_kernel, ndt_graph_kernels.cu:473-570): score and gradient only, as the
+// Line-search terms of one point at a candidate pose: score and gradient only, as the
 // accumulators S (a[0]), G (a[1..3]) and G p^T (a[4..12]) of point_terms, same arithmetic.
+// Graph semantics: the candidate pass of ndt_graph_linesearch_kernel
+// (ndt_graph_kernels.cu:473-570); CPU semantics: a More-Thuente trial, the score and gradient
+// of compute_derivatives_cpu_with_metric without the Hessian (solver.rs:663-673).
+template <bool CPU_SEM>
 __device__ __forceinline__ void point_terms_ls(const MapView& m, const uint32_t* off27,
                                                float px, float py, float pz,
                                                const float* fr, int max_nb, float d1f, float d2f,
@@ -807,6 +816,10 @@ __device__ __forceinline__ void point_terms_ls(const MapView& m, const uint32_t*
         const float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
         const float sq = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
         const float e = expf(-0.5f * d2f * sq);
+        if (CPU_SEM) {
+            const float wn = d2f * e;  // compute_derivative_single: zero unless d2*e in [0,1]
+            if (!(wn >= 0.f && wn <= 1.f)) continue;
+        }
         const float w = d1d2 * e;
         S = fmaf(-d1f, e, S);
         G[0] = fmaf(w, c0, G[0]);
@@ -910,6 +923,64 @@ __device__ void write_out(AlignOut& o, const double* pose, double score, const d
 }
 
 // One step of the controller (rank 0, lane 0). Returns 1 when the alignment is finished.
+// CPU path (NdtOptimizer::align, solver.rs:135-305), first half of a Newton step: the
+// correspondence check, the best score and pose, the singular and converged exits; else the
+// unit ascent direction in x (reversed when g.x <= 0) and the Newton step's norm in *dn.
+// Returns 1 when the alignment is finished (outputs written). Lane 0.
+__device__ int cpu_direction(const AlignParams& P, AlignShared& sh, const AlignJob& job,
+                             AlignOut& o, int it, double score, int ncorr, double* x,
+                             double* dn_out) {
+    if (ncorr < P.min_corr) {
+        if (it == 0) {
+            write_out(o, job.pose, 0.0, nullptr, 0, 0, 0, 0, NDT_STATUS_NO_CORRESPONDENCES);
+        } else {
+            write_out(o, sh.best_pose, sh.best_score, sh.last_H, P.max_iter, 0, sh.last_corr,
+                      sh.max_osc, NDT_STATUS_MAX_ITERATIONS);
+        }
+        return 1;
+    }
+    sh.last_corr = ncorr;
+    for (int i = 0; i < 36; ++i) sh.last_H[i] = sh.H[i];
+    if (score > sh.best_score) {
+        sh.best_score = score;
+        for (int i = 0; i < 6; ++i) sh.best_pose[i] = sh.pose[i];
+    }
+    for (int i = 0; i < 6; ++i) x[i] = sh.solve.x[i];
+    if (!sh.solve.ok) {
+        write_out(o, sh.best_pose, sh.best_score, sh.last_H, it, 0, sh.last_corr, sh.max_osc,
+                  NDT_STATUS_SINGULAR_HESSIAN);
+        return 1;
+    }
+    const double dn = sqrt(dot6(x, x));
+    if (dn < P.eps) {
+        write_out(o, sh.pose, score, sh.H, it + 1, 1, ncorr, sh.max_osc, NDT_STATUS_CONVERGED);
+        return 1;
+    }
+    double gd = 0.0;
+    for (int i = 0; i < 6; ++i) {
+        x[i] /= dn;
+        gd += sh.g[i] * x[i];
+    }
+    if (gd <= 0.0)
+        for (int i = 0; i < 6; ++i) x[i] = -x[i];
+    *dn_out = dn;
+    return 0;
+}
+
+// CPU path, second half: pose += step x (apply_pose_delta, types.rs:183-200), the oscillation
+// history, the max-iteration exit (best pose). Returns 1 when the alignment is finished.
+__device__ int cpu_step(const AlignParams& P, AlignShared& sh, AlignOut& o, int it,
+                        const double* x, double step) {
+    for (int i = 0; i < 6; ++i) sh.pose[i] += x[i] * step;
+    osc_update(sh, sh.pose, it);
+    if (it + 1 >= P.max_iter) {
+        write_out(o, sh.best_pose, sh.best_score, sh.last_H, P.max_iter, 0, sh.last_corr,
+                  sh.max_osc, NDT_STATUS_MAX_ITERATIONS);
+        return 1;
+    }
+    return 0;
+}
+
 template <bool CPU_SEM>
 __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, const AlignJob& job,
                             AlignOut& o, int it, double score, int ncorr) {
@@ -939,49 +1010,9 @@ __device__ __noinline__ int control_step(const AlignParams& P, AlignShared& sh, 
         return 0;
     }
     // CPU semantics: NdtOptimizer::align (solver.rs:135-305)
-    if (ncorr < P.min_corr) {
-        if (it == 0) {
-            write_out(o, job.pose, 0.0, nullptr, 0, 0, 0, 0, NDT_STATUS_NO_CORRESPONDENCES);
-        } else {
-            write_out(o, sh.best_pose, sh.best_score, sh.last_H, P.max_iter, 0, sh.last_corr,
-                      sh.max_osc, NDT_STATUS_MAX_ITERATIONS);
-        }
-        return 1;
-    }
-    sh.last_corr = ncorr;
-    for (int i = 0; i < 36; ++i) sh.last_H[i] = H[i];
-    if (score > sh.best_score) {
-        sh.best_score = score;
-        for (int i = 0; i < 6; ++i) sh.best_pose[i] = pose[i];
-    }
-    double x[6];
-    for (int i = 0; i < 6; ++i) x[i] = sh.solve.x[i];
-    if (!sh.solve.ok) {
-        write_out(o, sh.best_pose, sh.best_score, sh.last_H, it, 0, sh.last_corr, sh.max_osc,
-                  NDT_STATUS_SINGULAR_HESSIAN);
-        return 1;
-    }
-    const double dn = sqrt(dot6(x, x));
-    if (dn < P.eps) {
-        write_out(o, pose, score, H, it + 1, 1, ncorr, sh.max_osc, NDT_STATUS_CONVERGED);
-        return 1;
-    }
-    double gd = 0.0;
-    for (int i = 0; i < 6; ++i) {
-        x[i] /= dn;
-        gd += g[i] * x[i];
-    }
-    if (gd <= 0.0)
-        for (int i = 0; i < 6; ++i) x[i] = -x[i];
-    double step = dn < P.step_size ? dn : P.step_size;
-    for (int i = 0; i < 6; ++i) pose[i] += x[i] * step;
-    osc_update(sh, pose, it);
-    if (it + 1 >= P.max_iter) {
-        write_out(o, sh.best_pose, sh.best_score, sh.last_H, P.max_iter, 0, sh.last_corr,
-                  sh.max_osc, NDT_STATUS_MAX_ITERATIONS);
-        return 1;
-    }
-    return 0;
+    double x[6], dn;
+    if (cpu_direction(P, sh, job, o, it, score, ncorr, x, &dn)) return 1;
+    return cpu_step(P, sh, o, it, x, dn < P.step_size ? dn : P.step_size);
 }
 
 // GPU global timer (ns): per-alignment start / finish times for latency percentiles
@@ -1067,6 +1098,158 @@ __device__ __forceinline__ void warp_sum16(const float* v, int lane, int nv, dou
         }
     }
     if (lane < nv) out[lane] = (double)s[0] + (double)c[0];
+}
+
+// ---- More-Thuente line search of the CPU path (use_line_search, CPU semantics) ----
+// more_thuente_search (src/ndt_cuda/src/optimization/more_thuente.rs:236-410), after More &
+// Thuente (1994) with the interpolants of Sun & Yuan (2006): it minimises phi = -score along
+// the unit ascent direction, keeping the interval [a_l, a_u] on the auxiliary
+// psi(a) = phi(a) - phi(0) - mu phi'(0) a until a trial has psi <= 0 and psi' >= 0, then on
+// phi. Each trial is one round of the candidate pass (score and gradient at the trial pose);
+// lane 0 of rank 0's controller warp runs the search between rounds, in FP64.
+__device__ __forceinline__ double mt_clamp(double a) {
+    return a < MT_STEP_MIN ? MT_STEP_MIN : (a > MT_STEP_MAX ? MT_STEP_MAX : a);
+}
+
+// minimiser of the cubic through (a, fa, ga) and (b, fb, gb); false when it is complex
+__device__ bool mt_cubic(double a, double fa, double ga, double b, double fb, double gb,
+                         double& out) {
+    const double z = 3.0 * (fb - fa) / (b - a) - gb - ga;
+    const double w2 = z * z - gb * ga;
+    if (w2 < 0.0) return false;
+    const double w = sqrt(w2);
+    out = a + (b - a) * (w - ga - z) / (gb - ga + 2.0 * w);
+    return true;
+}
+
+// next trial (trial_value_selection, more_thuente.rs:83-194); l: the best end so far,
+// u: the other end, t: the last trial
+__device__ double mt_next(double al, double fl, double gl, double au, double fu, double gu,
+                          double at, double ft, double gt) {
+    double ac;
+    if (ft > fl) {  // bracketed by [al, at]
+        if (!mt_cubic(al, fl, gl, at, ft, gt, ac))
+            return al - 0.5 * (al - at) * gl / (gl - (fl - ft) / (al - at));
+        const double den = gl - (fl - ft) / (al - at);
+        if (fabs(den) < 1e-15) return ac;
+        const double aq = al - 0.5 * (al - at) * gl / den;
+        return fabs(ac - al) < fabs(aq - al) ? ac : 0.5 * (aq + ac);
+    }
+    if (gt * gl < 0.0) {  // slopes of opposite sign
+        const bool ok = mt_cubic(al, fl, gl, at, ft, gt, ac);
+        const double as = al - (al - at) / (gl - gt) * gl;
+        if (!ok) return as;
+        return fabs(ac - at) >= fabs(as - at) ? ac : as;
+    }
+    if (fabs(gt) <= fabs(gl)) {  // slope shrinking in magnitude
+        if (!mt_cubic(al, fl, gl, at, ft, gt, ac))
+            ac = at > al ? at + 0.66 * (au - at) : at - 0.66 * (at - au);
+        const double as = fabs(gl - gt) > 1e-15 ? al - (al - at) / (gl - gt) * gl : ac;
+        const double an = fabs(ac - at) < fabs(as - at) ? ac : as;
+        const double lim = at + 0.66 * (au - at);
+        return at > al ? fmin(lim, an) : fmax(lim, an);
+    }
+    if (mt_cubic(au, fu, gu, at, ft, gt, ac)) return ac;  // through the trial and u
+    return 0.5 * (al + au);
+}
+
+// interval update (update_interval, more_thuente.rs:196-234); true when it shrank to a point
+__device__ bool mt_update(AlignShared& sh, double at, double ft, double gt) {
+    if (ft > sh.mt_fl) {
+        sh.mt_au = at;
+        sh.mt_fu = ft;
+        sh.mt_gu = gt;
+        return false;
+    }
+    const double side = gt * (sh.mt_al - at);
+    if (side > 0.0) {
+        sh.mt_al = at;
+        sh.mt_fl = ft;
+        sh.mt_gl = gt;
+        return false;
+    }
+    if (side < 0.0) {
+        sh.mt_au = sh.mt_al;
+        sh.mt_fu = sh.mt_fl;
+        sh.mt_gu = sh.mt_gl;
+        sh.mt_al = at;
+        sh.mt_fl = ft;
+        sh.mt_gl = gt;
+        return false;
+    }
+    return true;
+}
+
+// After the Newton solve (lane 0): the first half of the CPU step, then the search from
+// step_size (solver.rs:268-276, 640-660) with its first trial pose in ls_pose[0]; without an
+// ascent direction (g.x <= 0) the step is step_size at once. Returns 1 when the alignment is
+// finished; sh.ls_active tells whether trials follow.
+__device__ __noinline__ int mt_prepare(const AlignParams& P, AlignShared& sh,
+                                       const AlignJob& job, AlignOut& o, int it, double score,
+                                       int ncorr) {
+    double x[6], dn;
+    sh.ls_active = 0;
+    if (cpu_direction(P, sh, job, o, it, score, ncorr, x, &dn)) return 1;
+    const double d0 = dot6(sh.g, x);
+    if (d0 <= 0.0) return cpu_step(P, sh, o, it, x, P.step_size);
+    for (int i = 0; i < 6; ++i) {
+        sh.ls_delta[i] = x[i];
+        sh.ls_orig[i] = sh.pose[i];
+    }
+    sh.ls_phi0 = score;
+    sh.ls_dphi0 = d0;
+    sh.mt_first = 1;
+    sh.mt_at = mt_clamp(P.step_size);
+    for (int i = 0; i < 6; ++i) sh.ls_pose[0][i] = sh.pose[i] + x[i] * sh.mt_at;
+    sh.ls_active = 1;
+    return 0;
+}
+
+// After a trial (lane 0; its score and slope in ls_phi[0], ls_dphi[0]): the search's next
+// move. Returns -1 with the next trial pose in ls_pose[0], else takes the step (the trial
+// meeting the strong Wolfe conditions, or step_max when the search ends without one:
+// solver.rs:694-698) and returns cpu_step's result.
+__device__ __noinline__ int mt_decide(const AlignParams& P, AlignShared& sh, AlignOut& o,
+                                      int it) {
+    const double mu = P.ls_mu, nu = P.ls_nu;
+    const double phi0 = -sh.ls_phi0, dphi0 = -sh.ls_dphi0;
+    const double at = sh.mt_at, phi = -sh.ls_phi[0], dphi = -sh.ls_dphi[0];
+    const double psi = phi - phi0 - mu * dphi0 * at, dpsi = dphi - mu * dphi0;
+    double step = -1.0;
+    if (sh.mt_first) {  // both ends at 0, on psi
+        sh.mt_first = 0;
+        sh.mt_al = sh.mt_au = 0.0;
+        sh.mt_fl = phi0 - phi0 - mu * dphi0 * sh.mt_al;
+        sh.mt_fu = phi0 - phi0 - mu * dphi0 * sh.mt_au;
+        sh.mt_gl = sh.mt_gu = dphi0 - mu * dphi0;
+        sh.mt_open = 1;
+        sh.mt_iter = 0;
+    } else {
+        if (sh.mt_open && psi <= 0.0 && dpsi >= 0.0) {  // from psi to phi
+            sh.mt_open = 0;
+            sh.mt_fl = sh.mt_fl + phi0 - mu * dphi0 * sh.mt_al;
+            sh.mt_gl += mu * dphi0;
+            sh.mt_fu = sh.mt_fu + phi0 - mu * dphi0 * sh.mt_au;
+            sh.mt_gu += mu * dphi0;
+        }
+        const bool point = sh.mt_open ? mt_update(sh, at, psi, dpsi) : mt_update(sh, at, phi, dphi);
+        if (point || ++sh.mt_iter >= MT_MAX_ITER) step = MT_STEP_MAX;
+    }
+    if (step < 0.0) {
+        if (psi <= 0.0 && fabs(dphi) <= nu * fabs(dphi0)) {
+            step = at;
+        } else {
+            const double an = mt_clamp(
+                sh.mt_open ? mt_next(sh.mt_al, sh.mt_fl, sh.mt_gl, sh.mt_au, sh.mt_fu, sh.mt_gu,
+                                     at, psi, dpsi)
+                           : mt_next(sh.mt_al, sh.mt_fl, sh.mt_gl, sh.mt_au, sh.mt_fu, sh.mt_gu,
+                                     at, phi, dphi));
+            sh.mt_at = an;
+            for (int i = 0; i < 6; ++i) sh.ls_pose[0][i] = sh.ls_orig[i] + sh.ls_delta[i] * an;
+            return -1;
+        }
+    }
+    return cpu_step(P, sh, o, it, sh.ls_delta, step);
 }
 
 // Line-search set-up after the Newton solve (graph path; ndt_graph_solve_kernel,
@@ -1161,7 +1344,10 @@ __device__ __noinline__ int ls_decide(const AlignParams& P, AlignShared& sh, Ali
 
 // REGCAP: registers per thread the launch bounds allow (128: the default; 80 and 64: more
 // resident CTAs per SM at the price of some spills; the autotuner picks)
-template <int THREADS, bool CPU_SEM, int REGCAP>
+// LS: the line-search code is compiled in (always for the graph path, where it is switched
+// at run time; for the CPU path only in the variants that run its More-Thuente search, so
+// the plain CPU kernels keep their registers)
+template <int THREADS, bool CPU_SEM, int REGCAP, bool LS>
 __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_align(const AlignParams P) {
     constexpr int NW = THREADS / 32;
@@ -1182,8 +1368,10 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     const MapView& m = P.map;
     const float* pts = P.pts + 3 * job.offset;
     const uint32_t n = job.n;
-    // graph path with line search: every iteration adds a candidate pass (two more barriers)
-    const bool line_search = !CPU_SEM && P.ls_cands > 0;
+    // line search: every iteration adds candidate passes (two more barriers each); the graph
+    // path scores up to 8 candidates in three rounds, the CPU path one More-Thuente trial per
+    // round
+    const bool line_search = LS && P.ls_cands > 0;
 
     if (tid == 0) {
         for (int i = 0; i < 6; ++i) {
@@ -1196,6 +1384,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         sh.osc = sh.max_osc = 0;
         for (int i = 0; i < 36; ++i) sh.last_H[i] = 0.0;
         sh.done = 0;
+        sh.ls_active = 0;
         sh.solve.have_w = 0;
     }
     nbhd_offsets(m, s_off27);
@@ -1280,10 +1469,14 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     corr_total += (uint64_t)ncorr;
                     AlignOut& o = P.out[jid];
                     int done = 0;
-                    if (line_search)
-                        ls_prepare(P, sh);  // the step is taken after the candidate pass
-                    else
+                    if (!line_search) {
                         done = control_step<CPU_SEM>(P, sh, job, o, it, sh.tot[A_SC], ncorr);
+                    } else if (CPU_SEM) {  // trials follow unless the step is already taken
+                        done = mt_prepare(P, sh, job, o, it, sh.tot[A_SC], ncorr);
+                    } else {
+                        ls_prepare(P, sh);  // the step is taken after the candidate pass
+                        sh.ls_active = 1;
+                    }
                     if (done) {
                         o.point_iters = point_iters;
                         o.corr_total = corr_total;
@@ -1291,14 +1484,18 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     sh.done = done;
                 }
                 __syncwarp();
-                if (!line_search) {
+                if (!sh.ls_active) {  // the step is taken: the new pose's frame to every rank
                     make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
                     if (lane > 0 && lane < K) {
                         AlignShared* rs = cluster.map_shared_rank(&sh, lane);
                         for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
                         for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
-                        rs->done = sh.done;
                     }
+                }
+                if (lane > 0 && lane < K) {
+                    AlignShared* rs = cluster.map_shared_rank(&sh, lane);
+                    rs->done = sh.done;
+                    rs->ls_active = sh.ls_active;
                 }
                 if (t) {  // controller sub-phase cycles: assembly, solve, step + next frame
                     t[44] = (double)(cb - ca);
@@ -1308,9 +1505,10 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                 }
             }
             if (line_search) {  // candidate frames, one warp per candidate, to every rank
-                __syncthreads();
-                for (int c = warp; c < P.ls_cands; c += NW) {
-                    make_frame_warp(sh.ls_pose[c], false, sh.ls_fr[c], sh.ls_trig[c],
+                __syncthreads();  // warp 0's decision (ls_active) is visible to the CTA
+                const int ncand = !sh.ls_active ? 0 : (CPU_SEM ? 1 : P.ls_cands);
+                for (int c = warp; c < ncand; c += NW) {
+                    make_frame_warp(sh.ls_pose[c], CPU_SEM, sh.ls_fr[c], sh.ls_trig[c],
                                     sh.ls_Ad[c], nullptr, lane);
                     if (lane > 0 && lane < K) {
                         AlignShared* rs = cluster.map_shared_rank(&sh, lane);
@@ -1335,9 +1533,10 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         // in order, and stops at the first that meets the strong Wolfe conditions. The rule
         // never looks past that candidate, so the outcome equals scoring all 8 at once, while
         // the common full step (alpha = 1 accepted) costs one candidate pass instead of 8.
-        for (int round = 0; line_search; ++round) {
-            const int c_lo = round == 0 ? 0 : (round == 1 ? 1 : 3);
-            const int c_hi = min(round == 0 ? 1 : (round == 1 ? 3 : LS_MAX), P.ls_cands);
+        for (int round = 0; line_search && sh.ls_active; ++round) {
+            const int c_lo = CPU_SEM ? 0 : (round == 0 ? 0 : (round == 1 ? 1 : 3));
+            const int c_hi =
+                CPU_SEM ? 1 : min(round == 0 ? 1 : (round == 1 ? 3 : LS_MAX), P.ls_cands);
             // candidate pass: score and gradient of each candidate pose of the round over this
             // rank's points, one candidate after another; FP64 warp sums of each candidate
             // kept in shared memory, summed over the CTA, then over the cluster by rank 0
@@ -1353,8 +1552,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
                           pz = __ldg(pts + 3 * (size_t)i + 2);
                     if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-                    point_terms_ls(m, s_off27, px, py, pz, sh.ls_fr[c], P.max_nb, P.d1f, P.d2f, a, lc,
-                                   nbl_smem + tid, THREADS);
+                    point_terms_ls<CPU_SEM>(m, s_off27, px, py, pz, sh.ls_fr[c], P.max_nb, P.d1f,
+                                            P.d2f, a, lc, nbl_smem + tid, THREADS);
                 }
                 double* wout = lsw + ((size_t)warp * LS_MAX + c) * LS_VALS;
                 warp_sum16(a, lane, LS_USED - 1, wout);
@@ -1387,7 +1586,9 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     __syncwarp();
                     if (lane == 0) {
                         AlignOut& o = P.out[jid];
-                        const int r = ls_decide(P, sh, o, it, (int)sh.tot[NACC], c_lo, c_hi);
+                        const int r = CPU_SEM ? mt_decide(P, sh, o, it)
+                                              : ls_decide(P, sh, o, it, (int)sh.tot[NACC], c_lo,
+                                                          c_hi);
                         if (r == 1) {
                             o.point_iters = point_iters;
                             o.corr_total = corr_total;
@@ -1396,12 +1597,18 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                         sh.done = r == 1;
                     }
                     __syncwarp();
-                    if (!sh.ls_more) make_frame_warp(sh.pose, false, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                    if (!sh.ls_more)
+                        make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
+                    else if (CPU_SEM)  // the search's next trial
+                        make_frame_warp(sh.ls_pose[0], true, sh.ls_fr[0], sh.ls_trig[0],
+                                        sh.ls_Ad[0], nullptr, lane);
                     if (lane > 0 && lane < K) {
                         AlignShared* rs = cluster.map_shared_rank(&sh, lane);
                         if (!sh.ls_more) {
                             for (int i = 0; i < 6; ++i) rs->pose[i] = sh.pose[i];
                             for (int i = 0; i < NFR; ++i) rs->fr[i] = sh.fr[i];
+                        } else if (CPU_SEM) {
+                            for (int i = 0; i < NFR; ++i) rs->ls_fr[0][i] = sh.ls_fr[0][i];
                         }
                         rs->done = sh.done;
                         rs->ls_more = sh.ls_more;
@@ -1903,14 +2110,13 @@ static int launch_queue_t(const AlignParams& p, uint32_t chunks, cudaStream_t s)
     return cuda_fail(e, "work-queue align launch");
 }
 
-template <int T, bool SEM, int CAP>
+template <int T, bool SEM, int CAP, bool LS>
 static cudaError_t launch_k(cudaLaunchConfig_t& cfg, const AlignParams& p, int K) {
-    cudaFuncSetAttribute(k_ndt_align<T, SEM, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    auto kern = k_ndt_align<T, SEM, CAP, LS>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cfg.dynamicSmemBytes);
-    if (K > 8)
-        cudaFuncSetAttribute(k_ndt_align<T, SEM, CAP>,
-                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    return cudaLaunchKernelEx(&cfg, k_ndt_align<T, SEM, CAP>, p);
+    if (K > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return cudaLaunchKernelEx(&cfg, kern, p);
 }
 
 template <int T, int CAP>
@@ -1921,9 +2127,8 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     // [max_nb][T] neighbour lists, [NACC - A_HTR][T] accumulators, then (line search)
     // [T/32][LS_MAX][LS_VALS] FP64 warp sums; the first two are multiples of 8 bytes (T is)
     cfg.dynamicSmemBytes = (size_t)T * (p.max_nb + NACC - A_HTR) * sizeof(uint32_t) +
-                           (p.ls_cands > 0 && p.semantics != NDT_SEMANTICS_CPU
-                                ? (size_t)(T / 32) * LS_MAX * LS_VALS * sizeof(double)
-                                : 0);
+                           (p.ls_cands > 0 ? (size_t)(T / 32) * LS_MAX * LS_VALS * sizeof(double)
+                                           : 0);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1932,8 +2137,11 @@ static int launch_t(const AlignParams& p, int K, cudaStream_t s) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = p.semantics == NDT_SEMANTICS_CPU ? launch_k<T, true, CAP>(cfg, p, K)
-                                                     : launch_k<T, false, CAP>(cfg, p, K);
+    // the CPU path's line search runs in the 128-register variant of the shape
+    cudaError_t e = p.semantics != NDT_SEMANTICS_CPU
+                        ? launch_k<T, false, CAP, true>(cfg, p, K)
+                        : (p.ls_cands > 0 ? launch_k<T, true, 128, true>(cfg, p, K)
+                                          : launch_k<T, true, CAP, false>(cfg, p, K));
     return cuda_fail(e, "ndt align launch");
 }
 

@@ -388,8 +388,7 @@ static bool config_ok(const ndt_config& c) {
            (R == 0 || R == 48 || R == 64 || R == 80 || R == 128) &&
            (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
            (c.cuda_graph == 0 || c.cuda_graph == 1) &&
-           (c.use_line_search == 0 ||
-            (c.use_line_search == 1 && c.semantics == NDT_SEMANTICS_GPU_GRAPH)) &&
+           (c.use_line_search == 0 || c.use_line_search == 1) &&
            c.work_queue >= -1 && c.work_queue <= 16 &&
            (c.work_queue <= 0 || (T != 128 || R == 0 || R == 64)) &&
            (c.work_queue <= 0 || (T != 512 || R == 0 || R == 128)) &&
@@ -774,7 +773,7 @@ static int log2_bucket(uint64_t v) {
 static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
     LaunchShape sh{0, 0, 128, 0};
     if (c->forced.cluster > 0) return c->forced;
-    const bool ls = c->cfg.use_line_search && c->cfg.semantics != NDT_SEMANTICS_CPU;
+    const bool ls = c->cfg.use_line_search != 0;
     if (c->cfg.work_queue > 0 && !ls) {
         sh.cluster = 1;
         sh.threads = c->cfg.threads_per_cta > 0 ? c->cfg.threads_per_cta : 256;
@@ -861,7 +860,8 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
         p.eps = (double)sqrtf(ef * ef);
     }
     p.status = (uint32_t*)c->d_status.p;
-    p.ls_cands = (c->cfg.use_line_search && !cpu) ? LS_MAX : 0;
+    // line search: the graph path's candidates, or (CPU path) the More-Thuente search
+    p.ls_cands = c->cfg.use_line_search ? LS_MAX : 0;
     p.ls_mu = LS_MU;
     p.ls_nu = LS_NU;
     p.trace = nullptr;
@@ -1565,7 +1565,7 @@ int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const 
     // work-queue candidates: (threads, registers, points per thread per chunk)
     const int QC[6][3] = {{256, 64, 2}, {256, 64, 4}, {256, 64, 8},
                           {256, 80, 4}, {128, 64, 4}, {512, 128, 2}};
-    const bool ls = c->cfg.use_line_search && c->cfg.semantics != NDT_SEMANTICS_CPU;
+    const bool ls = c->cfg.use_line_search != 0;
     std::vector<LaunchShape> cands;
     if (c->cfg.work_queue <= 0 || ls)
         for (int K : Ks)

@@ -175,6 +175,11 @@ struct QCtl {
 constexpr int LS_MAX = 8;
 constexpr double LS_MU = 1e-4;
 constexpr double LS_NU = 0.9;
+// Line search of the CPU path: the More-Thuente search with MoreThuenteConfig::default()
+// (more_thuente.rs:36-46): steps in [1e-9, 0.1], at most 10 iterations after the first trial
+constexpr double MT_STEP_MIN = 1e-9;
+constexpr double MT_STEP_MAX = 0.1;
+constexpr int MT_MAX_ITER = 10;
 
 struct LaunchShape {
     int cluster;

@@ -187,8 +187,7 @@ class NdtScanMatcher:
             trans_epsilon=config.trans_epsilon, step_size=config.step_size,
             outlier_ratio=config.outlier_ratio,
             min_points_per_voxel=config.min_points_per_voxel,
-            semantics=(capi.SEMANTICS_GPU_GRAPH if config.use_line_search
-                       else self._semantics(config.use_gpu)),
+            semantics=self._semantics(config.use_gpu),
             cluster_size=config.cluster_size, threads_per_cta=config.threads_per_cta,
             device=config.device, use_line_search=int(config.use_line_search))
         self._has_target = False
@@ -199,12 +198,9 @@ class NdtScanMatcher:
 
     def _with(self, use_gpu):
         """Selects the path: the graph kernels (align_gpu) or NdtOptimizer::align. With
-        use_line_search the graph path runs its parallel line search; the CPU path's
-        More-Thuente search (solver.rs:268-280) is not built, so that combination raises."""
+        use_line_search the graph path runs its parallel line search and the CPU path its
+        More-Thuente search (solver.rs:268-280)."""
         want = self._semantics(use_gpu)
-        if want == capi.SEMANTICS_CPU and self.config.use_line_search:
-            raise NotImplementedError(
-                "the CPU path's More-Thuente line search is not built; use the GPU path")
         if self._ctx.cfg.semantics != want:
             self._ctx.configure(semantics=want)
 

@@ -80,11 +80,13 @@ typedef struct ndt_config {
     int32_t cuda_graph;            /* 1: batches run as captured CUDA graphs (replayed while
                                       the batch shape repeats); 0: direct launches */
     int32_t use_line_search;       /* NdtScanMatcherConfig::use_line_search (ndt.rs:69, default
-                                      false): the graph path's parallel line search, 8 step
-                                      candidates 0.618^k under the strong Wolfe conditions
-                                      (ndt_graph_kernels.cu:388-430,473-570,626-710) instead
-                                      of the clamped step; graph semantics only (the CPU
-                                      path's More-Thuente search is not built) */
+                                      false). Graph semantics: the parallel line search, 8
+                                      step candidates 0.618^k under the strong Wolfe
+                                      conditions (ndt_graph_kernels.cu:388-430,473-570,
+                                      626-710) instead of the clamped step. CPU semantics: the
+                                      More-Thuente search of NdtOptimizer::align
+                                      (solver.rs:268-280,640-700; more_thuente.rs), one trial
+                                      pass per search step. Both run on the cluster kernel */
     int32_t work_queue;            /* Newton-kernel form: n > 0 the work-queue kernel (a
                                       persistent grid claiming chunks of n points per thread
                                       of any alignment's iteration); -1 one thread-block

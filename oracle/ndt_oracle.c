@@ -1001,6 +1001,155 @@ void or_score_gpu_sem(const or_grid* g, const float* src, size_t n, const double
 /* Alignment loops                                                                      */
 /* ------------------------------------------------------------------------------------ */
 /* count_oscillation (src/ndt_cuda/src/optimization/oscillation.rs:46-99) over positions */
+/* MoreThuenteConfig::default() (more_thuente.rs:36-46) */
+#define MT_STEP_MIN 1e-9
+#define MT_STEP_MAX 0.1
+#define MT_MAX_ITER 10
+
+/* ---- More-Thuente line search (CPU path with use_line_search) ----
+ * more_thuente_search (src/ndt_cuda/src/optimization/more_thuente.rs:236-410) after More &
+ * Thuente (1994), with the interpolants of Sun & Yuan (2006, eqs. 2.4.2, 2.4.5, 2.4.52). The
+ * score is maximised, so the search minimises phi = -score. Until a trial has psi <= 0 and
+ * psi' >= 0 the interval [a_l, a_u] is kept on psi(a) = phi(a) - phi(0) - mu phi'(0) a, then
+ * on phi itself. */
+
+/* minimiser of the cubic through (a, fa, ga) and (b, fb, gb); *ok = 0 when it is complex */
+static double mt_cubic(double a, double fa, double ga, double b, double fb, double gb, int* ok) {
+    const double z = 3.0 * (fb - fa) / (b - a) - gb - ga;
+    const double w2 = z * z - gb * ga;
+    if (w2 < 0.0) {
+        *ok = 0;
+        return 0.0;
+    }
+    *ok = 1;
+    const double w = sqrt(w2);
+    return a + (b - a) * (w - ga - z) / (gb - ga + 2.0 * w);
+}
+
+/* trial_value_selection (more_thuente.rs:83-194): l = best end, u = other end, t = trial */
+static double mt_next(double al, double fl, double gl, double au, double fu, double gu,
+                      double at, double ft, double gt) {
+    int ok;
+    if (ft > fl) { /* case 1: bracketed by [al, at] */
+        const double ac = mt_cubic(al, fl, gl, at, ft, gt, &ok);
+        if (!ok) return al - 0.5 * (al - at) * gl / (gl - (fl - ft) / (al - at));
+        const double den = gl - (fl - ft) / (al - at);
+        if (fabs(den) < 1e-15) return ac;
+        const double aq = al - 0.5 * (al - at) * gl / den;
+        return fabs(ac - al) < fabs(aq - al) ? ac : 0.5 * (aq + ac);
+    }
+    if (gt * gl < 0.0) { /* case 2: slopes of opposite sign */
+        const double ac = mt_cubic(al, fl, gl, at, ft, gt, &ok);
+        const double as = al - (al - at) / (gl - gt) * gl;
+        if (!ok) return as;
+        return fabs(ac - at) >= fabs(as - at) ? ac : as;
+    }
+    if (fabs(gt) <= fabs(gl)) { /* case 3: slope shrinking in magnitude */
+        double ac = mt_cubic(al, fl, gl, at, ft, gt, &ok);
+        if (!ok) ac = at > al ? at + 0.66 * (au - at) : at - 0.66 * (at - au);
+        const double as = fabs(gl - gt) > 1e-15 ? al - (al - at) / (gl - gt) * gl : ac;
+        const double an = fabs(ac - at) < fabs(as - at) ? ac : as;
+        const double lim = at + 0.66 * (au - at);
+        return at > al ? fmin(lim, an) : fmax(lim, an);
+    }
+    /* case 4: cubic through the trial and the other end */
+    const double ac = mt_cubic(au, fu, gu, at, ft, gt, &ok);
+    return ok ? ac : 0.5 * (al + au);
+}
+
+/* update_interval (more_thuente.rs:196-234); 1 when the interval has shrunk to a point */
+static int mt_update(double* al, double* fl, double* gl, double* au, double* fu, double* gu,
+                     double at, double ft, double gt) {
+    if (ft > *fl) {
+        *au = at; *fu = ft; *gu = gt;
+        return 0;
+    }
+    const double side = gt * (*al - at);
+    if (side > 0.0) {
+        *al = at; *fl = ft; *gl = gt;
+        return 0;
+    }
+    if (side < 0.0) {
+        *au = *al; *fu = *fl; *gu = *gl;
+        *al = at; *fl = ft; *gl = gt;
+        return 0;
+    }
+    return 1;
+}
+
+static double mt_clamp(double a, double lo, double hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+double or_mt_search(or_mt_fn f, void* ctx, double score0, double deriv0, double initial,
+                    double step_min, double step_max, double mu, double nu, int32_t max_iter,
+                    int32_t* converged, int32_t* evals) {
+    *converged = 0;
+    *evals = 0;
+    if (deriv0 <= 0.0) return 0.0;
+    const double phi0 = -score0, dphi0 = -deriv0;
+    double at = mt_clamp(initial, step_min, step_max), sc, dr;
+    f(at, ctx, &sc, &dr);
+    ++*evals;
+    double phi = -sc, dphi = -dr;
+    if (step_max - step_min < 0.0) {
+        *converged = 1;
+        return at;
+    }
+    double al = 0.0, au = 0.0;  /* both ends at 0, on psi: psi(0) = 0, psi'(0) */
+    double fl = phi0 - phi0 - mu * dphi0 * al, fu = phi0 - phi0 - mu * dphi0 * au;
+    double gl = dphi0 - mu * dphi0, gu = gl;
+    int open = 1;
+    double psi = phi - phi0 - mu * dphi0 * at, dpsi = dphi - mu * dphi0;
+    for (int it = 0; it < max_iter; ++it) {
+        if (psi <= 0.0 && fabs(dphi) <= nu * fabs(dphi0)) {
+            *converged = 1;
+            return at;
+        }
+        at = open ? mt_next(al, fl, gl, au, fu, gu, at, psi, dpsi)
+                  : mt_next(al, fl, gl, au, fu, gu, at, phi, dphi);
+        at = mt_clamp(at, step_min, step_max);
+        f(at, ctx, &sc, &dr);
+        ++*evals;
+        phi = -sc;
+        dphi = -dr;
+        psi = phi - phi0 - mu * dphi0 * at;
+        dpsi = dphi - mu * dphi0;
+        if (open && psi <= 0.0 && dpsi >= 0.0) {
+            open = 0;
+            fl = fl + phi0 - mu * dphi0 * al;
+            gl += mu * dphi0;
+            fu = fu + phi0 - mu * dphi0 * au;
+            gu += mu * dphi0;
+        }
+        const int done = open ? mt_update(&al, &fl, &gl, &au, &fu, &gu, at, psi, dpsi)
+                              : mt_update(&al, &fl, &gl, &au, &fu, &gu, at, phi, dphi);
+        if (done) break;
+    }
+    return at;
+}
+
+/* one trial of the CPU path's line search: score and directional derivative at
+ * pose + alpha dir (line_search_with_regularization, solver.rs:640-700; regularisation off) */
+typedef struct {
+    const or_grid* g;
+    const float* src;
+    size_t n;
+    const double* pose;
+    const double* dir;
+    double d1, d2;
+} mt_ctx;
+
+static int mt_eval_cpu(double alpha, void* vctx, double* score, double* deriv) {
+    const mt_ctx* c = (const mt_ctx*)vctx;
+    double p[6], gr[6], H[36];
+    for (int i = 0; i < 6; ++i) p[i] = c->pose[i] + c->dir[i] * alpha;
+    int32_t nc;
+    or_derivatives_cpu(c->g, c->src, c->n, p, c->d1, c->d2, score, gr, H, &nc);
+    double d = 0.0;
+    for (int i = 0; i < 6; ++i) d += gr[i] * c->dir[i];
+    *deriv = d;
+    return 0;
+}
+
 static int count_osc(const double* pos, int np) {
     int cnt = 0, best = 0;
     for (int i = 2; i < np; ++i) {
@@ -1035,8 +1184,26 @@ static void finish_result(const or_grid* g, const float* src, size_t n, const or
 
 /* NdtOptimizer::align, src/ndt_cuda/src/optimization/solver.rs:135-305 (no line search,
  * no GNSS regularisation: the library defaults). */
+static void align_cpu_impl(const or_grid* g, const float* src, size_t n,
+                           const double* pose_in, const or_config* cfg, or_result* out,
+                           double* trace);
+
 void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* pose_in,
                   const or_config* cfg, or_result* out) {
+    align_cpu_impl(g, src, n, pose_in, cfg, out, NULL);
+}
+
+/* as or_align_cpu, plus a 48-double record per iteration in trace (max_iterations records,
+ * the layout of or_align_gpu_sem_trace: it, score, correspondences, pose before the step,
+ * gradient, Hessian upper triangle, then the step taken in fields 36-41) */
+void or_align_cpu_trace(const or_grid* g, const float* src, size_t n, const double* pose_in,
+                        const or_config* cfg, or_result* out, double* trace) {
+    align_cpu_impl(g, src, n, pose_in, cfg, out, trace);
+}
+
+static void align_cpu_impl(const or_grid* g, const float* src, size_t n,
+                           const double* pose_in, const or_config* cfg, or_result* out,
+                           double* trace) {
     double d1, d2;
     or_gauss_params(cfg->resolution, cfg->outlier_ratio, &d1, &d2);
     memset(out, 0, sizeof *out);
@@ -1055,6 +1222,19 @@ void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* po
         double sc, gr[6], H[36];
         int32_t nc;
         or_derivatives_cpu(g, src, n, pose, d1, d2, &sc, gr, H, &nc);
+        double* tr = trace ? trace + 48 * (size_t)it : NULL;
+        if (tr) {
+            tr[0] = it;
+            tr[1] = sc;
+            tr[2] = nc;
+            for (int i = 0; i < 6; ++i) {
+                tr[3 + i] = pose[i];
+                tr[9 + i] = gr[i];
+            }
+            int u = 0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i; j < 6; ++j) tr[15 + u++] = H[i * 6 + j];
+        }
         if (nc < cfg->min_correspondences) {
             if (it == 0) {
                 memcpy(out->pose, pose_in, sizeof out->pose);
@@ -1107,7 +1287,26 @@ void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* po
         if (gd <= 0.0)
             for (int i = 0; i < 6; ++i) dir[i] = -dir[i];
         double step = dn < cfg->step_size ? dn : cfg->step_size;
+        if (cfg->ls_candidates > 0) {
+            /* line_search_with_regularization (solver.rs:640-700): More-Thuente from
+             * step_size with MoreThuenteConfig::default(); step_max when it does not
+             * converge, step_size when the direction is not an ascent one */
+            double d0 = 0.0;
+            for (int i = 0; i < 6; ++i) d0 += gr[i] * dir[i];
+            if (d0 <= 0.0) {
+                step = cfg->step_size;
+            } else {
+                mt_ctx c = {g, src, n, pose, dir, d1, d2};
+                int32_t conv, ev;
+                const double a = or_mt_search(mt_eval_cpu, &c, sc, d0, cfg->step_size,
+                                              MT_STEP_MIN, MT_STEP_MAX, cfg->ls_mu, cfg->ls_nu,
+                                              MT_MAX_ITER, &conv, &ev);
+                step = conv ? a : MT_STEP_MAX;
+            }
+        }
         for (int i = 0; i < 6; ++i) pose[i] += dir[i] * step;
+        if (tr)
+            for (int i = 0; i < 6; ++i) tr[36 + i] = dir[i] * step;
         memcpy(hist + 3 * nh, pose, 3 * sizeof(double));
         nh++;
     }

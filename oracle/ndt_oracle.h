@@ -54,10 +54,22 @@ typedef struct {
     double step_size;
     double outlier_ratio;
     int32_t min_correspondences;  /* 10 in OptimizationConfig::default() */
-    int32_t ls_candidates;        /* graph path line search: 0 off, else candidates (<= 8) */
+    int32_t ls_candidates;        /* line search: 0 off. Graph path: candidates (<= 8);
+                                     CPU path: any value > 0 turns on the More-Thuente
+                                     search (MoreThuenteConfig::default: step in
+                                     [1e-9, 0.1], at most 10 iterations) */
     double ls_mu;                 /* Armijo constant (PipelineV2Config::armijo_mu, 1e-4) */
     double ls_nu;                 /* curvature constant (PipelineV2Config::wolfe_nu, 0.9) */
 } or_config;
+
+/* More-Thuente line search (more_thuente.rs:236-410): maximises score(alpha) along a
+ * direction from score0 with slope deriv0 > 0, first trial `initial` clamped to
+ * [step_min, step_max]. f(alpha, ctx, &score, &deriv) evaluates a trial and returns 0.
+ * Returns the step; *converged: the strong Wolfe conditions held at it; *evals: trials. */
+typedef int (*or_mt_fn)(double alpha, void* ctx, double* score, double* deriv);
+double or_mt_search(or_mt_fn f, void* ctx, double score0, double deriv0, double initial,
+                    double step_min, double step_max, double mu, double nu, int32_t max_iter,
+                    int32_t* converged, int32_t* evals);
 
 /* derivatives/types.rs:61-75 */
 void or_gauss_params(double resolution, double outlier_ratio, double* d1, double* d2);
@@ -121,6 +133,8 @@ void or_align_cpu(const or_grid* g, const float* src, size_t n, const double* po
                   const or_config* cfg, or_result* out);
 void or_align_gpu_sem(const or_grid* g, const float* src, size_t n, const double* pose_in,
                       const or_config* cfg, or_result* out);
+void or_align_cpu_trace(const or_grid* g, const float* src, size_t n, const double* pose_in,
+                        const or_config* cfg, or_result* out, double* trace);
 void or_align_gpu_sem_trace(const or_grid* g, const float* src, size_t n,
                             const double* pose_in, const or_config* cfg, or_result* out,
                             double* trace);

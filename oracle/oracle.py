@@ -53,6 +53,26 @@ def config(resolution=2.0, max_iterations=30, max_neighbors=8, trans_epsilon=0.0
                     outlier_ratio, min_correspondences, ls_candidates, ls_mu, ls_nu)
 
 
+MT_FN = C.CFUNCTYPE(C.c_int, C.c_double, C.c_void_p, C.POINTER(C.c_double),
+                    C.POINTER(C.c_double))
+
+
+def mt_search(score_and_derivative, score0, deriv0, initial, step_min=1e-9, step_max=0.1,
+              mu=1e-4, nu=0.9, max_iterations=10):
+    """The CPU path's More-Thuente line search (more_thuente_search) on a Python function
+    alpha -> (score, directional derivative); returns (step, converged, evaluations)."""
+    def cb(alpha, _ctx, sc, dr):
+        s, d = score_and_derivative(alpha)
+        sc[0] = s
+        dr[0] = d
+        return 0
+    fn = MT_FN(cb)
+    conv, ev = C.c_int32(), C.c_int32()
+    a = lib().or_mt_search(fn, None, score0, deriv0, initial, step_min, step_max, mu, nu,
+                           max_iterations, C.byref(conv), C.byref(ev))
+    return a, bool(conv.value), ev.value
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -99,6 +119,8 @@ def lib():
                                         C.POINTER(OrResult)]),
             "or_align_gpu_sem_trace": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
                                               C.POINTER(OrResult), f64p]),
+            "or_align_cpu_trace": (None, [P, f32p, C.c_size_t, f64p, C.POINTER(OrConfig),
+                                          C.POINTER(OrResult), f64p]),
             "or_align_batch": (None, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), f64p,
                                       C.c_size_t, C.POINTER(OrConfig), C.c_int, C.c_int,
                                       C.POINTER(OrResult)]),
@@ -111,6 +133,10 @@ def lib():
             "or_pose_to_T34_zyx": (None, [f64p, f64p]),
             "or_eigen_sym3": (None, [f64p, f64p, f64p]),
             "or_eigen_sym6": (None, [f64p, f64p, f64p]),
+            "or_mt_search": (C.c_double, [MT_FN, P, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_int32, C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -247,15 +273,17 @@ class Grid:
         fn(self.h, src, len(src), pose, C.byref(c), C.byref(r))
         return r.as_dict()
 
-    def align_trace(self, src, pose, **cfg):
-        """Graph-kernel semantics with the per-iteration trace (48 doubles per iteration)."""
+    def align_trace(self, src, pose, semantics="gpu", **cfg):
+        """Alignment with the per-iteration trace (48 doubles per iteration: it, score,
+        correspondences, pose before the step, gradient, Hessian upper triangle, ...)."""
         c = config(resolution=self.res, **cfg)
         r = OrResult()
         src = _f32(src)
         tr = np.full((c.max_iterations, 48), np.nan)
-        lib().or_align_gpu_sem_trace(self.h, src, len(src), np.ascontiguousarray(pose, np.float64),
-                                     C.byref(c), C.byref(r), tr)
-        return r.as_dict(), tr[:r.iterations]
+        fn = lib().or_align_gpu_sem_trace if semantics == "gpu" else lib().or_align_cpu_trace
+        fn(self.h, src, len(src), np.ascontiguousarray(pose, np.float64), C.byref(c),
+           C.byref(r), tr)
+        return r.as_dict(), tr[~np.isnan(tr[:, 0])]
 
     def align_batch(self, scans, poses, semantics="gpu", nthreads=0, **cfg):
         c = config(resolution=self.res, **cfg)

@@ -55,12 +55,9 @@ def test_config_defaults_mirror_reference():
     assert cfg.use_line_search == 0  # NdtScanMatcherConfig::default, ndt.rs:99
 
 
-def test_line_search_only_on_the_graph_path():
-    """The configuration is checked before any device call: line search with the CPU path's
-    semantics (More-Thuente, not built) is an invalid argument, on any machine."""
-    with pytest.raises(capi.NdtError) as e:
-        capi.Context(semantics=capi.SEMANTICS_CPU, use_line_search=1)
-    assert e.value.code == -1
+def test_line_search_config_checked():
+    """The configuration is checked before any device call: use_line_search is 0 or 1 (both
+    semantics take it: the graph path's candidates, the CPU path's More-Thuente search)."""
     with pytest.raises(capi.NdtError) as e:
         capi.Context(use_line_search=2)
     assert e.value.code == -1

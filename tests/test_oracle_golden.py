@@ -251,6 +251,41 @@ def test_oracle_line_search(oracle, single_cases):
         assert steps.max() > 0.1  # a full step beyond the clamp was taken
 
 
+def test_oracle_more_thuente_known_answers(oracle):
+    """The CPU path's More-Thuente search against the reference's own unit tests
+    (src/ndt_cuda/src/optimization/more_thuente.rs:426-545)."""
+    # test_quadratic_minimization: score = -(x - 2)^2 from x = 0, step in [0, 5], first
+    # trial 1: the Wolfe conditions already hold there, so the search stops in [1, 2.5]
+    def quad(a):
+        return -(a - 2.0) ** 2, -2.0 * (a - 2.0)
+    a, conv, ev = oracle.mt_search(quad, -4.0, 4.0, 1.0, step_min=0.0, step_max=5.0,
+                                   max_iterations=20)
+    assert conv and 1.0 <= a <= 2.5 and quad(a)[0] > -4.0 and ev >= 1
+    # test_no_improvement_direction / test_negative_derivative: no ascent, no step
+    for d0 in (0.0, -1.0):
+        a, conv, ev = oracle.mt_search(lambda _a: (0.0, 0.0), 1.0, d0, 0.1)
+        assert a == 0.0 and not conv and ev == 0
+    # test_simple_line_search: score = 10 a - a^2 on [0, 10] from a = 1
+    a, conv, _ = oracle.mt_search(lambda x: (10 * x - x * x, 10 - 2 * x), 0.0, 10.0, 1.0,
+                                  step_min=0.0, step_max=10.0, max_iterations=20)
+    assert a > 0.0 and 10 * a - a * a > 0.0
+    # with the default bounds the trials never exceed step_max = 0.1
+    a, conv, _ = oracle.mt_search(quad, -4.0, 4.0, 0.1)
+    assert a <= 0.1 + 1e-15
+
+
+def test_oracle_cpu_line_search(oracle, single_cases):
+    """CPU path with use_line_search: every Newton step is sized by the More-Thuente search
+    (at most 0.1); the alignment reaches the same optimum as without it."""
+    for case in single_cases:
+        grid = oracle.Grid(case.map_points, 2.0)
+        plain = grid.align(case.scan, case.guess, semantics="cpu")
+        ls = grid.align(case.scan, case.guess, semantics="cpu", ls_candidates=8)
+        assert ls["status"] in (0, 1)
+        if plain["converged"] and ls["converged"]:
+            assert np.abs(ls["pose"][:3] - plain["pose"][:3]).max() < 0.05
+
+
 def test_half_cube_scenarios(oracle):
     """Ports of src/ndt_cuda/src/ndt.rs:1490-1600 (within 2 m, positive score/NVTL)."""
     m = synth.half_cubic_pcd() + np.array([100, 100, 0], np.float32)
