@@ -29,6 +29,7 @@ EXPORTS = [
     "ndt_align", "ndt_align_multi_pose", "ndt_align_batch", "ndt_align_batch_device",
     "ndt_batch_submit", "ndt_batch_poll", "ndt_batch_wait",
     "ndt_autotune", "ndt_eval_batch", "ndt_batch_timings", "ndt_initial_pose_search",
+    "ndt_tpe_propose",
     "ndt_pnet_config_default", "ndt_pnet_create", "ndt_pnet_destroy", "ndt_pnet_get_config",
     "ndt_pnet_add_map", "ndt_pnet_add_scan", "ndt_pnet_train", "ndt_pnet_propose",
     "ndt_pnet_debug_grad", "ndt_pnet_params", "ndt_learned_pose_search", "ndt_gemm_bf16",
@@ -80,7 +81,7 @@ class TuneResult(C.Structure):
 
 
 class ParticleConfig(C.Structure):
-    _fields_ = [("num_particles", C.c_uint32), ("reserved", C.c_uint32),
+    _fields_ = [("num_particles", C.c_uint32), ("guided", C.c_uint32),
                 ("xy_range", C.c_double), ("yaw_range", C.c_double),
                 ("z_sigma", C.c_double), ("roll_pitch_sigma", C.c_double),
                 ("seed", C.c_uint64)]
@@ -182,6 +183,8 @@ def load(build_if_missing=True):
         "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
         "ndt_initial_pose_search": (C.c_int, [P, P, C.c_uint64, C.POINTER(ParticleConfig),
                                               P, P]),
+        "ndt_tpe_propose": (C.c_int, [C.POINTER(ParticleConfig), C.c_uint64, C.c_uint64, P, P,
+                                      C.c_uint64, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
         "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
         "ndt_stats_reset": (C.c_int, [P]),
@@ -239,6 +242,21 @@ def result_dict(r: Result):
         "status": r.status,
     }
 
+
+
+def tpe_propose(query, particle, prior, trials, num_particles=200, guided=100, xy_range=2.0,
+                yaw_range=np.pi, z_sigma=0.0, roll_pitch_sigma=0.0, seed=0):
+    """The TPE proposal of a guided particle (host only, no device): trials are the query's
+    aligned results so far in the order they were aligned, rows (x, y, yaw, exp(-score/10))."""
+    pc = ParticleConfig(num_particles=num_particles, guided=guided, xy_range=xy_range,
+                        yaw_range=yaw_range, z_sigma=z_sigma, roll_pitch_sigma=roll_pitch_sigma,
+                        seed=seed)
+    t = np.ascontiguousarray(np.asarray(trials, np.float64).reshape(-1, 4))
+    pr = np.ascontiguousarray(prior, np.float64)
+    out = np.zeros(6)
+    check(load().ndt_tpe_propose(C.byref(pc), query, particle, pr.ctypes.data, t.ctypes.data,
+                                 len(t), out.ctypes.data))
+    return out
 
 class Context:
     """Thin owner of an ndt_ctx*: every method is one C-ABI call."""
@@ -399,9 +417,10 @@ class Context:
 
     def initial_pose_search(self, queries, priors, num_particles=200, xy_range=2.0,
                             yaw_range=np.pi, z_sigma=0.0, roll_pitch_sigma=0.0, seed=0,
-                            return_particles=False):
+                            return_particles=False, guided=0):
         """Batched multi-particle search; returns one estimate dict per query (and, when
-        asked, every particle's result, query-major)."""
+        asked, every particle's result, query-major). guided: the last particles of each
+        query that are TPE-guided (the reference's guided phase)."""
         qs = [as_xyz(q) for q in queries]
         m = len(qs)
         arr = (Scan * m)()
@@ -410,7 +429,7 @@ class Context:
             arr[i].num_points = len(s)
             for k in range(6):
                 arr[i].initial_pose[k] = float(pose[k])
-        pc = ParticleConfig(num_particles=num_particles, xy_range=xy_range,
+        pc = ParticleConfig(num_particles=num_particles, guided=guided, xy_range=xy_range,
                             yaw_range=yaw_range, z_sigma=z_sigma,
                             roll_pitch_sigma=roll_pitch_sigma, seed=seed)
         est = (PoseEstimate * m)()

@@ -1326,6 +1326,93 @@ static void make_particle(const ndt_particle_config& pc, uint64_t q, uint64_t k,
     }
 }
 
+// Particle k of query q, candidate c of a TPE proposal (c = 0: the particle's own draw, the
+// one make_particle gives): the same sampler on a stream whose seed mixes in c.
+static void draw_particle(const ndt_particle_config& pc, uint64_t q, uint64_t k, uint64_t c,
+                          const double* prior, double* pose) {
+    ndt_particle_config p = pc;
+    p.seed = pc.seed ^ (0x94d049bb133111ebull * c);
+    make_particle(p, q, k, prior, pose);
+}
+
+// ---- TPE-guided particles (estimate_initial_pose's guided phase, initial_pose.rs:280-420;
+// TreeStructuredParzenEstimator, cuda_ndt_matcher/src/tpe.rs) ----
+// A trial is an aligned particle: x, y, yaw of its result and exp(-score / 10); a query's
+// trials are kept best first, equal scores in arrival order (a stable sort).
+struct TpeTrial {
+    double x, y, yaw, score;
+};
+
+constexpr double TPE_PI = 3.14159265358979323846;
+constexpr int TPE_CANDIDATES = 100;  // N_EI_CANDIDATES
+
+static double tpe_log_sum_exp(const std::vector<double>& v) {
+    if (v.empty()) return -INFINITY;
+    double m = -INFINITY;
+    for (double x : v) m = std::max(m, x);
+    if (std::isinf(m)) return m;
+    double s = 0.0;
+    for (double x : v) s += std::exp(x - m);
+    return m + std::log(s);
+}
+
+// compute_log_likelihood_ratio (tpe.rs:160-196): Gaussian kernels of widths 0.25 m, 0.25 m
+// and 2.5 deg on x, y and the wrapped yaw difference around every trial; the best `above`
+// trials form the good set, the rest the bad set, each weighted by its size; the ratio is
+// log p_good - 5 log p_bad.
+static double tpe_ratio(const std::vector<TpeTrial>& t, size_t above, const double* in) {
+    const size_t n = t.size();
+    if (n == 0 || above == 0 || above >= n) return 0.0;
+    const double sig[3] = {0.25, 0.25, 2.5 * TPE_PI / 180.0};
+    const double lsig = std::log(sig[0]) + std::log(sig[1]) + std::log(sig[2]);
+    const double wa = std::log(1.0 / (double)above), wb = std::log(1.0 / (double)(n - above));
+    std::vector<double> a, b;
+    a.reserve(above);
+    b.reserve(n - above);
+    for (size_t i = 0; i < n; ++i) {
+        double d[3] = {in[0] - t[i].x, in[1] - t[i].y, in[5] - t[i].yaw};
+        while (d[2] >= TPE_PI) d[2] -= 2.0 * TPE_PI;
+        while (d[2] < -TPE_PI) d[2] += 2.0 * TPE_PI;
+        double lp = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double r = d[k] / sig[k];
+            lp += -0.5 * r * r;
+        }
+        lp -= lsig;
+        if (i < above)
+            a.push_back(lp + wa);
+        else
+            b.push_back(lp + wb);
+    }
+    return tpe_log_sum_exp(a) - tpe_log_sum_exp(b) * 5.0;
+}
+
+// get_next_input (tpe.rs:98-150): a random draw while the good set is empty, else the best of
+// 100 further draws by the likelihood ratio (the first draw stands when no ratio beats it)
+static void tpe_propose(const ndt_particle_config& pc, uint64_t q, uint64_t k,
+                        const double* prior, const std::vector<TpeTrial>& trials, double* pose) {
+    const size_t n = trials.size();
+    const size_t above = n ? std::min<size_t>(std::max<size_t>(n / 10, 1), 10) : 0;
+    draw_particle(pc, q, k, 0, prior, pose);
+    if (above == 0) return;
+    double best = -INFINITY, cand[6];
+    for (int c = 1; c <= TPE_CANDIDATES; ++c) {
+        draw_particle(pc, q, k, (uint64_t)c, prior, cand);
+        const double r = tpe_ratio(trials, above, cand);
+        if (r > best) {
+            best = r;
+            for (int i = 0; i < 6; ++i) pose[i] = cand[i];
+        }
+    }
+}
+
+static void tpe_add(std::vector<TpeTrial>& t, const ndt_result& r) {
+    const TpeTrial x{r.pose[0], r.pose[1], r.pose[5], std::exp(-r.score / 10.0)};
+    t.insert(std::upper_bound(t.begin(), t.end(), x,
+                              [](const TpeTrial& a, const TpeTrial& b) { return a.score > b.score; }),
+             x);
+}
+
 static int check_queries(const ndt_scan* queries, uint64_t nq) {
     for (uint64_t q = 0; q < nq; ++q) {
         if (queries[q].num_points == 0) {
@@ -1343,13 +1430,10 @@ static int check_queries(const ndt_scan* queries, uint64_t nq) {
 
 // np starting poses per query (starts: nq * np * 6) aligned in one launch, each scored by
 // NVTL at its aligned pose, then select_best_particle per query.
-static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, uint64_t np,
-                              const double* starts, ndt_pose_estimate* out,
-                              ndt_result* particles) {
-    if (nq * np > 0xFFFFFFull) {
-        set_error("too many particles in one search (queries x particles > 2^24)");
-        return NDT_ERR_CAPACITY;
-    }
+// Uploads the queries' points once (c->d_in; qoff: each query's first point) for the
+// particle alignments that follow.
+static int stage_queries(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
+                         std::vector<uint64_t>& qoff) {
     int rc;
     cudaSetDevice(c->device);
     uint64_t total = 0;
@@ -1365,33 +1449,41 @@ static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, 
         }
         total += queries[q].num_points;
     }
-    // each query's points are uploaded once; all of its particles share them
     if ((rc = pin_reserve(c->h_pts, total * 12 + 16)) || (rc = dev_reserve(c->d_in, total * 12 + 16)))
         return rc;
-    std::vector<AlignJob> jobs(nq * np);
-    std::vector<uint64_t> ns(nq * np), qoff(nq);
+    qoff.assign(nq, 0);
     uint64_t off = 0;
     for (uint64_t q = 0; q < nq; ++q) {
         qoff[q] = off;
+        off += queries[q].num_points;
+    }
+    stage_scans(c, queries, nq, qoff, total);
+    return NDT_OK;
+}
+
+// np particles per query from starts (query-major, 6 per particle) against the staged
+// points, in one launch; results query-major into res.
+static int align_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
+                        const std::vector<uint64_t>& qoff, uint64_t np, const double* starts,
+                        ndt_result* res) {
+    std::vector<AlignJob> jobs(nq * np);
+    std::vector<uint64_t> ns(nq * np);
+    for (uint64_t q = 0; q < nq; ++q)
         for (uint64_t k = 0; k < np; ++k) {
             AlignJob& j = jobs[q * np + k];
-            j.offset = off;
+            j.offset = qoff[q];
             j.n = (uint32_t)queries[q].num_points;
             j.slot = (uint32_t)(q * np + k);
             for (int d = 0; d < 6; ++d) j.pose[d] = starts[6 * (q * np + k) + d];
             ns[q * np + k] = queries[q].num_points;
         }
-        off += queries[q].num_points;
-    }
-    stage_scans(c, queries, nq, qoff, total);
-    std::vector<ndt_result> local;
-    ndt_result* res = particles;
-    if (!res) {
-        local.resize(nq * np);
-        res = local.data();
-    }
-    if ((rc = run_align(c, (const float*)c->d_in.p, jobs, ns, res))) return rc;
-    // select_best_particle: highest selection score, the later particle on ties
+    return run_align(c, (const float*)c->d_in.p, jobs, ns, res);
+}
+
+// select_best_particle (particle.rs:36-42): the highest selection score (NVTL when positive,
+// else 5 exp(-score / 10)), the later particle on ties
+static void select_best(const ndt_result* res, uint64_t nq, uint64_t np, const double* starts,
+                        ndt_pose_estimate* out) {
     for (uint64_t q = 0; q < nq; ++q) {
         int64_t best = -1;
         double best_sel = -INFINITY;
@@ -1417,6 +1509,77 @@ static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, 
         e.iterations = r.iterations;
         e.converged = r.converged;
     }
+}
+
+static int search_from_starts(ndt_ctx* c, const ndt_scan* queries, uint64_t nq, uint64_t np,
+                              const double* starts, ndt_pose_estimate* out,
+                              ndt_result* particles) {
+    if (nq * np > 0xFFFFFFull) {
+        set_error("too many particles in one search (queries x particles > 2^24)");
+        return NDT_ERR_CAPACITY;
+    }
+    std::vector<uint64_t> qoff;
+    int rc;
+    if ((rc = stage_queries(c, queries, nq, qoff))) return rc;
+    std::vector<ndt_result> local;
+    ndt_result* res = particles;
+    if (!res) {
+        local.resize(nq * np);
+        res = local.data();
+    }
+    if ((rc = align_starts(c, queries, nq, qoff, np, starts, res))) return rc;
+    select_best(res, nq, np, starts, out);
+    return NDT_OK;
+}
+
+// The guided search: every query's first np - ng particles (startup) in one launch, then ng
+// rounds; in each, every query's TPE proposes its next particle from all of that query's
+// results so far (on the context's host threads), and the round's particles are aligned in
+// one launch. Each query's particles follow the reference's sequential loop; the queries
+// share the launches.
+static int search_guided(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
+                         const ndt_particle_config& pc, ndt_pose_estimate* out,
+                         ndt_result* particles) {
+    const uint64_t np = pc.num_particles, ng = pc.guided, n0 = np - ng;
+    std::vector<uint64_t> qoff;
+    int rc;
+    if ((rc = stage_queries(c, queries, nq, qoff))) return rc;
+    std::vector<ndt_result> local;
+    ndt_result* res = particles;
+    if (!res) {
+        local.resize(nq * np);
+        res = local.data();
+    }
+    std::vector<double> starts(nq * np * 6);
+    std::vector<std::vector<TpeTrial>> trials(nq);
+    if (n0 > 0) {
+        std::vector<double> s0(nq * n0 * 6);
+        std::vector<ndt_result> r0(nq * n0);
+        for (uint64_t q = 0; q < nq; ++q)
+            for (uint64_t k = 0; k < n0; ++k)
+                make_particle(pc, q, k, queries[q].initial_pose, &s0[6 * (q * n0 + k)]);
+        if ((rc = align_starts(c, queries, nq, qoff, n0, s0.data(), r0.data()))) return rc;
+        for (uint64_t q = 0; q < nq; ++q)
+            for (uint64_t k = 0; k < n0; ++k) {
+                res[q * np + k] = r0[q * n0 + k];
+                std::memcpy(&starts[6 * (q * np + k)], &s0[6 * (q * n0 + k)], 6 * sizeof(double));
+                tpe_add(trials[q], r0[q * n0 + k]);
+            }
+    }
+    std::vector<double> sr(nq * 6);
+    std::vector<ndt_result> rr(nq);
+    for (uint64_t k = n0; k < np; ++k) {
+        c->pool.run(nq, [&](uint64_t q) {
+            tpe_propose(pc, q, k, queries[q].initial_pose, trials[q], &sr[6 * q]);
+        });
+        if ((rc = align_starts(c, queries, nq, qoff, 1, sr.data(), rr.data()))) return rc;
+        for (uint64_t q = 0; q < nq; ++q) {
+            res[q * np + k] = rr[q];
+            std::memcpy(&starts[6 * (q * np + k)], &sr[6 * q], 6 * sizeof(double));
+            tpe_add(trials[q], rr[q]);
+        }
+    }
+    select_best(res, nq, np, starts.data(), out);
     return NDT_OK;
 }
 
@@ -1430,7 +1593,7 @@ int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
     if (rc) return rc;
     if (nq == 0) return NDT_OK;
     const uint64_t np = pc->num_particles;
-    if (np == 0 || !(pc->xy_range >= 0.0) || !(pc->yaw_range >= 0.0) ||
+    if (np == 0 || pc->guided >= np || !(pc->xy_range >= 0.0) || !(pc->yaw_range >= 0.0) ||
         !(pc->z_sigma >= 0.0) || !(pc->roll_pitch_sigma >= 0.0)) {
         set_error("invalid particle configuration");
         return NDT_ERR_INVALID_ARGUMENT;
@@ -1440,11 +1603,30 @@ int ndt_initial_pose_search(ndt_ctx* c, const ndt_scan* queries, uint64_t nq,
         set_error("too many particles in one search (queries x particles > 2^24)");
         return NDT_ERR_CAPACITY;
     }
+    if (pc->guided > 0) return search_guided(c, queries, nq, *pc, out, particles);
     std::vector<double> starts(nq * np * 6);
     for (uint64_t q = 0; q < nq; ++q)
         for (uint64_t k = 0; k < np; ++k)
             make_particle(*pc, q, k, queries[q].initial_pose, &starts[6 * (q * np + k)]);
     return search_from_starts(c, queries, nq, np, starts.data(), out, particles);
+}
+
+int ndt_tpe_propose(const ndt_particle_config* pc, uint64_t query, uint64_t particle,
+                    const double prior[6], const double* trials, uint64_t num_trials,
+                    double pose_out[6]) {
+    if (!pc || !prior || !pose_out || (num_trials && !trials)) return NDT_ERR_INVALID_ARGUMENT;
+    std::vector<TpeTrial> t;
+    t.reserve(num_trials);
+    for (uint64_t i = 0; i < num_trials; ++i) {
+        const TpeTrial x{trials[4 * i], trials[4 * i + 1], trials[4 * i + 2], trials[4 * i + 3]};
+        t.insert(std::upper_bound(t.begin(), t.end(), x,
+                                  [](const TpeTrial& a, const TpeTrial& b) {
+                                      return a.score > b.score;
+                                  }),
+                 x);
+    }
+    tpe_propose(*pc, query, particle, prior, t, pose_out);
+    return NDT_OK;
 }
 
 int ndt_learned_pose_search(ndt_ctx* c, ndt_pnet* net, int32_t map_id, const ndt_scan* queries,

@@ -272,12 +272,18 @@ int ndt_batch_timings(ndt_ctx* ctx, double* start_ms, double* finish_ms, uint64_
  * particle, as Rust's max_by does. Particle k of query q starts from the query's prior pose
  * with x, y + U(-xy_range, xy_range), yaw + U(-yaw_range, yaw_range) (yaw_range = pi covers
  * the circle, like the reference's uniform yaw) and z, roll, pitch + N(0, sigma^2) — drawn
- * from a SplitMix64 stream seeded by (seed, q, k), so a search is reproducible. The
- * reference's later TPE-guided particles are sequential by design; this batched search draws
- * all of its particles up front. */
+ * from a SplitMix64 stream seeded by (seed, q, k), so a search is reproducible.
+ * With guided > 0 the last `guided` particles of each query are TPE-guided, as the reference's
+ * guided phase (initial_pose.rs:280-420; TreeStructuredParzenEstimator, tpe.rs; its defaults
+ * are 200 particles, 100 of them startup): each is the best of 100 further draws by the
+ * Parzen log-likelihood ratio over the query's aligned results so far (x, y, yaw kernels of
+ * 0.25 m, 0.25 m, 2.5 deg; the best max(1, min(10, n / 10)) results are the good set, score
+ * exp(-score / 10)). The startup particles go in one launch; the guided ones go in rounds, one
+ * particle of every query per launch. */
 typedef struct ndt_particle_config {
     uint32_t num_particles;        /* particles per query (200) */
-    uint32_t reserved;
+    uint32_t guided;               /* TPE-guided particles among them (0: all drawn up front;
+                                      the reference: 100); < num_particles */
     double xy_range;               /* 2.0 m */
     double yaw_range;              /* pi */
     double z_sigma;                /* 0 */
@@ -296,6 +302,13 @@ typedef struct ndt_pose_estimate {
     int32_t converged;
     int32_t reserved;
 } ndt_pose_estimate;
+
+/* The TPE proposal of a guided particle (host only): particle `particle` of query `query`
+ * from the query's prior and its num_trials aligned results so far, in the order they were
+ * aligned, 4 doubles each (x, y, yaw of the aligned pose, exp(-score / 10)). */
+int ndt_tpe_propose(const ndt_particle_config* cfg, uint64_t query, uint64_t particle,
+                    const double prior[6], const double* trials, uint64_t num_trials,
+                    double pose_out[6]);
 
 /* out: num_queries estimates; particles (optional, may be NULL): num_queries *
  * num_particles results, query-major. Each query's ndt_scan gives its points and prior. */

@@ -390,6 +390,70 @@ def particle(prior, q, k, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0, roll_pitch
     return p
 
 
+def tpe_propose(prior, q, k, trials, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0,
+                roll_pitch_sigma=0.0, seed=0):
+    """TPE proposal of guided particle k of query q (TreeStructuredParzenEstimator::
+    get_next_input, cuda_ndt_matcher/src/tpe.rs:98-196) from the query's aligned results so
+    far, rows (x, y, yaw, score) in arrival order: with the results sorted best first (stable),
+    the best max(1, min(10, n // 10)) form the good set; the particle's own draw stands unless
+    one of 100 further draws (candidate c: the particle stream with the seed xor
+    0x94d049bb133111eb * c) has a higher log p_good - 5 log p_bad, where p is a sum of Gaussian
+    kernels of 0.25 m, 0.25 m and 2.5 deg on x, y and the wrapped yaw difference."""
+    import math
+    rows = sorted((tuple(float(v) for v in t) for t in trials), key=lambda t: -t[3])
+    n = len(rows)
+    above = min(max(n // 10, 1), 10) if n else 0
+    kw = dict(xy_range=xy_range, yaw_range=yaw_range, z_sigma=z_sigma,
+              roll_pitch_sigma=roll_pitch_sigma)
+    pose = particle(prior, q, k, seed=seed, **kw)
+    if above == 0:
+        return pose
+    sig = (0.25, 0.25, 2.5 * math.pi / 180.0)
+    lsig = math.log(sig[0]) + math.log(sig[1]) + math.log(sig[2])
+    wa = math.log(1.0 / above)
+    wb = math.log(1.0 / (n - above)) if n > above else 0.0  # unused when n <= above
+
+    def lse(v):
+        if not v:
+            return -math.inf
+        m = -math.inf
+        for x in v:
+            m = max(m, x)
+        if math.isinf(m):
+            return m
+        acc = 0.0
+        for x in v:
+            acc += math.exp(x - m)
+        return m + math.log(acc)
+
+    def ratio(c):
+        if above >= n:
+            return 0.0
+        a, b = [], []
+        for i, (x, y, yaw, _) in enumerate(rows):
+            d = [float(c[0]) - x, float(c[1]) - y, float(c[5]) - yaw]
+            while d[2] >= math.pi:
+                d[2] -= 2.0 * math.pi
+            while d[2] < -math.pi:
+                d[2] += 2.0 * math.pi
+            lp = 0.0
+            for j in range(3):
+                r = d[j] / sig[j]
+                lp += -0.5 * r * r
+            lp -= lsig
+            (a if i < above else b).append(lp + (wa if i < above else wb))
+        return lse(a) - lse(b) * 5.0
+
+    best = -math.inf
+    for c in range(1, 101):
+        cand = particle(prior, q, k, seed=seed ^ ((0x94D049BB133111EB * c) & _M64), **kw)
+        r = ratio(cand)
+        if r > best:
+            best = r
+            pose = cand
+    return pose
+
+
 def selection_score(nvtl, score):
     """initial_pose.rs:233-245: NVTL when positive, else 5 exp(-score / 10)."""
     return nvtl if nvtl > 0.0 else 5.0 * np.exp(-score / 10.0)

@@ -104,3 +104,42 @@ def test_batch_timings(gpu):
     assert all(r["iterations"] >= 1 for r in res)
     with pytest.raises(capi.NdtError):
         ctx.batch_timings(len(scans) + 1)
+
+
+def test_initial_pose_search_guided(gpu, oracle, single_cases):
+    """TPE-guided particles (the reference's guided phase): the search is reproducible; the
+    winning particle started where the TPE proposes from the query's earlier results (or from
+    its startup draw); a full-circle search with the reference's defaults (200 particles, 100
+    of them guided) recovers the truth."""
+    case = single_cases[1]
+    ctx = capi.Context()
+    ctx.set_target(case.map_points)
+    prior = case.true_pose.copy()
+    prior[:2] += [1.2, -0.9]
+    prior[5] += 2.5
+    priors = [prior, case.guess]
+    queries = [case.scan, case.scan]
+    kw = dict(num_particles=200, guided=100, xy_range=2.0, yaw_range=np.pi, seed=5)
+    est, parts = ctx.initial_pose_search(queries, priors, return_particles=True, **kw)
+    est2 = ctx.initial_pose_search(queries, priors, **kw)
+    for q in range(2):
+        e = est[q]
+        np.testing.assert_array_equal(e["pose"], est2[q]["pose"])
+        assert e["particle"] == est2[q]["particle"]
+        k = e["particle"]
+        got = parts[q * 200:(q + 1) * 200]
+        if k < 100:
+            want = oracle.particle(priors[q], q, k, 2.0, np.pi, seed=5)
+        else:
+            trials = [[r["pose"][0], r["pose"][1], r["pose"][5], np.exp(-r["score"] / 10.0)]
+                      for r in got[:k]]
+            want = capi.tpe_propose(q, k, priors[q], trials, num_particles=200, guided=100,
+                                    xy_range=2.0, yaw_range=np.pi, seed=5)
+        np.testing.assert_array_equal(e["initial_pose"], want)
+        b, _ = oracle.select_best(got)
+        assert b == k
+    assert np.abs(est[0]["pose"][:2] - case.true_pose[:2]).max() < 0.2
+    dyaw = (est[0]["pose"][5] - case.true_pose[5] + np.pi) % (2 * np.pi) - np.pi
+    assert abs(dyaw) < np.radians(1.0)
+    with pytest.raises(capi.NdtError):  # guided must leave at least one startup particle
+        ctx.initial_pose_search(queries, priors, num_particles=10, guided=10)
