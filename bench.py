@@ -209,6 +209,19 @@ def init_pose_bench(repeats, cpu_seconds):
            "gpu_ms_per_search_of_16": (st["align_kernel_ms"] + st["score_kernel_ms"]) / repeats,
            "success_rate": ok / len(est), "success": "error < 0.2 m and < 1 deg",
            "scan_points_mean": float(np.mean([len(s) for s in w.scans])), "cuda_graph": True}
+    # the reference's own search shape: 200 particles, the last 100 TPE-guided (sequential per
+    # query: one launch per guided round for all 16 queries)
+    kg = dict(kw, guided=100)
+    ctx.initial_pose_search(w.scans, w.priors, **kg)
+    t0 = time.perf_counter()
+    for r in range(repeats):
+        est = ctx.initial_pose_search(w.scans, w.priors, **dict(kg, seed=5 + r))
+    wall = time.perf_counter() - t0
+    okg = sum(int(_pose_ok(e["pose"], t)) for e, t in zip(est, w.true_poses))
+    out["guided"] = {"value": 16 * repeats / wall, "unit": "estimates/s",
+                     "ms_per_search_of_16": wall / repeats * 1e3, "particles": 200,
+                     "guided_particles": 100, "success_rate": okg / len(est),
+                     "launches_per_search": 101}
     ctx.close()
     if cpu_seconds > 0:  # the restated CPU path on the host cores: one query's 200 particles
         from oracle import oracle as O
