@@ -1729,6 +1729,19 @@ __global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
     }
 }
 
+// Element e of QCtl's FP64 block, in the controller's shared state
+__device__ __forceinline__ double* qctl_slot(AlignShared& sh, int e) {
+    if (e < 6) return sh.pose + e;
+    if (e < 12) return sh.best_pose + (e - 6);
+    if (e < 13) return &sh.best_score;
+    if (e < 49) return sh.last_H + (e - 13);
+    if (e < 52) return sh.prev + (e - 49);
+    if (e < 55) return sh.prev2 + (e - 52);
+    if (e < 91) return sh.solve.W + (e - 55);
+    if (e < 118) return sh.Ad + (e - 91);
+    return sh.Bd + (e - 118);
+}
+
 // Newton step of alignment `job` after its iteration `it` (warp 0 of the CTA that finished
 // the iteration's last chunk, once the CTA has summed the chunk partials into sh.tot):
 // state from global memory, the controller of k_ndt_align, then the next frame and claim
@@ -1738,27 +1751,34 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
                                            uint32_t it, int lane) {
     const unsigned long long c0 = clock64();
     QCtl* q = P.qctl + job;
-    if (lane < 6) {
-        sh.pose[lane] = __ldcg(q->pose + lane);
-        sh.best_pose[lane] = __ldcg(q->best_pose + lane);
-    }
-    if (lane < 3) {
-        sh.prev[lane] = __ldcg(q->prev + lane);
-        sh.prev2[lane] = __ldcg(q->prev2 + lane);
-    }
-    for (int i = lane; i < 36; i += 32) {
-        sh.last_H[i] = __ldcg(q->last_H + i);
-        sh.solve.W[i] = __ldcg(q->W + i);
-    }
-    for (int i = lane; i < 27; i += 32) sh.Ad[i] = __ldcg(q->Ad + i);
-    for (int i = lane; i < 54; i += 32) sh.Bd[i] = __ldcg(q->Bd + i);
-    if (lane == 0) {
-        sh.best_score = __ldcg(&q->best_score);
-        sh.last_corr = __ldcg(&q->last_corr);
-        sh.osc = __ldcg(&q->osc);
-        sh.max_osc = __ldcg(&q->max_osc);
-        sh.n_eigen = __ldcg(&q->n_eigen);
-        sh.solve.have_w = __ldcg(&q->have_w);
+    {  // the state: every load in flight at once (one L2 round trip), then into shared memory
+        const double* qd = reinterpret_cast<const double*>(q);
+        double v[6];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const int e = lane + 32 * r;
+            v[r] = e < QCTL_DOUBLES ? __ldcg(qd + e) : 0.0;
+        }
+        int iv[5] = {0, 0, 0, 0, 0};
+        if (lane == 0) {
+            iv[0] = __ldcg(&q->last_corr);
+            iv[1] = __ldcg(&q->osc);
+            iv[2] = __ldcg(&q->max_osc);
+            iv[3] = __ldcg(&q->n_eigen);
+            iv[4] = __ldcg(&q->have_w);
+        }
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const int e = lane + 32 * r;
+            if (e < QCTL_DOUBLES) *qctl_slot(sh, e) = v[r];
+        }
+        if (lane == 0) {
+            sh.last_corr = iv[0];
+            sh.osc = iv[1];
+            sh.max_osc = iv[2];
+            sh.n_eigen = iv[3];
+            sh.solve.have_w = iv[4];
+        }
     }
     __syncwarp();
     const unsigned long long c1 = clock64();
@@ -1806,23 +1826,14 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
     if (!done) make_frame_warp(sh.pose, CPU_SEM, sh.fr, sh.trig, sh.Ad, sh.Bd, lane);
     __syncwarp();
     if (!done) {
-        if (lane < 6) {
-            __stcg(q->pose + lane, sh.pose[lane]);
-            __stcg(q->best_pose + lane, sh.best_pose[lane]);
+        double* qd = reinterpret_cast<double*>(q);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const int e = lane + 32 * r;
+            if (e < QCTL_DOUBLES) __stcg(qd + e, *qctl_slot(sh, e));
         }
-        if (lane < 3) {
-            __stcg(q->prev + lane, sh.prev[lane]);
-            __stcg(q->prev2 + lane, sh.prev2[lane]);
-        }
-        for (int i = lane; i < 36; i += 32) {
-            __stcg(q->last_H + i, sh.last_H[i]);
-            __stcg(q->W + i, sh.solve.W[i]);
-        }
-        for (int i = lane; i < 27; i += 32) __stcg(q->Ad + i, sh.Ad[i]);
-        for (int i = lane; i < 54; i += 32) __stcg(q->Bd + i, sh.Bd[i]);
         for (int i = lane; i < NFR; i += 32) __stcg(P.qframe + (size_t)job * NFR + i, sh.fr[i]);
         if (lane == 0) {
-            __stcg(&q->best_score, sh.best_score);
             __stcg(&q->last_corr, sh.last_corr);
             __stcg(&q->osc, sh.osc);
             __stcg(&q->max_osc, sh.max_osc);

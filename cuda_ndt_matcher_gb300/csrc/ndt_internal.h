@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -161,6 +162,8 @@ constexpr uint32_t QSPLIT_DIV = 4;
 // Controller state of an alignment between iterations (FP64; read and written only by the
 // controller of the alignment's current iteration).
 struct QCtl {
+    // the FP64 block (QCTL_DOUBLES, contiguous: the controller moves it with one load and one
+    // store per lane and element group)
     double pose[6], best_pose[6], best_score, last_H[36], prev[3], prev2[3];
     double W[36];
     double Ad[27], Bd[54];
@@ -168,6 +171,10 @@ struct QCtl {
     unsigned long long cyc_chunks, cyc_ctl;
     int32_t last_corr, osc, max_osc, n_eigen, have_w, pad;
 };
+constexpr int QCTL_DOUBLES = 172;
+static_assert(offsetof(QCtl, Bd) == 118 * sizeof(double) &&
+                  offsetof(QCtl, point_iters) == QCTL_DOUBLES * sizeof(double),
+              "QCtl's FP64 block is pose, best_pose, best_score, last_H, prev, prev2, W, Ad, Bd");
 
 // Line search of the graph path: at most 8 candidates (GRAPH_MAX_LS_CANDIDATES,
 // ndt_graph_common.cuh:18); Armijo and curvature constants of PipelineV2Config::default
