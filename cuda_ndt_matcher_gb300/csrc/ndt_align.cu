@@ -1729,6 +1729,49 @@ __global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
     }
 }
 
+// The graph path's step (control_step's !CPU_SEM branch: K3 direction and clamp,
+// ndt_graph_kernels.cu:311-463, then K5's oscillation and convergence rules) by the whole
+// warp: lanes 0-5 hold the direction's components and the two dot products run as one
+// shuffle tree; the scale needs no division unless the step is clamped (dn / dn is 1). Lane 0
+// keeps the oscillation history and writes the outputs. Returns 1 (every lane) when the
+// alignment is finished.
+__device__ __noinline__ int control_step_graph_warp(const AlignParams& P, AlignShared& sh,
+                                                    AlignOut& o, int it, double score,
+                                                    int ncorr, int lane) {
+    double xi = 0.0, gi = 0.0;
+    if (lane < 6) {
+        gi = sh.g[lane];
+        xi = sh.solve.ok ? sh.solve.x[lane] : -gi * 1e-4;
+    }
+    double dphi = gi * xi, dn2 = xi * xi;
+#pragma unroll
+    for (int m = 4; m > 0; m >>= 1) {
+        dphi += __shfl_xor_sync(0xffffffffu, dphi, m);
+        dn2 += __shfl_xor_sync(0xffffffffu, dn2, m);
+    }
+    dphi = __shfl_sync(0xffffffffu, dphi, 0);
+    dn2 = __shfl_sync(0xffffffffu, dn2, 0);
+    if (dphi <= 0.0) xi = -xi;
+    const double dn = sqrt(dn2);
+    const double step = dn > P.step_size ? P.step_size : dn;
+    const double scale = dn > 1e-10 ? (dn > P.step_size ? P.step_size / dn : 1.0) : 0.0;
+    if (lane < 6) sh.pose[lane] += scale * xi;
+    __syncwarp();
+    int done = 0;
+    if (lane == 0) {
+        osc_update(sh, sh.pose, it);
+        const int conv = step < P.eps;
+        if (conv || it + 1 >= P.max_iter) {
+            const int status = ncorr == 0 ? NDT_STATUS_NO_CORRESPONDENCES
+                                          : (conv ? NDT_STATUS_CONVERGED : NDT_STATUS_MAX_ITERATIONS);
+            write_out(o, sh.pose, score, sh.H, it + 1, conv && ncorr > 0, ncorr, sh.max_osc,
+                      status);
+            done = 1;
+        }
+    }
+    return __shfl_sync(0xffffffffu, done, 0);
+}
+
 // Element e of QCtl's FP64 block, in the controller's shared state
 __device__ __forceinline__ double* qctl_slot(AlignShared& sh, int e) {
     if (e < 6) return sh.pose + e;
@@ -1751,6 +1794,7 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
                                            uint32_t it, int lane) {
     const unsigned long long c0 = clock64();
     QCtl* q = P.qctl + job;
+    uint64_t cnt[2] = {0, 0};  // lane 0: point-iterations and correspondences so far
     {  // the state: every load in flight at once (one L2 round trip), then into shared memory
         const double* qd = reinterpret_cast<const double*>(q);
         double v[6];
@@ -1761,6 +1805,8 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
         }
         int iv[5] = {0, 0, 0, 0, 0};
         if (lane == 0) {
+            cnt[0] = __ldcg(&q->point_iters);
+            cnt[1] = __ldcg(&q->corr_total);
             iv[0] = __ldcg(&q->last_corr);
             iv[1] = __ldcg(&q->osc);
             iv[2] = __ldcg(&q->max_osc);
@@ -1810,13 +1856,19 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
             t[45] = (double)(c2 - c1);  // assembly + solve
             t[47] = sh.solve.sweeps;
         }
-        const int ncorr = (int)sh.tot[NACC];
-        const uint64_t pi = __ldcg(&q->point_iters) + jb.n;
-        const uint64_t ct = __ldcg(&q->corr_total) + (uint64_t)ncorr;
+    }
+    const int ncorr = (int)sh.tot[NACC];
+    AlignOut& o = P.out[job];
+    if (CPU_SEM) {
+        if (lane == 0) done = control_step<CPU_SEM>(P, sh, jb, o, (int)it, sh.tot[A_SC], ncorr);
+    } else {
+        done = control_step_graph_warp(P, sh, o, (int)it, sh.tot[A_SC], ncorr, lane);
+    }
+    if (lane == 0) {
+        const uint64_t pi = cnt[0] + jb.n;
+        const uint64_t ct = cnt[1] + (uint64_t)ncorr;
         __stcg(&q->point_iters, pi);
         __stcg(&q->corr_total, ct);
-        AlignOut& o = P.out[job];
-        done = control_step<CPU_SEM>(P, sh, jb, o, (int)it, sh.tot[A_SC], ncorr);
         if (done) {
             o.point_iters = pi;
             o.corr_total = ct;
