@@ -7,6 +7,7 @@
 // the NVTL kernel on the final poses (as a CUDA graph when configured), copies the
 // per-alignment records back and synchronises once.
 #include <algorithm>
+#include <memory>
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
@@ -294,20 +295,27 @@ static void stage_scans(ndt_ctx* c, const ndt_scan* scans, uint64_t m,
     c->stats.h2d_bytes += total * 12;
 }
 
-// Copies a planned batch to c->d_in on stream s, chunk by chunk: the context's host threads
-// pack a chunk into the pinned buffer, then its copy is issued (overlapping the packing of the
-// next). With d_arrive, a 4-byte copy after each chunk sets that device word to the points
-// resident so far (c->h_arrive holds one value per chunk and is reserved by the caller).
+// Copies a planned batch to c->d_in on stream s: the context's host threads pack the scans
+// into the pinned buffer in one pass (in launch order), and the thread that packs the last
+// scan of a chunk issues that chunk's copy, chunks strictly in order (under a lock), so the
+// copies overlap the packing with no barrier between chunks. With d_arrive, a 4-byte copy
+// after each chunk sets that device word to the points resident so far (a prefix of the
+// batch; c->h_arrive holds one value per chunk and is reserved by the caller).
 static void stage_plan(ndt_ctx* c, const StagePlan& pl, const std::vector<AlignJob>& jobs,
                        cudaStream_t s, uint32_t* d_arrive) {
+    const size_t nch = pl.chunk_job.size() - 1;
+    const uint64_t m = pl.chunk_job.back();
+    if (nch == 0 || m == 0) return;
     char* hp = (char*)c->h_pts.p;
     uint32_t* ha = (uint32_t*)c->h_arrive.p;
-    for (size_t k = 0; k + 1 < pl.chunk_job.size(); ++k) {
+    std::unique_ptr<std::atomic<uint32_t>[]> left(new std::atomic<uint32_t>[nch]);
+    for (size_t k = 0; k < nch; ++k) left[k].store(pl.chunk_job[k + 1] - pl.chunk_job[k]);
+    std::vector<char> packed(nch, 0);
+    size_t next = 0;
+    std::mutex mu;
+    const int dev = c->device;
+    auto issue = [&](size_t k) {
         const uint32_t a = pl.chunk_job[k], b = pl.chunk_job[k + 1];
-        c->pool.run(b - a, [&](uint64_t t) {
-            const AlignJob& jb = jobs[a + t];
-            if (jb.n) std::memcpy(hp + jb.offset * 12, pl.scans[jb.slot].xyz, (size_t)jb.n * 12);
-        });
         const uint64_t o0 = jobs[a].offset, o1 = jobs[b - 1].offset + jobs[b - 1].n;
         if (o1 > o0) {
             cudaMemcpyAsync((char*)c->d_in.p + o0 * 12, hp + o0 * 12, (o1 - o0) * 12,
@@ -319,7 +327,19 @@ static void stage_plan(ndt_ctx* c, const StagePlan& pl, const std::vector<AlignJ
             cudaMemcpyAsync(d_arrive, ha + k, 4, cudaMemcpyHostToDevice, s);
             c->stats.h2d_bytes += 4;
         }
-    }
+    };
+    c->pool.run(m, [&](uint64_t t) {
+        const AlignJob& jb = jobs[t];
+        if (jb.n) std::memcpy(hp + jb.offset * 12, pl.scans[jb.slot].xyz, (size_t)jb.n * 12);
+        const size_t k = (size_t)(std::upper_bound(pl.chunk_job.begin(), pl.chunk_job.end(),
+                                                   (uint32_t)t) -
+                                  pl.chunk_job.begin()) - 1;
+        if (left[k].fetch_sub(1) != 1) return;  // the chunk still has scans to pack
+        std::lock_guard<std::mutex> lk(mu);
+        packed[k] = 1;
+        if (next < nch && packed[next]) cudaSetDevice(dev);  // this thread issues copies
+        while (next < nch && packed[next]) issue(next++);
+    });
 }
 
 static void drop_graphs(ndt_ctx* c) {
