@@ -8,10 +8,14 @@
  *
  * Parity status: pinned against the reference's own known-answer tests (voxel
  * coordinates, Morton round trips, radix sort, segment detection, Newton steps on
- * diagonal Hessians, Gaussian parameter signs, covariance regularisation) through
- * tests/golden/ and tests/test_oracle_golden.py. The reference's Rust CPU path cannot
- * be built here (no cargo), so the end-to-end pose/score/NVTL restatement is pinned
- * by those component vectors plus finite-difference derivative checks.
+ * diagonal Hessians, Gaussian parameter signs, covariance regularisation, the
+ * More-Thuente unit tests) through tests/golden/, tests/test_oracle_golden.py and
+ * tests/test_capi_cpu.py. The graph semantics are also compared end to end with the
+ * reference's own CUDA kernels, compiled from its sources (oracle/ref_graph.c,
+ * tests/test_gpu_reference_kernels.py): this restatement sits as close to them as the
+ * reference's FP32 arithmetic allows. The reference's Rust CPU path cannot be built here
+ * (no cargo), so the CPU semantics are pinned by the component vectors plus
+ * finite-difference derivative checks.
  *
  * Two Newton semantics are restated (they disagree in the reference itself):
  *   - "cpu"  : NdtOptimizer::align (src/ndt_cuda/src/optimization/solver.rs:135-305)
