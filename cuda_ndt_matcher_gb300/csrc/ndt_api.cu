@@ -172,7 +172,7 @@ struct PendingAlign {
 
 // Host scans of a batch laid out for copying in: the jobs are in launch order (largest scan
 // first), job j's points go to jobs[j].offset, and the copy runs in chunks of jobs
-// [chunk_job[k], chunk_job[k + 1]) of 1 MB doubling to 16 MB, each starting on a 64-point
+// [chunk_job[k], chunk_job[k + 1]) of 256 KB doubling to 16 MB, each starting on a 64-point
 // (768-byte) boundary.
 struct StagePlan {
     const ndt_scan* scans = nullptr;
@@ -1164,7 +1164,7 @@ static int prepare_batch(ndt_ctx* x, const ndt_scan* scans, uint64_t m,
     plan.scans = scans;
     plan.chunk_job.clear();
     const uint64_t max_chunk = (16ull << 20) / 12;
-    uint64_t off = 0, in_chunk = 0, chunk = (1ull << 20) / 12;
+    uint64_t off = 0, in_chunk = 0, chunk = (256ull << 10) / 12;
     for (uint64_t t = 0; t < m; ++t) {
         const uint32_t i = order[t];
         if (t == 0 || in_chunk >= chunk) {
