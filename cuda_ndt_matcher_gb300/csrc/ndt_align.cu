@@ -1687,15 +1687,18 @@ __device__ __forceinline__ uint32_t qw_nch(unsigned long long w) {
 }
 
 // Chunks of iteration `it` of an alignment with n points: n / qchunk for its first
-// QSPLIT_ITER iterations, then QSPLIT_DIV times as many, that much smaller. The alignments that
+// QSPLIT_ITER iterations, then QSPLIT_DIV times as many, that much smaller, and from
+// QSPLIT_ITER2 on twice as many again (few alignments run that long). The alignments that
 // run long are the ones that finish a batch, on an otherwise idle GPU: smaller chunks spread
 // each of their iterations over more SMs. The rule depends on the iteration alone, so every
 // run sums an alignment's chunks over the same tree (results are identical run to run). At
 // most QMAXCH.
-constexpr uint32_t QSPLIT_ITER = 10;
+constexpr uint32_t QSPLIT_ITER = 10, QSPLIT_ITER2 = 20;
 __device__ __forceinline__ uint32_t queue_chunks(const AlignParams& P, uint32_t n, uint32_t it) {
     const uint32_t size =
-        it < QSPLIT_ITER ? (uint32_t)P.qchunk : max(1u, (uint32_t)P.qchunk / QSPLIT_DIV);
+        it < QSPLIT_ITER ? (uint32_t)P.qchunk
+                         : max(1u, (uint32_t)P.qchunk / (it < QSPLIT_ITER2 ? QSPLIT_DIV
+                                                                          : 2 * QSPLIT_DIV));
     return min(n ? (n + size - 1u) / size : 1u, QMAXCH);
 }
 

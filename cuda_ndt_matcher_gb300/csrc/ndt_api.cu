@@ -912,9 +912,9 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
             hs[j] = s;
         }
         hq = (uint32_t*)((char*)c->h_jobs.p + jb + sjb);
-        // partial-sum slots per alignment: its chunk count at the late-iteration chunk size
-        // (the most an iteration uses), capped at the 16-bit count of the claim word
-        const uint32_t small = std::max(1u, chunk / QSPLIT_DIV);
+        // partial-sum slots per alignment: its chunk count at the smallest (last iterations')
+        // chunk size, the most an iteration uses, capped at the 16-bit count of the claim word
+        const uint32_t small = std::max(1u, chunk / (2 * QSPLIT_DIV));
         uint64_t total = 0, full = 0;
         for (uint32_t j = 0; j < nj; ++j) {
             hq[j] = (uint32_t)total;

@@ -156,8 +156,9 @@ struct QJob {
 };
 constexpr uint32_t QDONE = 0xFFFFu;
 constexpr uint32_t QMAXCH = 0xFFFFu;  // chunks per iteration at most (16-bit count)
-// Chunks of an alignment's late iterations are 1/QSPLIT_DIV of the launch's chunk size (the
-// partial-sum slots are sized for them). At the 20k-point bench batch, 2 and 8 were slower.
+// Chunks of an alignment's late iterations are 1/QSPLIT_DIV of the launch's chunk size, and
+// 1/(2 QSPLIT_DIV) in its last ones (the partial-sum slots are sized for those). At the
+// 20k-point bench batch, 2 and 8 were slower as the first split.
 constexpr uint32_t QSPLIT_DIV = 4;
 // Controller state of an alignment between iterations (FP64; read and written only by the
 // controller of the alignment's current iteration).
