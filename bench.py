@@ -384,7 +384,7 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
       points;
     - the largest FP32-vs-FP64 covariance difference over the samples. The FP32 value is the
       reference GPU pipeline's cell-centre-shifted single-precision formula; the FP64 value
-      is this build's.
+      is the library's.
     It then aligns 16 dense 100k-point crop scans and reports aligns/s."""
     from cuda_ndt_matcher_gb300 import capi, synth
     from oracle import oracle as O

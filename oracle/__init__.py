@@ -1,2 +1,2 @@
-"""CPU restatement of the reference NDT path: test infrastructure only (the checker and the
+"""CPU restatement of the reference NDT path: test infrastructure only (the oracle and the
 timed CPU baseline). The product never imports this package."""

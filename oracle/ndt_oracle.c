@@ -2,7 +2,7 @@
  * ndt_oracle.c — CPU restatement of cuda_ndt_matcher's NDT hot path (test infrastructure).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs load this file's
- * library. It is the checker and the timed CPU baseline, never part of the GPU product.
+ * library. It is the oracle and the timed CPU baseline, never part of the GPU product.
  * Each function cites the reference file:line it restates (paths are relative to the
  * reference project root). Compiled with -ffp-contract=off so every FP operation is one
  * IEEE rounding, on x86-64 and aarch64 alike.

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product links this code; only tests/,
  * __graft_entry__.smoke() and bench.py's cpu_baseline / --impl reference legs load it,
- * and only as the checker (or as the timed CPU baseline), never as the thing measured
+ * and only as the oracle (or as the timed CPU baseline), never as the thing measured
  * on the GPU.
  *
  * Parity status: pinned against the reference's own known-answer tests (voxel
@@ -87,7 +87,7 @@ void or_morton_decode(uint64_t code, uint32_t* x, uint32_t* y, uint32_t* z);
 /* voxel_grid/gpu/morton.rs:197-281 (reference builder rule: aligned-min origin) */
 void or_morton_codes_ref(const float* pts, size_t n, float resolution, uint64_t* codes,
                          float* grid_min3);
-/* this build's rule: key = morton(voxel_coord - min voxel_coord) */
+/* the library's rule: key = morton(voxel_coord - min voxel_coord) */
 int or_morton_codes_coord(const float* pts, size_t n, float resolution, uint64_t* codes,
                           int32_t* min_coord3);
 

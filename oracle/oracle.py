@@ -1,6 +1,6 @@
 """ctypes wrapper over the oracle library (test infrastructure only).
 
-Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs as the checker
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs as the oracle
 and as the timed CPU baseline. The GPU product never imports this module.
 """
 import ctypes as C

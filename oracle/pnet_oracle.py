@@ -1,5 +1,5 @@
 """FP64 restatement of the proposal network's forward pass, loss and backward pass (test
-infrastructure only: the checker of the GPU training kernels, never part of the product).
+infrastructure only: the oracle of the GPU training kernels, never part of the product).
 
 It follows the kernels' arithmetic step by step, including where they round to bf16:
 - the GEMM operands: inputs, weights, hidden activations after GELU, and output gradients;

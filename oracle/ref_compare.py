@@ -1,9 +1,9 @@
-"""Prints this build's results beside the reference's own graph-path kernels and the FP64
+"""Prints the library's results beside the reference's own graph-path kernels and the FP64
 oracle (test infrastructure; needs a GPU and the oracle/_ref cubins).
 
     python -m oracle.ref_compare
 
-For each alignment: iterations (this build / FP64 oracle / reference kernels) and the largest
+For each alignment: iterations (the library / FP64 oracle / reference kernels) and the largest
 position difference of each pair. Where the reference departs from the FP64 evaluation of its
 own algorithm, that is its FP32 error (pose state, transform, atomic sums).
 """

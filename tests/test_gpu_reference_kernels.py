@@ -1,10 +1,10 @@
 """Parity against the reference's own graph-path CUDA kernels: K1-K5 and the voxel hash of
 src/cuda_ffi/csrc, compiled unmodified into oracle/_ref cubins and driven by
 oracle/ref_graph.c (a restatement of FullGpuPipelineV2::optimize), on the same voxel map,
-scans and initial poses as this build's C ABI.
+scans and initial poses as the library's C ABI.
 
 The reference keeps its pose in FP32 and reduces with FP32 atomicAdd, so it differs from
-itself run to run. Each comparison measures that spread too: this build is held to the
+itself run to run. Each comparison measures that spread too: the library is held to the
 stated tolerances and to agreeing with the reference at least as often as the reference
 agrees with itself."""
 import numpy as np
@@ -35,7 +35,7 @@ def _gauss_f32():
 
 
 def _map_both(ref, ctx, points):
-    """Builds this build's map, then gives the reference kernels the same voxels."""
+    """Builds the library's map, then gives the reference kernels the same voxels."""
     ctx.set_target(points)
     _, means, _, icovs, _ = ctx.map_voxels()
     ref.set_map(means, icovs, 2.0)
@@ -72,7 +72,7 @@ def test_neighbours_match_reference_kernel(ref, single_cases):
 
 
 def _ours_at(case, poses):
-    """This build's score, gradient, Hessian and correspondences at each pose (one traced
+    """The library's score, gradient, Hessian and correspondences at each pose (one traced
     iteration from each)."""
     ctx = capi.Context(max_iterations=1)
     ctx.set_target(case.map_points)
@@ -89,8 +89,8 @@ def _ours_at(case, poses):
 
 def test_derivatives_match_reference_kernel(ref, oracle, single_cases):
     """K2 at the same poses: the reference's score, gradient, Hessian and correspondence count
-    against this build's, both measured against the FP64 oracle. The reference transforms
-    points in plain FP32 and sums with FP32 atomics; this build's compensated transform and
+    against the library's, both measured against the FP64 oracle. The reference transforms
+    points in plain FP32 and sums with FP32 atomics; the library's compensated transform and
     FP64 reductions must be at least as close to FP64 as the reference is."""
     d1, d2 = _gauss_f32()
     for i, case in enumerate(single_cases):
@@ -110,7 +110,7 @@ def test_derivatives_match_reference_kernel(ref, oracle, single_cases):
             assert abs(os_ - fs) <= abs(rs - fs) + 1e-6 * abs(fs), msg
             assert np.abs(og - fg).max() <= np.abs(rg - fg).max() + 1e-6 * np.abs(fg).max(), msg
             assert np.abs(oH - fH).max() <= np.abs(rH - fH).max() + 1e-6 * np.abs(fH).max(), msg
-            # and this build against the reference, within the reference's own error
+            # and the library against the reference, within the reference's own error
             assert abs(os_ - rs) <= 1e-5 * abs(rs) + abs(rs - fs), msg
 
 
@@ -126,7 +126,7 @@ def _drot(a, b):
 def test_align_matches_reference_kernels(ref, oracle, single_cases, line_search):
     """Single alignments of the seeded 200k-point scenes against the reference's K1-K5 (K4
     with line search). The reference's FP32 pose state, transform and atomic sums move its
-    result away from an exact evaluation of its own algorithm (the FP64 oracle); this build
+    result away from an exact evaluation of its own algorithm (the FP64 oracle); the library
     must sit no farther from the reference than that FP64 evaluation does, plus the
     tolerances (pose 1e-4 m / 1e-5 rad, score and Hessian 1e-5 relative), and take the same
     number of iterations wherever the FP64 evaluation does."""
@@ -161,8 +161,8 @@ def test_align_matches_reference_kernels(ref, oracle, single_cases, line_search)
 
 
 def test_sequence_batch_matches_reference_kernels(ref, oracle):
-    """20k-point scans of the 5M-point sequence map, aligned in one batch by this build's
-    default kernel, against the reference aligning each scan on its own. This build agrees
+    """20k-point scans of the 5M-point sequence map, aligned in one batch by the library's
+    default kernel, against the reference aligning each scan on its own. The library agrees
     with the reference (same iterations, pose within tolerance) on at least as many scans as
     the FP64 evaluation of the reference's algorithm does; the remaining differences are the
     reference's own FP32 error, which its run-to-run spread does not show."""

@@ -208,7 +208,7 @@ def test_neighbour_semantics(oracle):
 
 
 def test_morton_rules_agree_on_workload(oracle):
-    """The reference builder's aligned-min Morton rule and this build's coordinate rule
+    """The reference builder's aligned-min Morton rule and the library's coordinate rule
     group the workload's points identically (boundary disagreements are counted)."""
     case = synth.single_case(1)
     a, _ = oracle.morton_codes_ref(case.map_points, 2.0)
