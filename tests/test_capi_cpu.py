@@ -107,6 +107,8 @@ def test_reference_kernel_driver_builds():
     names = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
     assert {"rg_open", "rg_set_map", "rg_align", "rg_eval", "rg_query", "rg_close",
             "rg_error"} <= names
+    if not ob.build_ref_cubins():  # compiled where the reference sources are
+        pytest.skip("neither the reference sources nor prebuilt cubins are here")
     assert ref_graph.available()
 
 
