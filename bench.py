@@ -39,7 +39,6 @@ FLOP_PER_POINT_ITER = 165
 FLOP_PER_PAIR = 65
 # DRAM bytes (read + write) of one Newton-kernel launch of the default workload (256 scans,
 # 5M-point map, seed 2), from one ncu capture of this bench per kernel form
-# (profiles/k_ndt_align_seq5M_b256.md, profiles/k_ndt_queue_seq5M_b256.md)
 NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
                      ("k_ndt_queue", 256, 5_000_000, 2): 109.4e6}
 
@@ -54,6 +53,9 @@ def parse():
     ap.add_argument("--map-points", type=int, default=5_000_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--parity", type=int, default=1,
+                    help="after timing, check 64 scans of the timed batch against the FP64 "
+                         "oracle and the reference's own kernels")
     ap.add_argument("--extras", type=int, default=1,
                     help="also run the initial-pose search and the uneven-queue workloads")
     ap.add_argument("--shape", default="",
@@ -157,6 +159,26 @@ def peaks():
                 "sm_max_mhz": 2070.0}, "fallback"
 
 
+def cpu_model():
+    """Host CPU model string (lscpu's "Model name", else /proc/cpuinfo's first model field)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu model", "hardware")):
+                    return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def phase_shares(st):
     keys = ["cycles_points", "cycles_cluster_wait", "cycles_control", "cycles_broadcast"]
     tot = sum(st[k] for k in keys) or 1
@@ -178,6 +200,7 @@ def cpu_baseline(grid_args, scans, poses, seconds, semantics="cpu"):
         i = j
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": "aligns/s", "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count(),
             "sample": f"{done} of the bench's 20k-point scans, NdtOptimizer::align restated "
                       f"(FP64, all neighbours, ND-clamp + SVD step), {cores} threads, {dt:.1f} s"}
 
@@ -457,6 +480,54 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
     return out
 
 
+def parity_sample(seq_map, scans, poses, results, n=64):
+    """Checker run after the timed regions: the first n scans of the timed batch, as the last
+    timed step aligned them, against the FP64 oracle (graph semantics, the same inputs) and
+    against the reference's own graph kernels K1-K5 (compiled from its sources, one alignment
+    at a time). Reports max and p99 of the pose, score and NVTL differences to FP64, the
+    scans meeting the per-scan bar (iterations equal, 1e-4 m, 1e-5 rad, 1e-5 relative), and
+    how often this library and the FP64 oracle each agree with the reference."""
+    from oracle import oracle as O
+    n = min(n, len(scans))
+    g = O.Grid(seq_map, 2.0)
+    want = g.align_batch(scans[:n], poses[:n], semantics="gpu")
+    got = results[:n]
+    dpos = np.array([np.abs(a["pose"][:3] - b["pose"][:3]).max() for a, b in zip(got, want)])
+    drot = np.array([np.abs(a["pose"][3:] - b["pose"][3:]).max() for a, b in zip(got, want)])
+    rel = lambda k: np.array([abs(a[k] - b[k]) / max(abs(b[k]), 1e-30)
+                              for a, b in zip(got, want)])
+    dsc, dnv = rel("score"), rel("nvtl")
+    same_it = np.array([a["iterations"] == b["iterations"] for a, b in zip(got, want)])
+    bar = same_it & (dpos <= 1e-4) & (drot <= 1e-5) & (dsc <= 1e-5) & (dnv <= 1e-5)
+    q = lambda v: {"max": float(v.max()), "p99": float(np.percentile(v, 99)),
+                   "median": float(np.median(v))}
+    out = {"scans": n, "against": "FP64 oracle, graph semantics (or_align_gpu_sem)",
+           "pose_m": q(dpos), "pose_rad": q(drot), "score_rel": q(dsc), "nvtl_rel": q(dnv),
+           "iterations_equal": int(same_it.sum()), "within_bar": int(bar.sum()),
+           "outside_bar_ids": [int(i) for i in np.nonzero(~bar)[0]]}
+    try:
+        from oracle import ref_graph
+        if not ref_graph.available():
+            raise RuntimeError("reference cubins not built")
+        rg = ref_graph.RefGraph()
+        rg.set_map(g.means, g.icovs, 2.0)
+        d1, d2 = (float(np.float32(x)) for x in O.gauss_params(2.0, 0.55))
+        same = lambda a, b: (a["iterations"] == b["iterations"]
+                             and np.abs(a["pose"][:3] - b["pose"][:3]).max() <= 1e-4
+                             and np.abs(a["pose"][3:] - b["pose"][3:]).max() <= 1e-5)
+        ours = fp64 = 0
+        for k in range(n):
+            r = rg.align(scans[k], poses[k], d1, d2)
+            ours += same(got[k], r)
+            fp64 += same(want[k], r)
+        rg.close()
+        out["reference_k1_k5_agreement"] = {"ours": ours, "fp64_oracle": fp64, "of": n,
+                                            "rule": "iterations equal, 1e-4 m, 1e-5 rad"}
+    except Exception as e:
+        out["reference_k1_k5_agreement"] = {"unavailable": f"{type(e).__name__}: {e}"}
+    return out
+
+
 def queue_bench(repeats):
     """A queue of 64 scans of log-uniform size 2k-40k points in one launch (CUDA graph):
     throughput and per-scan completion latency (device clock, from the batch's first start)."""
@@ -510,9 +581,15 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans",
-                   "batch": per_step, "map_points": args.map_points, "scan_points": 20000},
+        "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans, "
+                               "batched alignment", "batch": args.batch, "scan_points": 20000,
+                   "map_points": args.map_points, "semantics": "CPU path (NDT_USE_GPU=0)",
+                   "sampled_scans_per_step": per_step,
+                   "sample_rule": f"each step aligns {per_step} scans of the {args.batch}-scan "
+                                  "batch (one per host thread); aligns/s is per alignment, so "
+                                  "the rate compares with the GPU arm's"},
         "cpu_baseline": {"value": value, "unit": "aligns/s", "cores": cores, "kind": "port",
+                         "cpu_model": cpu_model(), "nproc": os.cpu_count(),
                          "sample": f"{per_step} scans per step, NdtOptimizer::align restated "
                                    "(the Rust reference cannot be built here)"},
         "e2e": {"value": value, "unit": "aligns/s", "h2d_bytes_per_step": 0,
@@ -693,6 +770,10 @@ def run_ours(args):
     perr = np.linalg.norm(got[:, :2] - truth[:, :2], axis=1)
     build_bytes = 248 * info.num_points + 64 * info.num_voxels + 16 * info.hash_capacity
 
+    parity = None
+    if rank == 0 and args.parity:
+        parity = parity_sample(seq.map, scans, poses,
+                               [capi.result_dict(r) for r in res_arr], n=64)
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline((seq.map, 2.0), scans, poses, args.cpu_seconds)
@@ -750,6 +831,7 @@ def run_ours(args):
                                "build_ms": build_ms, "bytes": int(build_bytes),
                                "peak_source": src},
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clk,
             "gpu_launches": int(st["align_launches"] + 2 * st["score_launches"]),
             "accuracy": {"median_xy_err_m": float(np.median(perr)),

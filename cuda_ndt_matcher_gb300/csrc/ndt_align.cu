@@ -2044,10 +2044,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                         stop = 1;
                     } else if (fed && blockIdx.x >= gridDim.x / 4u &&
                                now - idle_since > 20000ull) {
-                        // near the end of a batch: all but a quarter of the grid (one CTA
-                        // per SM) leave after 20 us without work, so a kernel queued on
-                        // another stream (the next asynchronous batch) can take their SMs;
-                        // the quarter that stays serves the remaining iterations
+                        // near the end of a batch: all but the first quarter of the grid
+                        // (by CTA index) leave after 20 us without work, so a kernel queued
+                        // on another stream (the next asynchronous batch) can take their
+                        // SMs; the quarter that stays serves the remaining iterations (with
+                        // fewer than 4 CTAs none stays idle, and the CTA running a Newton
+                        // step still claims the next iteration's chunks when it ends)
                         stop = 1;
                     }
                 }

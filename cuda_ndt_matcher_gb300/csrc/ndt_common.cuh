@@ -2,12 +2,12 @@
 //
 // Voxel map layout in HBM (built by voxel_build.cu, read by ndt_align.cu / ndt_score.cu):
 //   slots[cap]      uint4 {key32, mean.x, mean.y, mean.z}: open-addressing hash, 16 B per
-//                   slot, key32 = EMPTY_KEY when free. The home slot is the reference's
-//                   MurmurHash3 finaliser of the reference's 21-bit-per-axis packed cell key
-//                   (src/cuda_ffi/csrc/voxel_hash.cu:33-58), masked by the power-of-two
-//                   capacity; the stored key is the cell relative to the map's minimum cell
-//                   (key_bits per axis, <= 31 bits in total), so one 16-byte load both tests
-//                   the key and yields the centroid for the radius check.
+//                   slot, key32 = EMPTY_KEY when free. The stored key is the cell relative
+//                   to the map's minimum cell (key_bits per axis, <= 31 bits in total); the
+//                   home slot is mix32(key32) masked by the power-of-two capacity (the
+//                   reference uses the MurmurHash3 64-bit finaliser of a 63-bit packed key,
+//                   src/cuda_ffi/csrc/voxel_hash.cu:33-58). One 16-byte load both tests the
+//                   key and yields the centroid for the radius check.
 //   slot_icov[cap]  2 x float4 {c00, c01, c02, c11}, {c12, c22, 0, 0}: inverse covariance of
 //                   the voxel in that slot (one 32-byte sector per accepted neighbour).
 //   slot_vidx[cap]  int32 voxel index (ascending coordinate-Morton order), for the query API.
@@ -87,23 +87,6 @@ __device__ __forceinline__ uint32_t nbhd_index(const MapView& m, uint32_t corner
 __device__ __forceinline__ void nbhd_offsets(const MapView& m, uint32_t* off32) {
     for (int b = threadIdx.x; b < 32; b += blockDim.x)
         off32[b] = b < 27 ? nbhd_index(m, 0u, (uint32_t)b) : 0u;
-}
-
-// Reference key packing and hash (src/cuda_ffi/csrc/voxel_hash.cu:33-58).
-__host__ __device__ __forceinline__ uint64_t pack21(int32_t gx, int32_t gy, int32_t gz) {
-    uint64_t ux = (uint64_t)(int64_t)(gx + (1 << 20));
-    uint64_t uy = (uint64_t)(int64_t)(gy + (1 << 20));
-    uint64_t uz = (uint64_t)(int64_t)(gz + (1 << 20));
-    return (ux << 42) | (uy << 21) | uz;
-}
-
-__host__ __device__ __forceinline__ uint64_t fmix64(uint64_t k) {
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdull;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ull;
-    k ^= k >> 33;
-    return k;
 }
 
 // local key of a cell, or EMPTY_KEY when the cell lies outside the map's bounding box

@@ -27,6 +27,8 @@
 #include <cstdio>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "ndt_internal.h"
 
 namespace ndtgb {
@@ -271,9 +273,42 @@ static __device__ __align__(256) unsigned char g_static_sort_scratch[STATIC_SORT
 
 static std::mutex g_static_sort_mu;
 static void* g_static_sort_ptr[STATIC_SORT_MAX_DEVICES];
+static unsigned long long g_static_sort_ctx[STATIC_SORT_MAX_DEVICES];
 
-// Device address of the scratch array on the current device, resolved once per device (the
-// first call may load this module onto the device).
+// Unique id of the calling thread's current CUDA context (cuCtxGetId through the runtime's
+// driver entry points), 0 when it cannot be read. A device reset or a new primary context
+// gives a new id, and the module (with its __device__ array) is loaded again at a new address.
+static unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)p;
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device. It is resolved once per device
+// and context: the first call on a device (and the first after a cudaDeviceReset, which ends
+// the context the address belonged to) calls cudaGetSymbolAddress, which can load this
+// module onto the device. When the context id cannot be read, the address is resolved on
+// every call (a lookup, no allocation).
 static int static_sort_scratch(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -282,8 +317,12 @@ static int static_sort_scratch(void** out) {
         set_error("static radix sort: device ordinal out of range");
         return NDT_ERR_INVALID_ARGUMENT;
     }
+    // makes the device's primary context current (created if needed), so its id is readable
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return cuda_fail(e, "static radix sort: device set-up");
+    const unsigned long long ctx_id = current_context_id();
     std::lock_guard<std::mutex> lock(g_static_sort_mu);
-    if (!g_static_sort_ptr[dev]) {
+    if (!g_static_sort_ptr[dev] || ctx_id == 0 || g_static_sort_ctx[dev] != ctx_id) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "static radix sort: scratch set-up");
@@ -292,6 +331,7 @@ static int static_sort_scratch(void** out) {
             return NDT_ERR_CAPACITY;
         }
         g_static_sort_ptr[dev] = p;
+        g_static_sort_ctx[dev] = ctx_id;
     }
     *out = g_static_sort_ptr[dev];
     return NDT_OK;

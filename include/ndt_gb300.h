@@ -423,7 +423,8 @@ int ndt_radix_sort_pairs_u64_u32(uint64_t* d_keys, uint32_t* d_values, uint64_t 
  *  - n <= 1048576 pairs; larger n returns NDT_ERR_CAPACITY and touches nothing;
  *  - the first call on each device does the set-up (resolves the array's device address,
  *    which can load the library's kernels onto that device): make it, with that device
- *    current, before any stream capture;
+ *    current, before any stream capture. A cudaDeviceReset ends the context that address
+ *    belongs to; the first call after it (in a new context) does the set-up again;
  *  - the scratch needs no initial contents (nothing in it has to start at zero);
  *  - all calls on one device share the scratch: two calls whose work overlaps on the GPU
  *    (different streams, or host threads with no ordering between their streams) race and

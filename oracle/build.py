@@ -26,7 +26,10 @@ def build(force: bool = False) -> str:
 
 
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/src/cuda_ffi/csrc"
+# the reference checkout: NDT_REFERENCE_DIR, else the container's read-only mount; the GPU
+# machine has neither and uses the cubins built here
+REF_ROOT = os.environ.get("NDT_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "cuda_ffi", "csrc")
 # the reference's graph-path kernels and voxel hash, compiled unmodified into device-only
 # cubins with the reference's own flags (-O3, one architecture; src/cuda_ffi/build.rs:131-148)
 REF_CUBINS = {"ndt_graph_kernels.cubin": "ndt_graph_kernels.cu",

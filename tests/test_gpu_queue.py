@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from cuda_ndt_matcher_gb300 import capi, synth
+from parity_helpers import shadow_check, trajectory_has_indefinite_hessian
 from test_gpu_align import assert_parity
 
 pytestmark = pytest.mark.gpu
@@ -112,6 +113,23 @@ def test_queue_many_alignments(gpu, oracle):
     # correct summation orders part ways; both kernels are held to the same agreement count
     nq, nc = agree(a), agree(cl)
     assert nq >= 0.8 * len(scans) and nq >= nc - 0.02 * len(scans), (nq, nc)
+    # every scan that parts from the oracle: its oracle trajectory crosses an indefinite
+    # Hessian, and one GPU iteration from each oracle iterate lands on the next one
+    g = oracle.Grid(seq.map, 2.0)
+    step = capi.Context(work_queue=2, max_iterations=1)
+    step.set_target(seq.map)
+    step.trace(True)
+    apart = [i for i, (r, w) in enumerate(zip(a, want))
+             if not (r["iterations"] == w["iterations"] and
+                     np.abs(r["pose"][:3] - w["pose"][:3]).max() <= 1e-4 and
+                     np.abs(r["pose"][3:] - w["pose"][3:]).max() <= 1e-5)]
+    boundary = 0
+    for i in apart:
+        assert trajectory_has_indefinite_hessian(g, scans[i], poses[i]), ("definite", i)
+        fails, bnd = shadow_check(step, g, scans[i], poses[i])
+        assert not fails, ("scan", i, fails)
+        boundary += len(bnd)
+    assert boundary <= max(4, len(apart)), boundary
 
 
 def test_queue_autotune_and_forms(gpu):
