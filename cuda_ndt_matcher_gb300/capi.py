@@ -32,7 +32,8 @@ EXPORTS = [
     "ndt_tpe_propose",
     "ndt_pnet_config_default", "ndt_pnet_create", "ndt_pnet_destroy", "ndt_pnet_get_config",
     "ndt_pnet_add_map", "ndt_pnet_add_scan", "ndt_pnet_train", "ndt_pnet_propose",
-    "ndt_pnet_debug_grad", "ndt_pnet_params", "ndt_learned_pose_search", "ndt_gemm_bf16",
+    "ndt_pnet_debug_grad", "ndt_pnet_params", "ndt_pnet_stats_get", "ndt_learned_pose_search",
+    "ndt_gemm_bf16",
     "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
     "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
     "ndt_radix_sort_pairs_u64_u32", "ndt_radix_sort_pairs_u64_u32_static",
@@ -100,6 +101,12 @@ class PNetConfig(C.Structure):
                 ("xy_range", C.c_float), ("yaw_weight", C.c_float), ("seed", C.c_uint64)]
 
 
+class PNetStats(C.Structure):
+    _fields_ = [("inference_batches", C.c_uint64), ("queries", C.c_uint64),
+                ("inference_kernel_ms", C.c_double), ("train_steps", C.c_uint64),
+                ("train_ms", C.c_double)]
+
+
 class MapInfo(C.Structure):
     _fields_ = [("num_points", C.c_uint64), ("num_segments", C.c_uint64),
                 ("num_voxels", C.c_uint64), ("hash_capacity", C.c_uint64),
@@ -117,7 +124,8 @@ class Stats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("cycles_points", C.c_uint64), ("cycles_cluster_wait", C.c_uint64),
                 ("cycles_control", C.c_uint64), ("cycles_broadcast", C.c_uint64),
-                ("eigen_solves", C.c_uint64)]
+                ("eigen_solves", C.c_uint64), ("proposal_launches", C.c_uint64),
+                ("proposal_kernel_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -178,6 +186,7 @@ def load(build_if_missing=True):
         "ndt_pnet_propose": (C.c_int, [P, C.c_int32, P, C.c_uint64, P, P]),
         "ndt_pnet_debug_grad": (C.c_int, [P, P, P, C.c_uint64, P, P]),
         "ndt_pnet_params": (C.c_int, [P, P, C.POINTER(C.c_uint64), C.c_int32]),
+        "ndt_pnet_stats_get": (C.c_int, [P, C.POINTER(PNetStats)]),
         "ndt_learned_pose_search": (C.c_int, [P, P, C.c_int32, P, C.c_uint64, C.c_double,
                                               C.POINTER(ParticleConfig), P, P]),
         "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
@@ -543,10 +552,20 @@ class PNet:
                                          pose.ctypes.data, C.byref(sid)))
         return sid.value
 
-    def train(self, steps):
+    def train(self, steps, record_loss=True):
+        """steps Adam steps; with record_loss the per-step mean loss is returned (read back
+        after every step), else None."""
+        if not record_loss:
+            check(self.lib.ndt_pnet_train(self.h, steps, None))
+            return None
         loss = np.zeros(steps, np.float32)
         check(self.lib.ndt_pnet_train(self.h, steps, loss.ctypes.data))
         return loss
+
+    def stats(self):
+        st = PNetStats()
+        check(self.lib.ndt_pnet_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
 
     def propose(self, map_id, queries, coarse):
         qs = [as_xyz(q) for q in queries]

@@ -35,7 +35,7 @@
 namespace ndtgb {
 
 int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, int ldd,
-                 uint32_t* d_err, cudaStream_t s, int splits);
+                 uint32_t* d_err, cudaStream_t s, int splits, const GemmEpilogue* epi);
 constexpr int PN_MAX_SPLITS = 16;
 
 constexpr int PN_GRID = 64, PN_ZB = 8;
@@ -86,27 +86,26 @@ __global__ void k_bias_act(float* __restrict__ Z, const float* __restrict__ Zp, 
     }
 }
 
-// dX [B x N] f32 (from the GEMM) * GELU'(Z) -> dZ bf16 [B x N], dZT bf16 [N x B], dZf f32
-__global__ void k_gelu_back(const float* __restrict__ dX, const float* __restrict__ Z, int B,
-                            int N, __nv_bfloat16* __restrict__ dZ, __nv_bfloat16* __restrict__ dZT,
-                            float* __restrict__ dZf) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= B * N) return;
-    const int b = i / N, n = i % N;
-    const float g = dX[i] * gelu_grad(Z[i]);
-    dZf[i] = g;
-    const __nv_bfloat16 h = __float2bfloat16(g);
-    dZ[i] = h;
-    dZT[(size_t)n * B + b] = h;
-}
-
-// bias gradient: column sums over the batch
-__global__ void k_colsum(const float* __restrict__ G, int B, int N, float* __restrict__ out) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+// Bias gradients of every layer in one launch: column sums over the batch of each layer's
+// output gradient (one thread per column of the concatenated layers, fixed summation order)
+constexpr int PN_MAX_LAYERS = 16;
+struct ColsumTable {
+    const float* g[PN_MAX_LAYERS];
+    float* out[PN_MAX_LAYERS];
+    int n[PN_MAX_LAYERS];
+    int start[PN_MAX_LAYERS + 1];
+    int layers;
+};
+__global__ void k_colsum_all(const ColsumTable t, int B) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= t.start[t.layers]) return;
+    int l = 0;
+    while (c >= t.start[l + 1]) ++l;
+    const int n = c - t.start[l], N = t.n[l];
+    const float* G = t.g[l];
     float s = 0.f;
     for (int b = 0; b < B; ++b) s += G[(size_t)b * N + n];
-    out[n] = s;
+    t.out[l][n] = s;
 }
 
 // loss and output gradient, one thread per sample; O [B x P*4] (biased), T [B x 3]
@@ -156,24 +155,43 @@ __global__ void k_loss(const float* __restrict__ O, const float* __restrict__ T,
     }
 }
 
-// Adam on f32 masters, refreshed bf16 copy (and transposed copy) of a [R x C] weight
-__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
-                       float* __restrict__ v, size_t n, int C, float lr, float b1, float b2,
-                       float eps, float c1, float c2, __nv_bfloat16* __restrict__ wb,
-                       __nv_bfloat16* __restrict__ wbt, int R) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.f - b1) * gi;
-    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    w[i] = wi;
-    if (wb) {
+// Adam on the f32 masters of every parameter tensor in one launch (weights and biases of all
+// layers, concatenated), refreshing each weight's bf16 copy and bf16 transposed copy. The
+// step count t comes from the device counter the step's sampling kernel advanced, so a
+// captured training step replays without host updates.
+struct AdamTable {
+    float* w[2 * PN_MAX_LAYERS];
+    const float* g[2 * PN_MAX_LAYERS];
+    float* m[2 * PN_MAX_LAYERS];
+    float* v[2 * PN_MAX_LAYERS];
+    __nv_bfloat16* wb[2 * PN_MAX_LAYERS];
+    __nv_bfloat16* wbt[2 * PN_MAX_LAYERS];
+    int cols[2 * PN_MAX_LAYERS];   // C of a [R x C] weight (the transposed copy's index rule)
+    int rows[2 * PN_MAX_LAYERS];
+    uint64_t start[2 * PN_MAX_LAYERS + 1];
+    int tensors;
+};
+__global__ void k_adam_all(const AdamTable t, const uint64_t* __restrict__ step_ctr, float lr,
+                           float b1, float b2, float eps) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.start[t.tensors]) return;
+    int k = 0;
+    while (i >= t.start[k + 1]) ++k;
+    const size_t j = (size_t)(i - t.start[k]);
+    const float step = (float)*step_ctr;
+    const float c1 = 1.f - powf(b1, step), c2 = 1.f - powf(b2, step);
+    const float gi = t.g[k][j];
+    const float mi = b1 * t.m[k][j] + (1.f - b1) * gi;
+    const float vi = b2 * t.v[k][j] + (1.f - b2) * gi * gi;
+    t.m[k][j] = mi;
+    t.v[k][j] = vi;
+    const float wi = t.w[k][j] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    t.w[k][j] = wi;
+    if (t.wb[k]) {
         const __nv_bfloat16 h = __float2bfloat16(wi);
-        wb[i] = h;
-        if (wbt) wbt[(size_t)(i % C) * R + i / C] = h;
+        t.wb[k][j] = h;
+        const int C = t.cols[k];
+        if (t.wbt[k]) t.wbt[k][(size_t)(j % C) * t.rows[k] + j / C] = h;
     }
 }
 
@@ -242,7 +260,7 @@ __global__ void k_features(const float* __restrict__ scan_pts, const PnScan* __r
         if (gx < 0 || gy < 0 || gz < 0 || gx >= PN_GRID || gy >= PN_GRID || gz >= PN_ZB) continue;
         const int f = (gx * PN_GRID + gy) * PN_ZB + gz;
         X[(size_t)b * F + f] = one;
-        XT[(size_t)f * B + b] = one;
+        if (XT) XT[(size_t)f * B + b] = one;
     }
     const PnMap m = maps[s.map];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < PN_MAP_FEATS; c += gridDim.x * blockDim.x) {
@@ -260,7 +278,7 @@ __global__ void k_features(const float* __restrict__ scan_pts, const PnScan* __r
         const __nv_bfloat16 h = __float2bfloat16(val);
         const int f = PN_SCAN_FEATS + c;
         X[(size_t)b * F + f] = h;
-        XT[(size_t)f * B + b] = h;
+        if (XT) XT[(size_t)f * B + b] = h;
     }
 }
 
@@ -275,12 +293,10 @@ __device__ __forceinline__ float sm_unit(uint64_t& s) {
     return (float)(sm64(s) >> 40) * (1.f / 16777216.f);
 }
 
-// training batch: random scan, coarse pose = converged pose + (U(+-r), U(+-r)), yaw uniform
-__global__ void k_sample(uint64_t seed, uint64_t step, int B, uint32_t n_scans,
-                         const PnScan* __restrict__ scans, const double* __restrict__ conv,
-                         float xy_range, PnSample* __restrict__ smp, float* __restrict__ T) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
+__device__ __forceinline__ void sample_one(uint64_t seed, uint64_t step, int b,
+                                           uint32_t n_scans, const PnScan* __restrict__ scans,
+                                           const double* __restrict__ conv, float xy_range,
+                                           PnSample* __restrict__ smp, float* __restrict__ T) {
     uint64_t s = seed ^ (0x9e3779b97f4a7c15ull * (step + 1)) ^ (0xd1b54a32d192ed03ull * (b + 1));
     sm64(s);
     const uint32_t k = (uint32_t)(sm64(s) % n_scans);
@@ -300,6 +316,23 @@ __global__ void k_sample(uint64_t seed, uint64_t step, int B, uint32_t n_scans,
     T[3 * b + 2] = wrap_pi((float)c[5] - yaw);
 }
 
+
+// training batch: random scan, coarse pose = converged pose + (U(+-r), U(+-r)), yaw uniform.
+// One block: it reads the step counter, draws the batch of that step and advances the
+// counter (the later kernels of the step read the new value as Adam's step count t).
+__global__ void k_sample(uint64_t seed, uint64_t* __restrict__ step_ctr, int B,
+                         uint32_t n_scans, const PnScan* __restrict__ scans,
+                         const double* __restrict__ conv, float xy_range,
+                         PnSample* __restrict__ smp, float* __restrict__ T) {
+    __shared__ uint64_t s_step;
+    if (threadIdx.x == 0) s_step = *step_ctr;
+    __syncthreads();
+    const uint64_t step = s_step;
+    for (int b = threadIdx.x; b < B; b += blockDim.x)
+        sample_one(seed, step, b, n_scans, scans, conv, xy_range, smp, T);
+    __syncthreads();
+    if (threadIdx.x == 0) *step_ctr = step + 1;
+}
 // proposals: pose = coarse + (4 o0, 4 o1, 0, 0, 0, pi o2), yaw wrapped; logits o3
 __global__ void k_decode(const float* __restrict__ O, const PnSample* __restrict__ smp,
                          const double* __restrict__ coarse6, int B, int P,
@@ -340,7 +373,7 @@ struct ndt_pnet {
     std::vector<PnLayer> L;
     // batch buffers (capacity cap_b samples)
     int cap_b = 0;
-    std::vector<DevBuf> X, XT, Z, dZ, dZT, dZf, dX;  // per layer
+    std::vector<DevBuf> X, XT, Z, dZ, dZT, dZf;  // per layer
     DevBuf loss, T, smp, coarse, poses, logits, err;
     DevBuf Zp;              // split-K partial products
     DevBuf q_pts, q_scans;  // inference queries
@@ -355,6 +388,10 @@ struct ndt_pnet {
     bool data_dirty = true;
     uint64_t step = 0;
     PinBuf h_loss;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // CUDA-event timing on the network's stream
+    ndt_pnet_stats stats{};
+    DevBuf step_ctr;                    // Adam step count on the device (advanced by k_sample)
+    cudaGraphExec_t train_exec = nullptr;  // one captured training step, replayed
 };
 
 static uint64_t host_sm64(uint64_t& s) {
@@ -386,7 +423,6 @@ static int pn_reserve_batch(ndt_pnet* p, int B) {
     p->dZ.resize(nl);
     p->dZT.resize(nl);
     p->dZf.resize(nl);
-    p->dX.resize(nl);
     int rc;
     for (int l = 0; l < nl; ++l) {
         const size_t in = p->L[l].in, out = p->L[l].out;
@@ -395,8 +431,7 @@ static int pn_reserve_batch(ndt_pnet* p, int B) {
             (rc = dev_reserve(p->Z[l], (size_t)B * out * 4)) ||
             (rc = dev_reserve(p->dZ[l], (size_t)B * out * 2)) ||
             (rc = dev_reserve(p->dZT[l], (size_t)B * out * 2)) ||
-            (rc = dev_reserve(p->dZf[l], (size_t)B * out * 4)) ||
-            (rc = dev_reserve(p->dX[l], (size_t)B * in * 4)))
+            (rc = dev_reserve(p->dZf[l], (size_t)B * out * 4)))
             return rc;
     }
     const size_t no = (size_t)p->cfg.proposals * PN_OUT_PER;
@@ -416,6 +451,11 @@ static int pn_reserve_batch(ndt_pnet* p, int B) {
 
 static int pn_upload_data(ndt_pnet* p) {
     if (!p->data_dirty) return 0;
+    // the captured training step holds the data buffers' addresses, which may move here
+    if (p->train_exec) {
+        cudaGraphExecDestroy(p->train_exec);
+        p->train_exec = nullptr;
+    }
     int rc;
     if ((rc = dev_reserve(p->maps_d, std::max<size_t>(1, p->maps_h.size()) * sizeof(PnMap))) ||
         (rc = dev_reserve(p->scan_pts_d, std::max<size_t>(1, p->scan_pts_h.size()) * 4)) ||
@@ -441,56 +481,78 @@ static int pn_upload_data(ndt_pnet* p) {
 
 static inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
-// forward over X[0] (already filled) for B samples; leaves the biased output in Z[last]
-static int pn_forward(ndt_pnet* p, int B) {
+// forward over X[0] (already filled) for B samples; leaves the biased output in Z[last].
+// Layers after the first add their bias and activation in the GEMM's epilogue, which also
+// writes the next layer's bf16 input (and, for training, its transposed copy). The input
+// layer's long K is split so every SM streams a share of the operands; its partial products
+// are summed by k_bias_act.
+static int pn_forward(ndt_pnet* p, int B, bool need_t) {
     const int nl = (int)p->L.size();
     cudaStream_t s = p->stream;
     int rc;
     for (int l = 0; l < nl; ++l) {
         PnLayer& L = p->L[l];
-        // a long K over few output tiles (the input layer) is split so every SM streams a
-        // share of the operands
+        const bool last = l == nl - 1;
         const int tiles = ((B + 127) / 128) * ((L.out + 127) / 128);
         int splits = 1;
         if (tiles < 64 && L.in >= 4096) splits = std::min(PN_MAX_SPLITS, L.in / 64 / 8);
-        float* dst = splits > 1 ? (float*)p->Zp.p : (float*)p->Z[l].p;
-        if ((rc = gemm_bf16_tn(p->X[l].p, L.wb.p, dst, B, L.out, L.in, L.out,
-                               (uint32_t*)p->err.p, s, splits)))
+        if (splits > 1) {
+            if ((rc = gemm_bf16_tn(p->X[l].p, L.wb.p, (float*)p->Zp.p, B, L.out, L.in, L.out,
+                                   (uint32_t*)p->err.p, s, splits, nullptr)))
+                return rc;
+            k_bias_act<<<blocks((size_t)B * L.out), 256, 0, s>>>(
+                (float*)p->Z[l].p, (const float*)p->Zp.p, splits, (const float*)L.b.p, B, L.out,
+                last ? 1 : 0, last ? nullptr : (__nv_bfloat16*)p->X[l + 1].p,
+                last || !need_t ? nullptr : (__nv_bfloat16*)p->XT[l + 1].p);
+            continue;
+        }
+        GemmEpilogue e{};
+        e.mode = last ? GEMM_EPI_BIAS : GEMM_EPI_BIAS_GELU;
+        e.bias = (const float*)L.b.p;
+        e.x = last ? nullptr : (__nv_bfloat16*)p->X[l + 1].p;
+        e.xt = last || !need_t ? nullptr : (__nv_bfloat16*)p->XT[l + 1].p;
+        if ((rc = gemm_bf16_tn(p->X[l].p, L.wb.p, (float*)p->Z[l].p, B, L.out, L.in, L.out,
+                               (uint32_t*)p->err.p, s, 1, &e)))
             return rc;
-        const bool last = l == nl - 1;
-        k_bias_act<<<blocks((size_t)B * L.out), 256, 0, s>>>(
-            (float*)p->Z[l].p, splits > 1 ? (const float*)p->Zp.p : nullptr, splits,
-            (const float*)L.b.p, B, L.out, last ? 1 : 0,
-            last ? nullptr : (__nv_bfloat16*)p->X[l + 1].p,
-            last ? nullptr : (__nv_bfloat16*)p->XT[l + 1].p);
     }
     return cuda_fail(cudaGetLastError(), "proposal forward");
 }
 
-// backward from the loss gradient in dZ*[last]; fills every layer's gw, gb
+// backward from the loss gradient in dZ*[last]; fills every layer's gw, gb. The input
+// gradient's GEMM applies GELU' of the layer below in its epilogue and writes that layer's
+// output gradient in f32 and in both bf16 layouts; the bias gradients are one launch.
 static int pn_backward(ndt_pnet* p, int B) {
     const int nl = (int)p->L.size();
     cudaStream_t s = p->stream;
     int rc;
+    ColsumTable ct{};
+    ct.layers = nl;
+    ct.start[0] = 0;
     for (int l = nl - 1; l >= 0; --l) {
         PnLayer& L = p->L[l];
         // dW = dZ^T X  (A = dZ^T [out x B], B-operand = X^T [in x B])
         if ((rc = gemm_bf16_tn(p->dZT[l].p, p->XT[l].p, (float*)L.gw.p, L.out, L.in, B, L.in,
-                               (uint32_t*)p->err.p, s, 1)))
+                               (uint32_t*)p->err.p, s, 1, nullptr)))
             return rc;
-        k_colsum<<<blocks(L.out), 256, 0, s>>>((const float*)p->dZf[l].p, B, L.out,
-                                               (float*)L.gb.p);
         if (l > 0) {
-            // dX = dZ W  (A = dZ [B x out], B-operand = W^T [in x out])
-            if ((rc = gemm_bf16_tn(p->dZ[l].p, L.wbt.p, (float*)p->dX[l].p, B, L.in, L.out,
-                                   L.in, (uint32_t*)p->err.p, s, 1)))
+            // dX = dZ W  (A = dZ [B x out], B-operand = W^T [in x out]), then * GELU'(Z_{l-1})
+            GemmEpilogue e{};
+            e.mode = GEMM_EPI_GELU_BACK;
+            e.zin = (const float*)p->Z[l - 1].p;
+            e.x = (__nv_bfloat16*)p->dZ[l - 1].p;
+            e.xt = (__nv_bfloat16*)p->dZT[l - 1].p;
+            if ((rc = gemm_bf16_tn(p->dZ[l].p, L.wbt.p, (float*)p->dZf[l - 1].p, B, L.in, L.out,
+                                   L.in, (uint32_t*)p->err.p, s, 1, &e)))
                 return rc;
-            k_gelu_back<<<blocks((size_t)B * L.in), 256, 0, s>>>(
-                (const float*)p->dX[l].p, (const float*)p->Z[l - 1].p, B, L.in,
-                (__nv_bfloat16*)p->dZ[l - 1].p, (__nv_bfloat16*)p->dZT[l - 1].p,
-                (float*)p->dZf[l - 1].p);
         }
     }
+    for (int l = 0; l < nl; ++l) {
+        ct.g[l] = (const float*)p->dZf[l].p;
+        ct.out[l] = (float*)p->L[l].gb.p;
+        ct.n[l] = p->L[l].out;
+        ct.start[l + 1] = ct.start[l] + p->L[l].out;
+    }
+    k_colsum_all<<<blocks(ct.start[nl]), 256, 0, s>>>(ct, B);
     return cuda_fail(cudaGetLastError(), "proposal backward");
 }
 
@@ -504,34 +566,68 @@ static int pn_loss(ndt_pnet* p, int B) {
     return cuda_fail(cudaGetLastError(), "proposal loss");
 }
 
+// Adam over every parameter tensor in one launch; the step count is the device counter
 static int pn_adam(ndt_pnet* p) {
-    p->step++;
-    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    const float c1 = 1.f - powf(b1, (float)p->step), c2 = 1.f - powf(b2, (float)p->step);
-    cudaStream_t s = p->stream;
+    AdamTable t{};
+    int k = 0;
+    t.start[0] = 0;
     for (size_t l = 0; l < p->L.size(); ++l) {
         PnLayer& L = p->L[l];
         const size_t nw = (size_t)L.in * L.out;
-        k_adam<<<blocks(nw), 256, 0, s>>>((float*)L.w.p, (const float*)L.gw.p, (float*)L.mw.p,
-                                           (float*)L.vw.p, nw, L.in, p->cfg.learning_rate, b1,
-                                           b2, eps, c1, c2, (__nv_bfloat16*)L.wb.p,
-                                           l > 0 ? (__nv_bfloat16*)L.wbt.p : nullptr, L.out);
-        k_adam<<<blocks(L.out), 256, 0, s>>>((float*)L.b.p, (const float*)L.gb.p, (float*)L.mb.p,
-                                              (float*)L.vb.p, L.out, L.out, p->cfg.learning_rate,
-                                              b1, b2, eps, c1, c2, nullptr, nullptr, 1);
+        t.w[k] = (float*)L.w.p;
+        t.g[k] = (const float*)L.gw.p;
+        t.m[k] = (float*)L.mw.p;
+        t.v[k] = (float*)L.vw.p;
+        t.wb[k] = (__nv_bfloat16*)L.wb.p;
+        t.wbt[k] = l > 0 ? (__nv_bfloat16*)L.wbt.p : nullptr;
+        t.cols[k] = L.in;
+        t.rows[k] = L.out;
+        t.start[k + 1] = t.start[k] + nw;
+        ++k;
+        t.w[k] = (float*)L.b.p;
+        t.g[k] = (const float*)L.gb.p;
+        t.m[k] = (float*)L.mb.p;
+        t.v[k] = (float*)L.vb.p;
+        t.wb[k] = nullptr;
+        t.wbt[k] = nullptr;
+        t.cols[k] = L.out;
+        t.rows[k] = 1;
+        t.start[k + 1] = t.start[k] + (uint64_t)L.out;
+        ++k;
     }
+    t.tensors = k;
+    k_adam_all<<<blocks(t.start[k]), 256, 0, p->stream>>>(
+        t, (const uint64_t*)p->step_ctr.p, p->cfg.learning_rate, 0.9f, 0.999f, 1e-8f);
     return cuda_fail(cudaGetLastError(), "proposal update");
 }
 
-static int pn_features(ndt_pnet* p, int B, const void* pts, const void* scans) {
+// input features of B samples into X[0] (and, for training, the transposed copy XT[0])
+static int pn_features(ndt_pnet* p, int B, const void* pts, const void* scans, bool need_t) {
     const size_t F = (size_t)p->L[0].in;
     cudaMemsetAsync(p->X[0].p, 0, (size_t)B * F * 2, p->stream);
-    cudaMemsetAsync(p->XT[0].p, 0, (size_t)B * F * 2, p->stream);
+    if (need_t) cudaMemsetAsync(p->XT[0].p, 0, (size_t)B * F * 2, p->stream);
     k_features<<<dim3(8, B), 256, 0, p->stream>>>(
         (const float*)pts, (const PnScan*)scans, (const PnSample*)p->smp.p,
         (const PnMap*)p->maps_d.p, B, (int)F, (__nv_bfloat16*)p->X[0].p,
-        (__nv_bfloat16*)p->XT[0].p);
+        need_t ? (__nv_bfloat16*)p->XT[0].p : nullptr);
     return cuda_fail(cudaGetLastError(), "proposal features");
+}
+
+// One training step on the network's stream: sample a batch (advancing the device step
+// counter), features, forward, loss, backward, Adam. Stream-ordered only, so it can be
+// captured into a graph.
+static int pn_train_step(ndt_pnet* p, int B) {
+    cudaStream_t s = p->stream;
+    k_sample<<<1, 256, 0, s>>>(p->cfg.seed, (uint64_t*)p->step_ctr.p, B,
+                               (uint32_t)p->scans_h.size(), (const PnScan*)p->scans_d.p,
+                               (const double*)p->conv_d.p, p->cfg.xy_range, (PnSample*)p->smp.p,
+                               (float*)p->T.p);
+    int rc;
+    if ((rc = pn_features(p, B, p->scan_pts_d.p, p->scans_d.p, true)) ||
+        (rc = pn_forward(p, B, true)) || (rc = pn_loss(p, B)) || (rc = pn_backward(p, B)) ||
+        (rc = pn_adam(p)))
+        return rc;
+    return 0;
 }
 
 extern "C" {
@@ -561,7 +657,8 @@ int ndt_pnet_create(const ndt_pnet_config* cfg, int32_t device, ndt_pnet** out) 
         ndt_pnet_config_default(&c);
     const int no = c.proposals * PN_OUT_PER;
     if (c.input_dim <= 0 || c.input_dim % 64 || c.hidden <= 0 || c.hidden % 64 ||
-        c.hidden_layers < 1 || c.proposals < 1 || no % 64 || c.batch < 1 || c.batch % 64 ||
+        c.hidden_layers < 1 || c.hidden_layers + 1 > PN_MAX_LAYERS || c.proposals < 1 ||
+        no % 64 || c.batch < 1 || c.batch % 64 ||
         !(c.learning_rate > 0.f)) {
         set_error("proposal network: input_dim, hidden, 4 * proposals and batch must be "
                   "positive multiples of 64");
@@ -577,8 +674,11 @@ int ndt_pnet_create(const ndt_pnet_config* cfg, int32_t device, ndt_pnet** out) 
     p->cfg = c;
     p->device = device;
     cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    cudaEventCreate(&p->ev0);
+    cudaEventCreate(&p->ev1);
     int rc = dev_reserve(p->err, 16);
     if (!rc) cudaMemsetAsync(p->err.p, 0, 16, p->stream);
+    if (!rc && !(rc = dev_reserve(p->step_ctr, 8))) cudaMemsetAsync(p->step_ctr.p, 0, 8, p->stream);
     // layers: input -> hidden x hidden_layers -> 4 * proposals; weights N(0, 2 / in)
     std::vector<int> dims = {c.input_dim};
     for (int i = 0; i < c.hidden_layers; ++i) dims.push_back(c.hidden);
@@ -638,7 +738,7 @@ int ndt_pnet_destroy(ndt_pnet* p) {
     for (auto& L : p->L)
         for (DevBuf* b : {&L.w, &L.b, &L.wb, &L.wbt, &L.mw, &L.vw, &L.mb, &L.vb, &L.gw, &L.gb})
             dev_free(*b);
-    for (auto* v : {&p->X, &p->XT, &p->Z, &p->dZ, &p->dZT, &p->dZf, &p->dX})
+    for (auto* v : {&p->X, &p->XT, &p->Z, &p->dZ, &p->dZT, &p->dZf})
         for (auto& b : *v) dev_free(b);
     for (auto& b : p->map_imgs) dev_free(b);
     for (DevBuf* b : {&p->loss, &p->T, &p->smp, &p->coarse, &p->poses, &p->logits, &p->err,
@@ -646,6 +746,10 @@ int ndt_pnet_destroy(ndt_pnet* p) {
                       &p->conv_d})
         dev_free(*b);
     pin_free(p->h_loss);
+    if (p->train_exec) cudaGraphExecDestroy(p->train_exec);
+    dev_free(p->step_ctr);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return NDT_OK;
@@ -733,16 +837,31 @@ int ndt_pnet_train(ndt_pnet* p, uint64_t steps, float* loss_out) {
     if (rc) return rc;
     const int B = p->cfg.batch;
     cudaStream_t s = p->stream;
+    cudaEventRecord(p->ev0, s);
     for (uint64_t it = 0; it < steps; ++it) {
-        k_sample<<<blocks(B, 128), 128, 0, s>>>(p->cfg.seed, p->step, B,
-                                                 (uint32_t)p->scans_h.size(),
-                                                 (const PnScan*)p->scans_d.p,
-                                                 (const double*)p->conv_d.p, p->cfg.xy_range,
-                                                 (PnSample*)p->smp.p, (float*)p->T.p);
-        if ((rc = pn_features(p, B, p->scan_pts_d.p, p->scans_d.p)) || (rc = pn_forward(p, B)) ||
-            (rc = pn_loss(p, B)) ||
-            (rc = pn_backward(p, B)) || (rc = pn_adam(p)))
-            return rc;
+        if (p->train_exec) {
+            rc = cuda_fail(cudaGraphLaunch(p->train_exec, s), "proposal training step");
+        } else {
+            // the first step runs eagerly (kernel attributes, launch checks); the step is
+            // then captured once and replayed: every step reads its step count from the
+            // device counter, so the replays need no host updates
+            if ((rc = pn_train_step(p, B)) || (rc = pn_check(p, "proposal training"))) return rc;
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                const int rc_cap = pn_train_step(p, B);
+                e = cudaStreamEndCapture(s, &g);
+                if (rc_cap) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc_cap;
+                }
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&p->train_exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if ((rc = cuda_fail(e, "proposal training step capture"))) return rc;
+        }
+        if (rc) return rc;
+        p->step++;
         if (loss_out) {
             cudaMemcpyAsync(p->h_loss.p, p->loss.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s);
             if ((rc = pn_check(p, "proposal training"))) return rc;
@@ -751,7 +870,12 @@ int ndt_pnet_train(ndt_pnet* p, uint64_t steps, float* loss_out) {
             loss_out[it] = (float)(acc / B);
         }
     }
-    return pn_check(p, "proposal training");
+    cudaEventRecord(p->ev1, s);
+    if ((rc = pn_check(p, "proposal training"))) return rc;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p->ev0, p->ev1) == cudaSuccess) p->stats.train_ms += ms;
+    p->stats.train_steps += steps;
+    return NDT_OK;
 }
 
 int ndt_pnet_propose(ndt_pnet* p, int32_t map_id, const ndt_scan* q, uint64_t nq,
@@ -795,17 +919,32 @@ int ndt_pnet_propose(ndt_pnet* p, int32_t map_id, const ndt_scan* q, uint64_t nq
         const int B = (int)std::min<uint64_t>(nq - b0, (uint64_t)p->cfg.batch);
         cudaMemcpyAsync(p->smp.p, smp.data() + b0, B * sizeof(PnSample), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(p->coarse.p, coarse.data() + 6 * b0, B * 48, cudaMemcpyHostToDevice, s);
-        if ((rc = pn_features(p, B, p->q_pts.p, p->q_scans.p)) || (rc = pn_forward(p, B))) break;
+        cudaEventRecord(p->ev0, s);
+        if ((rc = pn_features(p, B, p->q_pts.p, p->q_scans.p, false)) ||
+            (rc = pn_forward(p, B, false)))
+            break;
         k_decode<<<blocks((size_t)B * P), 256, 0, s>>>(
             (const float*)p->Z[p->L.size() - 1].p, (const PnSample*)p->smp.p,
             (const double*)p->coarse.p, B, P, (double*)p->poses.p, (double*)p->logits.p);
+        cudaEventRecord(p->ev1, s);
         cudaMemcpyAsync(poses + 6 * P * b0, p->poses.p, (size_t)B * P * 48, cudaMemcpyDeviceToHost, s);
         if (logits)
             cudaMemcpyAsync(logits + P * b0, p->logits.p, (size_t)B * P * 8,
                             cudaMemcpyDeviceToHost, s);
         rc = pn_check(p, "proposal inference");
+        float ms = 0.f;
+        if (!rc && cudaEventElapsedTime(&ms, p->ev0, p->ev1) == cudaSuccess)
+            p->stats.inference_kernel_ms += ms;
+        p->stats.inference_batches++;
     }
+    if (!rc) p->stats.queries += nq;
     return rc;
+}
+
+int ndt_pnet_stats_get(ndt_pnet* p, ndt_pnet_stats* out) {
+    if (!p || !out) return NDT_ERR_INVALID_ARGUMENT;
+    *out = p->stats;
+    return NDT_OK;
 }
 
 // One forward + backward on caller-given inputs (no features, no update): the loss and every
@@ -833,7 +972,8 @@ int ndt_pnet_debug_grad(ndt_pnet* p, const float* x, const float* targets, uint6
     cudaMemcpyAsync(p->XT[0].p, xt.data(), xt.size() * 2, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(p->T.p, targets, (size_t)B * 12, cudaMemcpyHostToDevice, s);
     int rc;
-    if ((rc = pn_forward(p, B)) || (rc = pn_loss(p, B)) || (rc = pn_backward(p, B))) return rc;
+    if ((rc = pn_forward(p, B, true)) || (rc = pn_loss(p, B)) || (rc = pn_backward(p, B)))
+        return rc;
     std::vector<float> lb(B);
     cudaMemcpyAsync(lb.data(), p->loss.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s);
     size_t off = 0;

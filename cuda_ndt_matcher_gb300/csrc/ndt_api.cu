@@ -1207,6 +1207,8 @@ static void stats_add(ndt_stats& a, const ndt_stats& b) {
     a.cycles_control += b.cycles_control;
     a.cycles_broadcast += b.cycles_broadcast;
     a.eigen_solves += b.eigen_solves;
+    a.proposal_launches += b.proposal_launches;
+    a.proposal_kernel_ms += b.proposal_kernel_ms;
 }
 
 static AsyncSlot* find_ticket(ndt_ctx* c, uint64_t ticket) {
@@ -1662,7 +1664,12 @@ int ndt_learned_pose_search(ndt_ctx* c, ndt_pnet* net, int32_t map_id, const ndt
     if ((rc = ndt_pnet_get_config(net, &pcfg))) return rc;
     const uint64_t np = (uint64_t)pcfg.proposals;
     std::vector<double> starts(nq * np * 6);
+    ndt_pnet_stats before, after;
+    ndt_pnet_stats_get(net, &before);
     if ((rc = ndt_pnet_propose(net, map_id, queries, nq, starts.data(), nullptr))) return rc;
+    ndt_pnet_stats_get(net, &after);
+    c->stats.proposal_launches += after.inference_batches - before.inference_batches;
+    c->stats.proposal_kernel_ms += after.inference_kernel_ms - before.inference_kernel_ms;
     if ((rc = search_from_starts(c, queries, nq, np, starts.data(), out, nullptr))) return rc;
     std::vector<uint64_t> redo;
     for (uint64_t q = 0; q < nq; ++q) {

@@ -1,6 +1,7 @@
 // ndt_internal.h — host-side structures shared by the library's translation units.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -14,6 +15,24 @@
 namespace ndtgb {
 
 // Grow-only device allocation owned by a context.
+// Elementwise work fused into the tcgen05 GEMM's epilogue (tc_gemm.cu), per element (row m,
+// column n) of the accumulator acc:
+//   GEMM_EPI_STORE        D = acc
+//   GEMM_EPI_BIAS_GELU    z = acc + bias[n]: D = z, x = GELU(z) as bf16 into x [M x N] and
+//                         xt [N x M] (the next layer's input in both operand layouts)
+//   GEMM_EPI_BIAS         z = acc + bias[n]: D = z (the output layer)
+//   GEMM_EPI_GELU_BACK    g = acc * GELU'(zin[m][n]): D = g, bf16 g into x [M x N] and
+//                         xt [N x M] (the previous layer's output gradient)
+// Not with split-K (a partial product has no bias and no activation).
+enum { GEMM_EPI_STORE = 0, GEMM_EPI_BIAS_GELU = 1, GEMM_EPI_BIAS = 2, GEMM_EPI_GELU_BACK = 3 };
+struct GemmEpilogue {
+    int mode;
+    const float* bias;
+    const float* zin;
+    __nv_bfloat16* x;
+    __nv_bfloat16* xt;
+};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;

@@ -12,15 +12,32 @@
 //   warp 1, lane 0  MMA issuer: per stage four tcgen05.mma.kind::f16 (M 128, N 128, K 16)
 //                   into a 128-column f32 accumulator in tensor memory; tcgen05.commit
 //                   arrives on the stage's "empty" mbarrier when those MMAs are done;
-//   warps 0-3       epilogue: tcgen05.ld of their 32 accumulator rows, f32 stores.
+//   warps 0-3       epilogue: tcgen05.ld of their 32 accumulator rows, f32 stores, and
+//                   optionally the network's elementwise step fused in (GemmEpilogue): bias
+//                   + GELU (or identity) with the activation stored as bf16 in both layouts,
+//                   or the GELU derivative of the backward pass.
 // Every mbarrier wait is bounded (about one second of the global timer); on timeout the CTA
 // records an error code in *err, stops issuing work and frees its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 
 #include "ndt_internal.h"
 
 namespace ndtgb {
+
+__device__ __forceinline__ float gelu_tanh(float z) {  // tanh approximation of GELU
+    const float k = 0.7978845608f;                      // sqrt(2 / pi)
+    const float u = k * (z + 0.044715f * z * z * z);
+    return 0.5f * z * (1.f + tanhf(u));
+}
+__device__ __forceinline__ float gelu_tanh_grad(float z) {
+    const float k = 0.7978845608f;
+    const float u = k * (z + 0.044715f * z * z * z);
+    const float t = tanhf(u);
+    return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * k * (1.f + 3.f * 0.044715f * z * z);
+}
+
 
 constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 4;
 constexpr int GB_TILE_BYTES = GB_M * GB_K * 2;          // 16 KB per operand box
@@ -79,10 +96,60 @@ __host__ __device__ constexpr uint32_t mma_idesc_bf16(int m, int n) {
            ((uint32_t)(m >> 4) << 24);
 }
 
+// Fused epilogue of 32 accumulator columns [c0, c0 + 32) of row `row` (one lane = one row):
+// per column, the 32 lanes of a warp write 32 consecutive rows of xt (64 coalesced bytes);
+// the row-major outputs go out as 16-byte vectors.
+__device__ __forceinline__ void epilogue_fused(const GemmEpilogue& epi, const uint32_t* r,
+                                               float* D, int ldd, int M, int N, int row,
+                                               int c0) {
+    const bool in_row = row < M;
+    float v[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+        const int n = c0 + q;
+        float a = __uint_as_float(r[q]);
+        float out = a;
+        if (n < N) {
+            if (epi.mode == GEMM_EPI_GELU_BACK) {
+                const float z = in_row ? epi.zin[(size_t)row * N + n] : 0.f;
+                out = a * gelu_tanh_grad(z);
+                v[q] = out;
+            } else {
+                out = a + epi.bias[n];
+                v[q] = epi.mode == GEMM_EPI_BIAS_GELU ? gelu_tanh(out) : out;
+            }
+            if (in_row) D[(size_t)row * ldd + n] = out;
+            if (epi.xt && in_row) epi.xt[(size_t)n * M + row] = __float2bfloat16(v[q]);
+        } else {
+            v[q] = 0.f;
+        }
+    }
+    if (epi.x && in_row) {
+        __nv_bfloat16* xr = epi.x + (size_t)row * N + c0;
+        if (c0 + 32 <= N && (N & 7) == 0) {
+#pragma unroll
+            for (int q = 0; q < 32; q += 8) {
+                __nv_bfloat162 h0 = __floats2bfloat162_rn(v[q], v[q + 1]);
+                __nv_bfloat162 h1 = __floats2bfloat162_rn(v[q + 2], v[q + 3]);
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(v[q + 4], v[q + 5]);
+                __nv_bfloat162 h3 = __floats2bfloat162_rn(v[q + 6], v[q + 7]);
+                uint4 u;
+                u.x = *reinterpret_cast<uint32_t*>(&h0);
+                u.y = *reinterpret_cast<uint32_t*>(&h1);
+                u.z = *reinterpret_cast<uint32_t*>(&h2);
+                u.w = *reinterpret_cast<uint32_t*>(&h3);
+                *reinterpret_cast<uint4*>(xr + q) = u;
+            }
+        } else {
+            for (int q = 0; q < 32 && c0 + q < N; ++q) xr[q] = __float2bfloat16(v[q]);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128, 1)
     k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    float* __restrict__ D, int M, int N, int K, int ldd, int splits,
-                   size_t split_stride, uint32_t* err) {
+                   size_t split_stride, uint32_t* err, const GemmEpilogue epi) {
     extern __shared__ __align__(1024) uint8_t gb_smem_raw[];
     __shared__ __align__(8) uint64_t full[GB_STAGES], empty[GB_STAGES], done;
     __shared__ uint32_t tmem_base;
@@ -201,6 +268,10 @@ __global__ void __launch_bounds__(128, 1)
                   "=r"(r[30]), "=r"(r[31])
                 : "r"(ta));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (epi.mode != GEMM_EPI_STORE) {
+                epilogue_fused(epi, r, D, ldd, M, N, row, n0 + c);
+                continue;
+            }
             if (row < M) {
                 float* dst = D + (size_t)row * ldd + n0 + c;
                 if (n0 + c + 32 <= N) {
@@ -264,12 +335,21 @@ static int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t co
 
 // splits > 1: split-K, partial products of k-range z at D + z * M * ldd (the caller sums)
 int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, int ldd,
-                 uint32_t* d_err, cudaStream_t s, int splits) {
+                 uint32_t* d_err, cudaStream_t s, int splits, const GemmEpilogue* epi) {
     if (M <= 0 || N <= 0 || K <= 0 || K % GB_K || ldd < N || ((uintptr_t)A & 15) ||
         ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || (ldd & 3) || splits < 1 ||
         splits > K / GB_K || splits > 65535) {
         set_error("gemm: K must be a multiple of 64, operands 16-byte aligned, ldd >= N, "
                   "1 <= splits <= K / 64");
+        return NDT_ERR_INVALID_ARGUMENT;
+    }
+    GemmEpilogue e{};
+    if (epi) e = *epi;
+    if (e.mode != GEMM_EPI_STORE &&
+        (splits != 1 || ldd != N || ((uintptr_t)e.x & 15) ||
+         (e.mode == GEMM_EPI_GELU_BACK ? !e.zin : !e.bias))) {
+        set_error("gemm: a fused epilogue needs splits = 1, ldd = N, its bias (or input) and "
+                  "16-byte aligned outputs");
         return NDT_ERR_INVALID_ARGUMENT;
     }
     CUtensorMap ta, tb;
@@ -285,7 +365,7 @@ int gemm_bf16_tn(const void* A, const void* B, float* D, int M, int N, int K, in
     dim3 grid((unsigned)((N + GB_N - 1) / GB_N), (unsigned)((M + GB_M - 1) / GB_M),
               (unsigned)splits);
     k_gemm_bf16_tn<<<grid, 128, GB_SMEM, s>>>(ta, tb, D, M, N, K, ldd, splits,
-                                              (size_t)M * ldd, d_err);
+                                              (size_t)M * ldd, d_err, e);
     return cuda_fail(cudaGetLastError(), "gemm launch");
 }
 
@@ -302,7 +382,7 @@ extern "C" int ndt_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32
     if (e != cudaSuccess) return cuda_fail(e, "gemm error word");
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemsetAsync(err, 0, 4, s);
-    int rc = gemm_bf16_tn(d_a, d_b, d_d, m, n, k, n, err, s, splits);
+    int rc = gemm_bf16_tn(d_a, d_b, d_d, m, n, k, n, err, s, splits, nullptr);
     if (rc) return rc;
     uint32_t h = 0;
     cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, s);

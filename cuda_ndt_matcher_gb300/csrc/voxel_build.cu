@@ -13,16 +13,18 @@
 //   4. segments            : boundary flags + exclusive scan -> segment id / start
 //                            (src/cuda_ffi/csrc/segment_detect.cu:27-146).
 //   5. voxel statistics    : one thread per segment, FP64 two-pass centred moments over the
-//                            segment's points in input order, cyclic-Jacobi eigen
-//                            regularisation to the min-ratio, FP64 inverse, f32 outputs
+//                            segment's points in input order; eigenvector directions by an
+//                            f32 Jacobi, refined in FP64 (orthonormalisation, one or two
+//                            Jacobi sweeps); regularisation to the min-ratio and inverse in
+//                            FP64, f32 outputs
 //                            (Voxel::from_statistics / regularize_covariance,
 //                            src/ndt_cuda/src/voxel_grid/types.rs:54-190).
 //   6. compaction          : valid voxels keep their Morton order.
 //   7. hash insert         : bounded linear probing with atomicCAS, displacement recorded
 //                            (voxel_hash_build_kernel, src/cuda_ffi/csrc/voxel_hash.cu:69-114).
 // This translation unit is compiled with -fmad=false: every FP64/FP32 operation is one IEEE
-// rounding, so the statistics match a CPU evaluation of the same operation sequence bit for
-// bit.
+// rounding, so the moments (counts, means, unregularised covariances) match a CPU evaluation
+// of the same operation sequence bit for bit.
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -510,48 +512,248 @@ struct SegRec {
     uint32_t count;
 };
 
-// Cyclic Jacobi for a symmetric 3x3 in FP64 (same operation sequence as the CPU oracle).
-__device__ void jacobi3(double* a, double* v) {
+// Cyclic Jacobi for a symmetric 3x3 in f32 (row-major a, eigenvectors in the columns of v).
+// It only has to find the eigenvector directions to f32 accuracy: the eigenvalues and the
+// regularised covariance and inverse are then formed in FP64 (k_voxel_stats).
+__device__ void jacobi3f(float* a, float* v) {
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) v[i * 3 + j] = (i == j) ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 32; ++sweep) {
-        double off = 0.0, dg = 0.0;
-        for (int i = 0; i < 3; ++i) {
-            dg += a[i * 3 + i] * a[i * 3 + i];
-            for (int j = i + 1; j < 3; ++j) off += a[i * 3 + j] * a[i * 3 + j];
-        }
-        if (off <= 1e-40 * dg) break;
-        for (int p = 0; p < 2; ++p) {
-            for (int q = p + 1; q < 3; ++q) {
-                double apq = a[p * 3 + q];
-                if (apq == 0.0) continue;
-                double theta = (a[q * 3 + q] - a[p * 3 + p]) / (2.0 * apq);
-                double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
-                if (theta < 0.0) t = -t;
-                double c = 1.0 / sqrt(t * t + 1.0);
-                double s = t * c;
-                a[p * 3 + p] = a[p * 3 + p] - t * apq;
-                a[q * 3 + q] = a[q * 3 + q] + t * apq;
-                a[p * 3 + q] = 0.0;
-                a[q * 3 + p] = 0.0;
-                int r = 3 - p - q;
-                double arp = a[r * 3 + p], arq = a[r * 3 + q];
-                double np = c * arp - s * arq;
-                double nq = s * arp + c * arq;
-                a[r * 3 + p] = np;
-                a[p * 3 + r] = np;
-                a[r * 3 + q] = nq;
-                a[q * 3 + r] = nq;
-                for (int k = 0; k < 3; ++k) {
-                    double vrp = v[k * 3 + p], vrq = v[k * 3 + q];
-                    v[k * 3 + p] = c * vrp - s * vrq;
-                    v[k * 3 + q] = s * vrp + c * vrq;
-                }
+        for (int j = 0; j < 3; ++j) v[i * 3 + j] = (i == j) ? 1.f : 0.f;
+#pragma unroll 1
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        const float off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+        const float dg = a[0] * a[0] + a[4] * a[4] + a[8] * a[8];
+        if (!(off > 1e-14f * dg)) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            const float apq = a[p * 3 + q];
+            if (apq == 0.f) continue;
+            const float theta = (a[q * 3 + q] - a[p * 3 + p]) / (2.f * apq);
+            float t = 1.f / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+            if (theta < 0.f) t = -t;
+            const float c = 1.f / sqrtf(t * t + 1.f);
+            const float sn = t * c;
+            a[p * 3 + p] -= t * apq;
+            a[q * 3 + q] += t * apq;
+            a[p * 3 + q] = a[q * 3 + p] = 0.f;
+            const int r = 3 - p - q;
+            const float arp = a[r * 3 + p], arq = a[r * 3 + q];
+            a[r * 3 + p] = a[p * 3 + r] = c * arp - sn * arq;
+            a[r * 3 + q] = a[q * 3 + r] = sn * arp + c * arq;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float vp = v[k * 3 + p], vq = v[k * 3 + q];
+                v[k * 3 + p] = c * vp - sn * vq;
+                v[k * 3 + q] = sn * vp + c * vq;
             }
         }
     }
 }
 
+// FP64 cyclic Jacobi sweeps on B = V^T A V, rotating V along (B and V row-major, V's columns
+// the eigenvector estimates), until the reference's rule 2 off^2 < 1e-28 diag^2 holds or
+// max_sweeps pass. Started from an orthonormalised f32 solution, B is diagonal to about 1e-7
+// of its scale and one or two sweeps reach FP64 accuracy.
+__device__ void jacobi3_refine(double* B, double* V, int max_sweeps) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        const double off = B[1] * B[1] + B[2] * B[2] + B[5] * B[5];
+        const double dg = B[0] * B[0] + B[4] * B[4] + B[8] * B[8];
+        if (2.0 * off <= 1e-28 * dg) break;
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            const double bpq = B[p * 3 + q];
+            if (bpq == 0.0) continue;
+            const double theta = (B[q * 3 + q] - B[p * 3 + p]) / (2.0 * bpq);
+            double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+            if (theta < 0.0) t = -t;
+            const double c = 1.0 / sqrt(t * t + 1.0);
+            const double sn = t * c;
+            B[p * 3 + p] -= t * bpq;
+            B[q * 3 + q] += t * bpq;
+            B[p * 3 + q] = B[q * 3 + p] = 0.0;
+            const int r = 3 - p - q;
+            const double brp = B[r * 3 + p], brq = B[r * 3 + q];
+            B[r * 3 + p] = B[p * 3 + r] = c * brp - sn * brq;
+            B[r * 3 + q] = B[q * 3 + r] = sn * brp + c * brq;
+            for (int k = 0; k < 3; ++k) {
+                const double vp = V[k * 3 + p], vq = V[k * 3 + q];
+                V[k * 3 + p] = c * vp - sn * vq;
+                V[k * 3 + q] = sn * vp + c * vq;
+            }
+        }
+    }
+}
+
+// FP64 Rayleigh quotient v^T A v / v^T v of an f32 unit vector v (|v|^2 = 1 +- 1e-7, so
+// 1 / v^T v = 2 - v^T v to FP64 rounding): FP64-accurate for an eigenvalue, since its error
+// is quadratic in v's direction error. *w receives 1 / v^T v.
+__device__ __forceinline__ double rayleigh(const double* A, const double* v, double* w) {
+    double num = 0.0;
+    for (int rr = 0; rr < 3; ++rr)
+        num += v[rr] * (A[rr * 3] * v[0] + A[rr * 3 + 1] * v[1] + A[rr * 3 + 2] * v[2]);
+    const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    *w = 2.0 - vv;
+    return num * *w;
+}
+
+// Inverse of a symmetric positive definite 3x3 by its adjugate (FP64); false unless det > 0.
+__device__ __forceinline__ bool inverse_sym3(const double* C, float* icov6) {
+    const double c00 = C[4] * C[8] - C[5] * C[5];
+    const double c01 = C[2] * C[5] - C[1] * C[8];
+    const double c02 = C[1] * C[5] - C[2] * C[4];
+    const double c11 = C[0] * C[8] - C[2] * C[2];
+    const double c12 = C[1] * C[2] - C[0] * C[5];
+    const double c22 = C[0] * C[4] - C[1] * C[1];
+    const double det = C[0] * c00 + C[1] * c01 + C[2] * c02;
+    if (!(det > 0.0)) return false;
+    const double id = 1.0 / det;
+    icov6[0] = (float)(c00 * id);
+    icov6[1] = (float)(c01 * id);
+    icov6[2] = (float)(c02 * id);
+    icov6[3] = (float)(c11 * id);
+    icov6[4] = (float)(c12 * id);
+    icov6[5] = (float)(c22 * id);
+    return true;
+}
+
+// First-order correction of an f32 eigenvector v (eigenvalue lam) against the eigenvectors
+// v_j of the set `others` (bit mask): v += sum_j (v_j^T (A v - lam v)) / (lam - lam_j) v_j
+// (w_j = 1 / v_j^T v_j). The direction error drops from about 1e-7 lambda_max / gap to its
+// square; the 1 / gap factors need only f32 accuracy.
+__device__ __forceinline__ void refine_vector(const double* A, double* v, double lam,
+                                              const double (*vs)[3], const double* lams,
+                                              const double* ws, int others) {
+    double r[3];
+    for (int rr = 0; rr < 3; ++rr)
+        r[rr] = A[rr * 3] * v[0] + A[rr * 3 + 1] * v[1] + A[rr * 3 + 2] * v[2] - lam * v[rr];
+    double dv[3] = {0.0, 0.0, 0.0};
+    for (int j = 0; j < 3; ++j) {
+        if (!(others >> j & 1)) continue;
+        const double proj = vs[j][0] * r[0] + vs[j][1] * r[1] + vs[j][2] * r[2];
+        const double inv = (double)(1.f / (float)(lam - lams[j]));
+        const double c = proj * ws[j] * inv;
+        for (int k = 0; k < 3; ++k) dv[k] += c * vs[j][k];
+    }
+    for (int k = 0; k < 3; ++k) v[k] += dv[k];
+}
+
+// Regularised covariance and inverse of the FP64 covariance A (Voxel::from_statistics /
+// regularize_covariance, src/ndt_cuda/src/voxel_grid/types.rs:54-190): eigenvalues below
+// ratio * lambda_max are raised to it; cov' = V diag(clamped) V^T when any was, else A;
+// inverse V diag(1 / clamped) V^T. a32 / V32: the f32 Jacobi's eigenvalues (diagonal) and
+// eigenvectors (columns). Which eigenvalues clamp is read from the f32 eigenvalues when they
+// lie clear of the threshold (1e-3 relative, against their 1e-5 error there), and the clamped
+// ones lie at least lambda_max / 100 below the others; then, with FP64 Rayleigh quotients as
+// the eigenvalues:
+//   - nothing clamps: cov' = A, inverse by the adjugate (A's condition number <= 1 / ratio);
+//   - one clamps: cov' = A + (thr - lambda_c) v_c v_c^T, v_c refined against the other two;
+//   - two clamp: cov' = thr I + (lambda_u - thr) v_u v_u^T, v_u refined against the other
+//     two (mixing inside the clamped pair then cannot matter);
+//   and the inverse by the adjugate of cov'.
+// Anything else takes the full FP64 route: the f32 eigenvectors orthonormalised
+// (Gram-Schmidt), Jacobi sweeps on V^T A V to the reference's stopping rule, and the
+// reconstruction from the eigen-decomposition. Every route is FP64-accurate, so the f32
+// outputs agree with an FP64 eigen-decomposition to f32 rounding.
+__device__ bool regularize(const double* A, const float* a32, const float* V32, float ratio,
+                           SegRec& r) {
+    const float e32[3] = {a32[0], a32[4], a32[8]};
+    const float mx32 = fmaxf(e32[0], fmaxf(e32[1], e32[2]));
+    bool fast = mx32 > 0.f;
+    int clamp = 0;  // bit i: eigenvalue i clamps
+    if (fast) {
+        const float thr32 = mx32 * ratio;
+        for (int i = 0; i < 3; ++i) {
+            if (e32[i] <= thr32 * 0.999f) {
+                clamp |= 1 << i;
+            } else if (!(e32[i] >= thr32 * 1.001f)) {
+                fast = false;
+            }
+        }
+        for (int i = 0; i < 3 && fast; ++i)
+            for (int j = 0; j < 3; ++j)
+                if ((clamp >> i & 1) && !(clamp >> j & 1) && e32[j] - e32[i] < 0.01f * mx32)
+                    fast = false;
+    }
+    if (fast) {
+        if (!clamp) {
+            for (int q = 0; q < 9; ++q) r.cov[q] = (float)A[q];
+            return inverse_sym3(A, r.icov);
+        }
+        double v[3][3], w[3], lam[3];
+        for (int i = 0; i < 3; ++i) {
+            for (int k = 0; k < 3; ++k) v[i][k] = (double)V32[k * 3 + i];
+            lam[i] = rayleigh(A, v[i], &w[i]);
+        }
+        const double mx = fmax(lam[0], fmax(lam[1], lam[2]));
+        if (!(mx > 0.0)) return false;
+        const double thr = mx * (double)ratio;
+        const int one = __popc(clamp) == 1;
+        const int t = one ? __ffs(clamp) - 1 : __ffs(7 & ~clamp) - 1;  // the vector to refine
+        double u[3] = {v[t][0], v[t][1], v[t][2]};
+        refine_vector(A, u, lam[t], v, lam, w, 7 & ~(1 << t));
+        const double wu = 2.0 - (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        double C[9];
+        const double c = one ? (thr - lam[t]) * wu : (lam[t] - thr) * wu;
+        for (int rr = 0; rr < 3; ++rr)
+            for (int cc = rr; cc < 3; ++cc) {  // upper triangle, mirrored: C stays symmetric
+                const double base = one ? A[rr * 3 + cc] : (rr == cc ? thr : 0.0);
+                C[rr * 3 + cc] = C[cc * 3 + rr] = base + c * u[rr] * u[cc];
+            }
+        for (int q = 0; q < 9; ++q) r.cov[q] = (float)C[q];
+        return inverse_sym3(C, r.icov);
+    }
+    // full FP64 route: orthonormal basis from the f32 eigenvectors, Jacobi sweeps on V^T A V
+    double V[9];
+    for (int q = 0; q < 9; ++q) V[q] = (double)V32[q];
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < i; ++j) {
+            const double d = V[i] * V[j] + V[3 + i] * V[3 + j] + V[6 + i] * V[6 + j];
+            for (int k = 0; k < 3; ++k) V[k * 3 + i] -= d * V[k * 3 + j];
+        }
+        const double inv = 1.0 / sqrt(V[i] * V[i] + V[3 + i] * V[3 + i] + V[6 + i] * V[6 + i]);
+        for (int k = 0; k < 3; ++k) V[k * 3 + i] *= inv;
+    }
+    double AV[9], B[9];
+    for (int rr = 0; rr < 3; ++rr)
+        for (int cc = 0; cc < 3; ++cc)
+            AV[rr * 3 + cc] =
+                A[rr * 3] * V[cc] + A[rr * 3 + 1] * V[3 + cc] + A[rr * 3 + 2] * V[6 + cc];
+    for (int rr = 0; rr < 3; ++rr)
+        for (int cc = rr; cc < 3; ++cc)
+            B[rr * 3 + cc] = B[cc * 3 + rr] =
+                V[rr] * AV[cc] + V[3 + rr] * AV[3 + cc] + V[6 + rr] * AV[6 + cc];
+    jacobi3_refine(B, V, 4);
+    const double ev[3] = {B[0], B[4], B[8]};
+    const double mx = fmax(ev[0], fmax(ev[1], ev[2]));
+    if (!(mx > 0.0)) return false;
+    const double thr = mx * (double)ratio;
+    int needs = 0;
+    double cl[3], icl[3];
+    for (int i = 0; i < 3; ++i) {
+        cl[i] = ev[i] < thr ? thr : ev[i];
+        if (ev[i] < thr) needs = 1;
+        icl[i] = 1.0 / cl[i];
+    }
+    for (int rr = 0; rr < 3; ++rr)
+        for (int cc = rr; cc < 3; ++cc) {
+            double sr = 0.0, si = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                const double vv = V[rr * 3 + k] * V[cc * 3 + k];
+                sr += vv * cl[k];
+                si += vv * icl[k];
+            }
+            const float fc = (float)(needs ? sr : A[rr * 3 + cc]);
+            r.cov[rr * 3 + cc] = r.cov[cc * 3 + rr] = fc;
+            r.icov[rr == 0 ? cc : (rr == 1 ? 2 + cc : 5)] = (float)si;
+        }
+    return true;
+}
+
+// Voxel statistics, one thread per segment: FP64 centred two-pass moments over the
+// segment's points in input order (count, mean, covariance / (n - 1)), then the regularised
+// covariance and its inverse (regularize). GB300's FP64 rate is a small fraction of its FP32
+// rate: the eigenvector directions come from an f32 Jacobi, and FP64 is spent only where the
+// outputs depend on it.
 __global__ void __launch_bounds__(128) k_voxel_stats(
     const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
     const uint32_t* __restrict__ starts, const uint32_t* __restrict__ num_seg, uint32_t nf,
@@ -582,54 +784,35 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
             sum[1] += (double)p[1];
             sum[2] += (double)p[2];
         }
-        double nn = (double)cnt;
-        double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
-        double sq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const double nn = (double)cnt;
+        const double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
+        // upper triangle xx, xy, xz, yy, yz, zz (the products are symmetric bit for bit)
+        double sq[6] = {0, 0, 0, 0, 0, 0};
         for (uint32_t k = b; k < e; ++k) {
             const float* p = pts + 3 * (size_t)sidx[k];
-            double d[3] = {(double)p[0] - mean[0], (double)p[1] - mean[1],
-                           (double)p[2] - mean[2]};
-            for (int rr = 0; rr < 3; ++rr)
-                for (int cc = 0; cc < 3; ++cc) sq[rr * 3 + cc] += d[rr] * d[cc];
+            const double d0 = (double)p[0] - mean[0], d1 = (double)p[1] - mean[1],
+                         d2 = (double)p[2] - mean[2];
+            sq[0] += d0 * d0;
+            sq[1] += d0 * d1;
+            sq[2] += d0 * d2;
+            sq[3] += d1 * d1;
+            sq[4] += d1 * d2;
+            sq[5] += d2 * d2;
         }
-        double cov[9];
-        for (int q = 0; q < 9; ++q) cov[q] = sq[q] / (nn - 1.0);
-        double a[9], V[9], ev[3];
-        for (int q = 0; q < 9; ++q) a[q] = cov[q];
-        jacobi3(a, V);
-        for (int i = 0; i < 3; ++i) ev[i] = a[i * 3 + i];
-        double mx = 0.0;
-        for (int i = 0; i < 3; ++i) mx = fmax(mx, ev[i]);
-        if (mx > 0.0) {
-            double thr = mx * (double)ratio;
-            int needs = 0;
-            double cl[3];
-            for (int i = 0; i < 3; ++i) {
-                cl[i] = ev[i] < thr ? thr : ev[i];
-                if (ev[i] < thr) needs = 1;
-            }
-            double rc[9], ic[9];
-            for (int rr = 0; rr < 3; ++rr) {
-                for (int cc = rr; cc < 3; ++cc) {
-                    double sr = 0.0, si = 0.0;
-                    for (int k = 0; k < 3; ++k) {
-                        sr += V[rr * 3 + k] * cl[k] * V[cc * 3 + k];
-                        si += V[rr * 3 + k] * (1.0 / cl[k]) * V[cc * 3 + k];
-                    }
-                    rc[rr * 3 + cc] = rc[cc * 3 + rr] = sr;
-                    ic[rr * 3 + cc] = ic[cc * 3 + rr] = si;
-                }
-            }
-            for (int q = 0; q < 9; ++q) r.cov[q] = (float)(needs ? rc[q] : cov[q]);
-            r.icov[0] = (float)ic[0];
-            r.icov[1] = (float)ic[1];
-            r.icov[2] = (float)ic[2];
-            r.icov[3] = (float)ic[4];
-            r.icov[4] = (float)ic[5];
-            r.icov[5] = (float)ic[8];
+        const double nm1 = nn - 1.0;
+        double A[9];
+        A[0] = sq[0] / nm1;
+        A[1] = A[3] = sq[1] / nm1;
+        A[2] = A[6] = sq[2] / nm1;
+        A[4] = sq[3] / nm1;
+        A[5] = A[7] = sq[4] / nm1;
+        A[8] = sq[5] / nm1;
+        float a32[9], V32[9];
+        for (int q = 0; q < 9; ++q) a32[q] = (float)A[q];
+        jacobi3f(a32, V32);
+        ok = regularize(A, a32, V32, ratio, r) ? 1u : 0u;
+        if (ok)
             for (int q = 0; q < 3; ++q) r.mean[q] = (float)mean[q];
-            ok = 1;
-        }
     }
     if (ok) rec[s] = r;
     valid[s] = ok;

@@ -150,6 +150,10 @@ typedef struct ndt_stats {
     uint64_t cycles_control;       /* FP64 reduction, Hessian assembly, 6x6 solve, step */
     uint64_t cycles_broadcast;     /* pose broadcast barrier */
     uint64_t eigen_solves;         /* iterations whose Hessian took the eigen path */
+    /* learned initial-pose search: forward passes of the proposal network and their
+     * CUDA-event time (features, GEMMs, decode) on the network's stream */
+    uint64_t proposal_launches;
+    double proposal_kernel_ms;
 } ndt_stats;
 
 typedef struct ndt_ctx ndt_ctx;
@@ -353,6 +357,17 @@ int ndt_pnet_add_scan(ndt_pnet* net, int32_t map_id, const float* xyz, uint64_t 
                       const double pose[6], int32_t* scan_id);
 /* `steps` Adam steps of `batch` freshly perturbed samples; loss_out (optional) per step. */
 int ndt_pnet_train(ndt_pnet* net, uint64_t steps, float* loss_out);
+/* Counters of a network since creation: inference_kernel_ms is the CUDA-event time of the
+ * device work of ndt_pnet_propose (feature build, every layer's GEMM and activation, decode;
+ * not the query upload), train_ms that of ndt_pnet_train. */
+typedef struct ndt_pnet_stats {
+    uint64_t inference_batches;    /* forward passes (one per `batch` queries) */
+    uint64_t queries;
+    double inference_kernel_ms;
+    uint64_t train_steps;
+    double train_ms;
+} ndt_pnet_stats;
+int ndt_pnet_stats_get(ndt_pnet* net, ndt_pnet_stats* out);
 /* Candidate poses of each query (its ndt_scan's initial_pose is the coarse pose):
  * poses num_queries * proposals * 6, logits num_queries * proposals (optional). */
 int ndt_pnet_propose(ndt_pnet* net, int32_t map_id, const ndt_scan* queries,

@@ -4,7 +4,7 @@ Hessian along a trajectory."""
 import numpy as np
 
 # per-iteration bars: the next iterate from the same start pose
-STEP_POS, STEP_ROT, STEP_REL = 1e-6, 1e-7, 1e-6
+STEP_POS, STEP_ROT, STEP_REL = 1e-6, 1e-6, 1e-6
 # an iterate whose point-voxel pair set differs (FP32 against FP64 radius test)
 BOUNDARY_POS, BOUNDARY_ROT = 1e-4, 1e-5
 
@@ -53,3 +53,15 @@ def trajectory_has_indefinite_hessian(grid, scan, pose, semantics="gpu"):
         if ev.max() >= 0.0:
             return True
     return False
+
+
+def matrix_ulps(a, b):
+    """Per row (one 3x3 matrix per row, 9 entries), the largest entry difference in units of
+    the f32 spacing at that matrix's largest entry: the f32-ULP error of a matrix relative to
+    its norm (an entry near zero gets no tighter bar than the matrix's scale)."""
+    a = np.asarray(a, np.float64).reshape(len(a), -1)
+    b = np.asarray(b, np.float64).reshape(len(b), -1)
+    scale = np.maximum(np.abs(a).max(axis=1), np.abs(b).max(axis=1))
+    spacing = np.spacing(scale.astype(np.float32)).astype(np.float64)
+    spacing[spacing == 0] = np.finfo(np.float32).tiny
+    return np.abs(a - b).max(axis=1) / spacing

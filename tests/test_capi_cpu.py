@@ -41,6 +41,8 @@ def test_struct_layouts():
     assert C.sizeof(capi.Scan) == 8 + 8 + 48
     assert C.sizeof(capi.ParticleConfig) == 4 + 4 + 4 * 8 + 8
     assert C.sizeof(capi.PoseEstimate) == 12 * 8 + 3 * 8 + 4 * 4
+    assert C.sizeof(capi.Stats) == 19 * 8
+    assert C.sizeof(capi.PNetStats) == 5 * 8
 
 
 def test_config_defaults_mirror_reference():

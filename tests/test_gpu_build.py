@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from cuda_ndt_matcher_gb300 import capi, synth
+from parity_helpers import matrix_ulps
 
 pytestmark = pytest.mark.gpu
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
@@ -158,8 +159,14 @@ def test_map_build_matches_oracle(gpu, oracle, name):
     assert np.array_equal(coords, g.coords)            # membership and Morton order
     assert np.array_equal(counts, g.counts)            # per-voxel counts
     assert np.array_equal(means, g.means)              # FP64 sums in input order
-    assert np.array_equal(covs, g.covs)                # same FP64 operation sequence
-    assert np.array_equal(icovs, g.icovs)
+    # regularised covariance and inverse: the library forms them in FP64 from f32 eigenvector
+    # directions (Rayleigh quotients, rank-one clamp, adjugate inverse), the oracle from an
+    # FP64 Jacobi; both are FP64-accurate, so they agree to f32 rounding
+    cu, iu = matrix_ulps(covs, g.covs), matrix_ulps(icovs, g.icovs)
+    print(f"{name}: {len(coords)} voxels, covariance max {cu.max():.1f} f32 ULP "
+          f"({(cu > 0).sum()} differ), inverse max {iu.max():.1f} f32 ULP ({(iu > 0).sum()} "
+          f"differ)")
+    assert cu.max() <= 2 and iu.max() <= 4, (cu.max(), iu.max())
     # the reference's uncentred FP64 formula differs only in the last f32 bits
     r = oracle.Grid(pts, 2.0, centered=False)
     assert np.array_equal(coords, r.coords) and np.array_equal(counts, r.counts)
