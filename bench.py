@@ -279,8 +279,9 @@ def learned_bench(steps=20000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
     labels are plain NDT's converged poses; perturbations x, y U(+-5 m), yaw uniform, drawn on
     the device (steps x 256 samples). Evaluation: n_test held-out scans per map, coarse poses
     x, y U(+-5 m) with an unknown heading. Plain = 200 particles over the same range;
-    learned = 16 proposals refined by NDT; learned + fallback = the plain search where the
-    best NVTL is below 2.3.
+    learned = 16 proposals refined by NDT; refine8 = then 8 particles (x, y +- 0.5 m, yaw +-
+    5 deg) around each query's winner, aligned as a second round; fallback = the plain
+    search where the best NVTL is below 2.3 (fallback29: below 2.9).
     - success: error < 0.2 m and < 1 deg against the true pose;
     - judged success (plain NDT as judge): a learned result counts only if it succeeds and
       its converged NVTL matches the plain search's on the same query (within nvtl_tol
@@ -312,7 +313,8 @@ def learned_bench(steps=20000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
     pairs = list(zip(dims[:-1], dims[1:]))
     flops_step = 2 * cfg.batch * (2 * sum(i * o for i, o in pairs) + sum(i * o for i, o in pairs[1:]))
     rng = np.random.default_rng(99)
-    names = ("plain_200", "learned_16", "learned_16_fallback")
+    names = ("plain_200", "learned_16", "learned_16_refine8", "learned_16_refine8_fallback",
+             "learned_16_refine8_fallback29")
     out = {k: {"ok": 0, "judged": 0, "nvtl_match": 0, "gpu_ms": 0.0, "net_ms": 0.0,
                "wall_s": 0.0, "fallbacks": 0} for k in names}
     n = 0
@@ -325,13 +327,19 @@ def learned_bench(steps=20000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
             c[5] = rng.uniform(-np.pi, np.pi)
             coarse.append(c)
         fb = []
+        plain_cfg = dict(num_particles=200, xy_range=5.0, yaw_range=np.pi, seed=3)
+        refine = dict(num_particles=8, xy_range=0.5, yaw_range=np.radians(5.0), seed=5)
         runs = {
-            "plain_200": lambda: ctx.initial_pose_search(m.test_scans, coarse, num_particles=200,
-                                                         xy_range=5.0, yaw_range=np.pi, seed=3),
+            "plain_200": lambda: ctx.initial_pose_search(m.test_scans, coarse, **plain_cfg),
             "learned_16": lambda: ctx.learned_pose_search(net, mid, m.test_scans, coarse),
-            "learned_16_fallback": lambda: ctx.learned_pose_search(
-                net, mid, m.test_scans, coarse, nvtl_threshold=2.3,
-                fallback=dict(num_particles=200, xy_range=5.0, yaw_range=np.pi, seed=3))}
+            "learned_16_refine8": lambda: ctx.learned_pose_search(
+                net, mid, m.test_scans, coarse, refine=refine),
+            "learned_16_refine8_fallback": lambda: ctx.learned_pose_search(
+                net, mid, m.test_scans, coarse, refine=refine, nvtl_threshold=2.3,
+                fallback=plain_cfg),
+            "learned_16_refine8_fallback29": lambda: ctx.learned_pose_search(
+                net, mid, m.test_scans, coarse, refine=refine, nvtl_threshold=2.9,
+                fallback=plain_cfg)}
         plain = None
         for name in names:
             ctx.stats_reset()
@@ -387,10 +395,11 @@ def learned_bench(steps=20000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
 
 def tile_stream_bench(pts, scans, guesses, events=40):
     """Tiles of 100 x 100 m streamed over the large map at 2 m: a 5 x 5 tile window slides
-    east one tile column at a time. Each event uploads one tile, drops the one leaving the
-    window and commits a background rebuild, while a batch of dense scans is aligned on the
-    current map. Reported: rebuild time per commit (device), wall time per event (upload +
-    commit + aligning the batch + waiting for the rebuild) and the tile rate that wall time
+    east one tile column at a time. Each event puts one tile (upload + its cells' statistics),
+    drops the one leaving the window and commits a background merge of the resident tiles'
+    cells, while a batch of dense scans is aligned on the current map. Reported: device time
+    per event (the put's cell statistics + the merge), wall time per event (upload, put,
+    commit, aligning the batch, waiting for the merge) and the tile rate that wall time
     sustains."""
     from cuda_ndt_matcher_gb300 import capi
     tx = np.floor(pts[:, 0] / 100.0).astype(np.int64)
@@ -405,24 +414,34 @@ def tile_stream_bench(pts, scans, guesses, events=40):
         ctx.tile_put((i + 10) * 32 + (j + 10), tile(i, j))
     ctx.tiles_commit(wait=True)
     ev = [(i, j) for i in range(-2, -2 + events // 5 + 1) for j in range(-2, 3)][:events]
-    build_ms, wall = [], []
+    build_ms, put_ms, wall = [], [], []
     for k, (i, j) in enumerate(ev):
         t0 = time.perf_counter()
         ctx.tile_put((i + 10) * 32 + (j + 10), tile(i, j))
+        put_ms.append(ctx.tiles_status()["put_ms"])
         old = (i - 5, j)
         ctx.tile_remove((old[0] + 10) * 32 + (old[1] + 10))
         ctx.tiles_commit(wait=False)
         ctx.align_batch(scans, guesses)        # alignment continues on the current map
         while ctx.tiles_status()["pending"]:
             time.sleep(0.0002)
-        ctx.map_info()                         # switch to the rebuilt map
+        ctx.map_info()                         # switch to the merged map
         wall.append(time.perf_counter() - t0)
         build_ms.append(ctx.tiles_status()["build_ms"])
     st = ctx.tiles_status()
+    # the same window rebuilt from all its points at once, for comparison
+    full = capi.Context(resolution=2.0)
+    win = np.concatenate([tile(i, j) for (i, j) in ev[-25:]])
+    full.set_target(win)
+    full.set_target(win)
+    full_ms = float(full.map_info().build_ms)
+    full.close()
     ctx.close()
     return {"tile_m": 100, "window_tiles": 25, "points_in_window": int(st["points"]),
-            "events": len(ev), "rebuild_ms_mean": float(np.mean(build_ms)),
-            "rebuild_ms_max": float(np.max(build_ms)),
+            "events": len(ev), "put_cell_stats_ms_mean": float(np.mean(put_ms)),
+            "merge_ms_mean": float(np.mean(build_ms)), "merge_ms_max": float(np.max(build_ms)),
+            "device_ms_per_event": float(np.mean(put_ms) + np.mean(build_ms)),
+            "full_window_rebuild_ms": full_ms,
             "event_wall_ms_mean": float(np.mean(wall) * 1e3),
             "sustained_tiles_per_s": float(1.0 / np.mean(wall)),
             "aligned_per_event": len(scans)}
@@ -508,6 +527,11 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
             "sampled": len(pick),
             "fp32_vs_fp64_cov_rel_err_max": fp32_err,
             "dense_scan_aligns_per_s": len(scans) / (st["align_kernel_ms"] / 1e3),
+            "dense_scan_iterations_per_align": st["iterations"] / max(st["alignments"], 1),
+            "dense_scan_pairs_per_point_iter": st["correspondences"] /
+            max(st["point_iterations"], 1),
+            "dense_scan_kernel_us_per_point_iter": st["align_kernel_ms"] * 1e3 /
+            max(st["point_iterations"], 1),
             "dense_scan_e2e_aligns_per_s": len(scans) / wall,
             "dense_scan_median_err_m": float(np.median(err))}
         ctx.close()
@@ -902,7 +926,7 @@ def run_ours(args):
 
 def run_only(names, args):
     """The named extra workloads alone (comma-separated: init_pose, queue, learned,
-    large_map)."""
+    large_map, tiles)."""
     out = {}
     for nm in names.split(","):
         if nm == "init_pose":
@@ -913,6 +937,18 @@ def run_only(names, args):
             out["learned_init_pose"] = learned_bench()
         elif nm == "large_map":
             out["large_map"] = large_map_bench()
+        elif nm == "tiles":
+            from cuda_ndt_matcher_gb300 import synth
+            pts = synth.large_map(seed=7, extent=2000.0, n_points=50_000_000)
+            rng = np.random.default_rng(11)
+            scans, guesses = [], []
+            for i in range(16):
+                p = np.array([rng.uniform(-800, 800), rng.uniform(-800, 800), 1.8, 0, 0,
+                              rng.uniform(-np.pi, np.pi)])
+                near = pts[(np.abs(pts[:, 0] - p[0]) < 61) & (np.abs(pts[:, 1] - p[1]) < 61)]
+                scans.append(synth.crop_scan(near, p, 100_000, seed=i))
+                guesses.append(p)
+            out["tile_streaming"] = tile_stream_bench(pts, scans, guesses)
         else:
             raise SystemExit(f"unknown workload {nm}")
     return out

@@ -35,7 +35,8 @@ EXPORTS = [
     "ndt_pnet_debug_grad", "ndt_pnet_params", "ndt_pnet_stats_get", "ndt_learned_pose_search",
     "ndt_gemm_bf16",
     "ndt_neighbors_query", "ndt_stats_get", "ndt_stats_reset",
-    "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_last_error_string",
+    "ndt_profile_enable", "ndt_debug_trace", "ndt_debug_read", "ndt_debug_queue_stall",
+    "ndt_last_error_string",
     "ndt_radix_sort_pairs_u64_u32", "ndt_radix_sort_pairs_u64_u32_static",
     "ndt_detect_segments", "ndt_morton_codes",
 ]
@@ -164,7 +165,7 @@ def load(build_if_missing=True):
         "ndt_tiles_commit": (C.c_int, [P, C.c_int32]),
         "ndt_tiles_status": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32),
-                                       C.POINTER(C.c_float)]),
+                                       C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "ndt_map_voxels": (C.c_int, [P, P, P, P, P, P, C.c_uint64]),
         "ndt_align": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(Result)]),
         "ndt_align_multi_pose": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
@@ -187,7 +188,8 @@ def load(build_if_missing=True):
         "ndt_pnet_debug_grad": (C.c_int, [P, P, P, C.c_uint64, P, P]),
         "ndt_pnet_params": (C.c_int, [P, P, C.POINTER(C.c_uint64), C.c_int32]),
         "ndt_pnet_stats_get": (C.c_int, [P, C.POINTER(PNetStats)]),
-        "ndt_learned_pose_search": (C.c_int, [P, P, C.c_int32, P, C.c_uint64, C.c_double,
+        "ndt_learned_pose_search": (C.c_int, [P, P, C.c_int32, P, C.c_uint64,
+                                              C.POINTER(ParticleConfig), C.c_double,
                                               C.POINTER(ParticleConfig), P, P]),
         "ndt_gemm_bf16": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
         "ndt_initial_pose_search": (C.c_int, [P, P, C.c_uint64, C.POINTER(ParticleConfig),
@@ -196,6 +198,7 @@ def load(build_if_missing=True):
                                       C.c_uint64, P]),
         "ndt_neighbors_query": (C.c_int, [P, P, C.c_uint64, C.c_int32, P, P]),
         "ndt_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
+        "ndt_debug_queue_stall": (C.c_int, [P, C.c_uint64, C.c_int32]),
         "ndt_stats_reset": (C.c_int, [P]),
         "ndt_profile_enable": (C.c_int, [P, C.c_int]),
         "ndt_debug_trace": (C.c_int, [P, C.c_int]),
@@ -316,11 +319,11 @@ class Context:
 
     def tiles_status(self):
         nt, npnt = C.c_uint64(), C.c_uint64()
-        pend, rc, ms = C.c_int32(), C.c_int32(), C.c_float()
+        pend, rc, ms, put = C.c_int32(), C.c_int32(), C.c_float(), C.c_float()
         check(self.lib.ndt_tiles_status(self.h, C.byref(nt), C.byref(npnt), C.byref(pend),
-                                        C.byref(rc), C.byref(ms)))
+                                        C.byref(rc), C.byref(ms), C.byref(put)))
         return {"tiles": nt.value, "points": npnt.value, "pending": bool(pend.value),
-                "last_rc": rc.value, "build_ms": ms.value}
+                "last_rc": rc.value, "build_ms": ms.value, "put_ms": put.value}
 
     def set_target_device(self, ptr, n):
         check(self.lib.ndt_set_target_device(self.h, ptr, n))
@@ -470,6 +473,11 @@ class Context:
                                            idx.ctypes.data, cnt.ctypes.data))
         return idx, cnt
 
+    def debug_queue_stall(self, limit_ns, withhold_next=False):
+        """Test hook: the work-queue kernel's no-progress limit, and (withhold_next) a next
+        launch whose chunks all start out claimed, so the limit runs out."""
+        check(self.lib.ndt_debug_queue_stall(self.h, int(limit_ns), 1 if withhold_next else 0))
+
     def trace(self, enable=True):
         check(self.lib.ndt_debug_trace(self.h, 1 if enable else 0))
 
@@ -488,9 +496,16 @@ class Context:
         check(self.lib.ndt_stats_reset(self.h))
 
     def learned_pose_search(self, net, map_id, queries, coarse, nvtl_threshold=2.3,
-                            fallback=None):
-        """Proposal network + NDT refinement (+ plain particle search below the NVTL
-        threshold when `fallback` is a dict of initial_pose_search particle settings)."""
+                            fallback=None, refine=None):
+        """Proposal network + NDT refinement; `refine` (a dict of particle settings: particles
+        around each query's best proposal result, aligned as a second round); plain particle
+        search below the NVTL threshold when `fallback` is a dict of initial_pose_search
+        particle settings."""
+        def pcfg(d):
+            f = dict(num_particles=200, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0,
+                     roll_pitch_sigma=0.0, seed=0)
+            f.update(d)
+            return ParticleConfig(**f)
         qs = [as_xyz(q) for q in queries]
         m = len(qs)
         arr = (Scan * m)()
@@ -499,15 +514,13 @@ class Context:
             arr[i].num_points = len(s)
             for k in range(6):
                 arr[i].initial_pose[k] = float(pose[k])
-        pc = None
-        if fallback is not None:
-            f = dict(num_particles=200, xy_range=2.0, yaw_range=np.pi, z_sigma=0.0,
-                     roll_pitch_sigma=0.0, seed=0)
-            f.update(fallback)
-            pc = ParticleConfig(**f)
+        pc = pcfg(fallback) if fallback is not None else None
+        rf = pcfg(refine) if refine is not None else None
         est = (PoseEstimate * m)()
         used = np.zeros(m, np.int32)
-        check(self.lib.ndt_learned_pose_search(self.h, net.h, map_id, arr, m, nvtl_threshold,
+        check(self.lib.ndt_learned_pose_search(self.h, net.h, map_id, arr, m,
+                                               C.byref(rf) if rf is not None else None,
+                                               nvtl_threshold,
                                                C.byref(pc) if pc is not None else None, est,
                                                used.ctypes.data))
         return [{"pose": np.array(e.pose), "initial_pose": np.array(e.initial_pose),

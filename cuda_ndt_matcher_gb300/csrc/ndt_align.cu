@@ -1658,7 +1658,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
 // incremented; the controller, after the increment that completes the iteration, fences and
 // sums the partials in chunk order, so results do not depend on which CTA ran which chunk.
 // No CTA ever waits for another; a CTA that finds nothing to claim polls, and gives up with a
-// status bit after 2 s without work (every alignment ends within max_iterations steps).
+// status bit after P.stall_ns (2 s) without work (every alignment ends within max_iterations
+// steps).
 // Host batches may still be copying in when the kernel starts (P.qarrive): the points are laid
 // out largest alignment first, in copy chunks that start on 768-byte boundaries, and a copy
 // stream writes the count of resident points after each chunk. An alignment's first
@@ -1727,7 +1728,9 @@ __global__ void __launch_bounds__(128) k_queue_init(const AlignParams P) {
         q->point_iters = q->corr_total = 0;
         q->cyc_chunks = q->cyc_ctl = 0;
         q->t_start = 0;
-        P.qjobs[j].gen_claim = qword(0u, queue_chunks(P, job.n, 0u));
+        const uint32_t nch0 = queue_chunks(P, job.n, 0u);
+        // withhold (test hook): every chunk of the first iteration already claimed
+        P.qjobs[j].gen_claim = qword(0u, nch0) | (P.withhold ? (unsigned long long)nch0 : 0ull);
         P.qjobs[j].done = 0u;
     }
 }
@@ -2039,7 +2042,7 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                         idle_since = now;
                     } else if (!fed && now - idle_since > QSTARVE_NS) {
                         stop = 1;  // starved of input: the continuation launch finishes
-                    } else if (now - idle_since > 2000000000ull) {
+                    } else if (now - idle_since > P.stall_ns) {
                         atomicOr(P.status, ST_QUEUE_STALL);
                         stop = 1;
                     } else if (fed && blockIdx.x >= gridDim.x / 4u &&

@@ -233,11 +233,18 @@ struct ndt_ctx {
         uint64_t id;
         DevBuf pts;
         uint64_t n;
+        TileSegs segs;           // the tile's segments (built on put)
+        float seg_res = 0.f;     // map parameters the segments were built with
+        int32_t seg_min = 0;
+        float seg_ratio = 0.f;
     };
     std::vector<Tile> tiles;
     Map map_b;
-    BuildScratch bs_b;
-    DevBuf d_gather, d_status_b;
+    BuildScratch bs_b, bs_tile;
+    DevBuf d_gather, d_status_b, d_tile_refs;
+    float tile_put_ms = 0.f;     // device time of the last put's segment build
+    uint64_t stall_ns = QSTALL_NS;  // work-queue no-progress limit (ndt_debug_queue_stall)
+    int32_t withhold_next = 0;
     cudaStream_t bstream = nullptr;
     std::thread builder;
     std::atomic<int> build_state{0};  // 0 idle, 1 running, 2 finished
@@ -362,7 +369,8 @@ static int check_status(ndt_ctx* c, uint32_t st) {
         return NDT_ERR_PROBE_LIMIT;
     }
     if (st & ST_QUEUE_STALL) {
-        set_error("work-queue Newton kernel found no work for 2 s with alignments open");
+        set_error("work-queue Newton kernel found no work for " +
+                  std::to_string(c->stall_ns / 1000000ull) + " ms with alignments open");
         return NDT_ERR_DEVICE;
     }
     set_error("device reported status " + std::to_string(st));
@@ -482,7 +490,14 @@ int ndt_ctx_destroy(ndt_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->cstream) cudaStreamSynchronize(c->cstream);
     if (c->builder.joinable()) c->builder.join();
-    for (auto& t : c->tiles) dev_free(t.pts);
+    for (auto& t : c->tiles)
+        for (DevBuf* b : {&t.pts, &t.segs.idx, &t.segs.starts, &t.segs.rec, &t.segs.valid})
+            dev_free(*b);
+    for (DevBuf* b : {&c->bs_tile.keys_a, &c->bs_tile.keys_b, &c->bs_tile.vals_a,
+                      &c->bs_tile.vals_b, &c->bs_tile.tmp, &c->bs_tile.seg_ids,
+                      &c->bs_tile.seg_starts, &c->bs_tile.seg_valid, &c->bs_tile.seg_rank,
+                      &c->bs_tile.seg_rec, &c->bs_tile.small, &c->d_tile_refs})
+        dev_free(*b);
     for (DevBuf* b : {&c->map_b.slots, &c->map_b.slot_icov, &c->map_b.slot_vidx, &c->map_b.grid,
                       &c->map_b.nmask,
                       &c->map_b.vox_coord, &c->map_b.vox_mean, &c->map_b.vox_cov,
@@ -538,6 +553,14 @@ int ndt_ctx_configure(ndt_ctx* c, const ndt_config* cfg) {
 int ndt_profile_enable(ndt_ctx* c, int enable) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
     c->profile = enable != 0;
+    return NDT_OK;
+}
+
+int ndt_debug_queue_stall(ndt_ctx* c, uint64_t limit_ns, int32_t withhold_next) {
+    if (!c || (withhold_next != 0 && withhold_next != 1)) return NDT_ERR_INVALID_ARGUMENT;
+    c->stall_ns = limit_ns ? limit_ns : QSTALL_NS;
+    c->withhold_next = withhold_next;
+    c->cfg_gen++;  // captured batches bake the limit in
     return NDT_OK;
 }
 
@@ -627,35 +650,59 @@ int ndt_set_target_device(ndt_ctx* c, const float* d_xyz, uint64_t n) {
     return set_target_dev(c, d_xyz, n);
 }
 
+// Builds a tile's segments (cells, counts, FP64 statistics) with the context's current map
+// parameters, on the tile stream.
+static int tile_segments(ndt_ctx* c, ndt_ctx::Tile& t) {
+    float ms = 0.f;
+    const int rc = build_tile_segments(c->bs_tile, (const float*)t.pts.p, (size_t)t.n, c->cfg,
+                                       c->bstream, t.segs, &ms);
+    if (rc) return rc;
+    t.seg_res = c->cfg.resolution;
+    t.seg_min = c->cfg.min_points_per_voxel;
+    t.seg_ratio = c->cfg.eigenvalue_ratio;
+    c->tile_put_ms = ms;
+    c->stats.build_ms += ms;
+    return 0;
+}
+
 int ndt_tile_put(ndt_ctx* c, uint64_t tile_id, const float* xyz, uint64_t n) {
     if (!c || (!xyz && n)) return NDT_ERR_INVALID_ARGUMENT;
     if (n == 0) {
         set_error("Target point cloud is empty");
         return NDT_ERR_EMPTY_INPUT;
     }
+    if (n >= 0xFFFFFFF0ull) {
+        set_error("a tile holds fewer than 2^32 points");
+        return NDT_ERR_CAPACITY;
+    }
     cudaSetDevice(c->device);
     ndt_ctx::Tile* t = nullptr;
     for (auto& x : c->tiles)
         if (x.id == tile_id) t = &x;
-    if (!t) {
-        c->tiles.push_back(ndt_ctx::Tile{tile_id, DevBuf{}, 0});
+    if (t) {
+        tiles_settle(c, true);  // a running merge reads this tile's buffers
+    } else {
+        c->tiles.push_back(ndt_ctx::Tile{});
         t = &c->tiles.back();
+        t->id = tile_id;
     }
     int rc = dev_reserve(t->pts, n * 12);
     if (rc) return rc;
     t->n = n;
     cudaMemcpyAsync(t->pts.p, xyz, n * 12, cudaMemcpyHostToDevice, c->bstream);
     c->stats.h2d_bytes += n * 12;
-    return cuda_fail(cudaStreamSynchronize(c->bstream), "tile upload");
+    if ((rc = cuda_fail(cudaStreamSynchronize(c->bstream), "tile upload"))) return rc;
+    return tile_segments(c, *t);
 }
 
 int ndt_tile_remove(ndt_ctx* c, uint64_t tile_id) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
     for (size_t i = 0; i < c->tiles.size(); ++i)
         if (c->tiles[i].id == tile_id) {
-            // a running rebuild has already gathered its points: the buffer can go
-            tiles_settle(c, true);
-            dev_free(c->tiles[i].pts);
+            tiles_settle(c, true);  // a running merge reads the tile's buffers
+            ndt_ctx::Tile& t = c->tiles[i];
+            for (DevBuf* b : {&t.pts, &t.segs.idx, &t.segs.starts, &t.segs.rec, &t.segs.valid})
+                dev_free(*b);
             c->tiles.erase(c->tiles.begin() + (long)i);
             return NDT_OK;
         }
@@ -674,21 +721,38 @@ int ndt_tiles_commit(ndt_ctx* c, int32_t wait) {
         return NDT_ERR_EMPTY_INPUT;
     }
     cudaSetDevice(c->device);
-    int rc = dev_reserve(c->d_gather, total * 12);
-    if (rc) return rc;
+    int rc;
+    // tiles whose segments were built with other map parameters are rebuilt first
+    for (auto& t : c->tiles)
+        if (t.seg_res != c->cfg.resolution || t.seg_min != c->cfg.min_points_per_voxel ||
+            t.seg_ratio != c->cfg.eigenvalue_ratio)
+            if ((rc = tile_segments(c, t))) return rc;
+    std::vector<TileSegRef> refs;
     uint64_t off = 0;
-    for (auto& t : c->tiles) {  // device-side gather of the resident tiles, in put order
-        cudaMemcpyAsync((char*)c->d_gather.p + off * 12, t.pts.p, t.n * 12,
-                        cudaMemcpyDeviceToDevice, c->bstream);
-        off += t.n;
+    for (auto& t : c->tiles) {
+        TileSegRef r{};
+        r.rec = (const SegRec*)t.segs.rec.p;
+        r.valid = (const uint32_t*)t.segs.valid.p;
+        r.starts = (const uint32_t*)t.segs.starts.p;
+        r.idx = (const uint32_t*)t.segs.idx.p;
+        r.pts = (const float*)t.pts.p;
+        r.seg_off = off;
+        r.S = t.segs.geo.S;
+        r.nf = (uint32_t)t.segs.geo.nf;
+        for (int a = 0; a < 3; ++a) {
+            r.mn[a] = t.segs.geo.mn[a];
+            r.mx[a] = t.segs.geo.mx[a];
+        }
+        off += r.S;
+        refs.push_back(r);
     }
     c->build_state.store(1);
     const ndt_config cfg = c->cfg;
-    c->builder = std::thread([c, total, cfg]() {
+    c->builder = std::thread([c, refs, cfg]() {
         cudaSetDevice(c->device);
         float ms = 0.f;
-        int r = build_map(c->map_b, c->bs_b, (const float*)c->d_gather.p, (size_t)total, cfg,
-                          (uint32_t*)c->d_status_b.p, c->bstream, &ms);
+        int r = merge_tiles(c->map_b, c->bs_b, refs, c->d_tile_refs, cfg,
+                            (uint32_t*)c->d_status_b.p, c->bstream, &ms);
         uint32_t st = 0;
         if (!r) {
             cudaMemcpyAsync(&st, c->d_status_b.p, 4, cudaMemcpyDeviceToHost, c->bstream);
@@ -717,8 +781,9 @@ int ndt_tiles_commit(ndt_ctx* c, int32_t wait) {
 }
 
 int ndt_tiles_status(ndt_ctx* c, uint64_t* num_tiles, uint64_t* num_points, int32_t* pending,
-                     int32_t* last_rc, float* build_ms) {
+                     int32_t* last_rc, float* build_ms, float* put_ms) {
     if (!c) return NDT_ERR_INVALID_ARGUMENT;
+    if (put_ms) *put_ms = c->tile_put_ms;
     uint64_t n = 0;
     for (auto& t : c->tiles) n += t.n;
     if (num_tiles) *num_tiles = c->tiles.size();
@@ -880,6 +945,9 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
         p.eps = (double)sqrtf(ef * ef);
     }
     p.status = (uint32_t*)c->d_status.p;
+    p.stall_ns = c->stall_ns;
+    p.withhold = c->withhold_next;
+    c->withhold_next = 0;
     // line search: the graph path's candidates, or (CPU path) the More-Thuente search
     p.ls_cands = c->cfg.use_line_search ? LS_MAX : 0;
     p.ls_mu = LS_MU;
@@ -1652,9 +1720,9 @@ int ndt_tpe_propose(const ndt_particle_config* pc, uint64_t query, uint64_t part
 }
 
 int ndt_learned_pose_search(ndt_ctx* c, ndt_pnet* net, int32_t map_id, const ndt_scan* queries,
-                            uint64_t nq, double nvtl_threshold,
-                            const ndt_particle_config* fallback, ndt_pose_estimate* out,
-                            int32_t* used_fallback) {
+                            uint64_t nq, const ndt_particle_config* refine,
+                            double nvtl_threshold, const ndt_particle_config* fallback,
+                            ndt_pose_estimate* out, int32_t* used_fallback) {
     if (!c || !net || (nq && (!queries || !out))) return NDT_ERR_INVALID_ARGUMENT;
     int rc = need_target(c);
     if (rc) return rc;
@@ -1671,6 +1739,21 @@ int ndt_learned_pose_search(ndt_ctx* c, ndt_pnet* net, int32_t map_id, const ndt
     c->stats.proposal_launches += after.inference_batches - before.inference_batches;
     c->stats.proposal_kernel_ms += after.inference_kernel_ms - before.inference_kernel_ms;
     if ((rc = search_from_starts(c, queries, nq, np, starts.data(), out, nullptr))) return rc;
+    if (refine && refine->num_particles > 0) {
+        // a second round around each query's best proposal result: refine->num_particles
+        // particles drawn around it (the particle search's rule, seeded), all aligned in one
+        // launch; the better of the two rounds' winners is kept
+        std::vector<ndt_scan> around(queries, queries + nq);
+        for (uint64_t q = 0; q < nq; ++q)
+            for (int k = 0; k < 6; ++k) around[q].initial_pose[k] = out[q].pose[k];
+        ndt_particle_config rc2 = *refine;
+        rc2.guided = 0;
+        std::vector<ndt_pose_estimate> second(nq);
+        if ((rc = ndt_initial_pose_search(c, around.data(), nq, &rc2, second.data(), nullptr)))
+            return rc;
+        for (uint64_t q = 0; q < nq; ++q)
+            if (second[q].selection_score > out[q].selection_score) out[q] = second[q];
+    }
     std::vector<uint64_t> redo;
     for (uint64_t q = 0; q < nq; ++q) {
         const bool fb = fallback && out[q].nvtl < nvtl_threshold;

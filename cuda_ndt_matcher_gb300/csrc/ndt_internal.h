@@ -76,8 +76,51 @@ size_t detect_segments_temp_bytes(size_t n);
 int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_t* idx,
                  int32_t* d_minmax /* 6 ints + count */, cudaStream_t s);
 
+// Point count and cell box of a set of segments (a point set's, or a merge of tiles').
+struct SegGeometry {
+    size_t nf = 0;      // finite points
+    uint32_t S = 0;     // segments (occupied cells)
+    int32_t mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+};
 int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
               uint32_t* d_status, cudaStream_t s, float* build_ms);
+
+// Per-segment (per occupied cell) record of a build: cell, count and, for a voxel, its
+// mean, regularised covariance and inverse (upper triangle).
+struct SegRec {
+    float mean[3];
+    float cov[9];
+    float icov[6];  // c00, c01, c02, c11, c12, c22
+    int32_t coord[3];
+    uint32_t count;
+};
+
+// A map tile's segments, built once when the tile is put: point indices in key order,
+// segment starts, records and validity, with the tile's cell box.
+struct TileSegs {
+    DevBuf idx, starts, rec, valid;
+    SegGeometry geo;
+};
+int build_tile_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+                        cudaStream_t s, TileSegs& out, float* ms_out);
+
+// One tile as the merge kernels read it (device pointers; seg_off = the tile's first segment
+// in the concatenation of all tiles' segments, in tile order).
+struct TileSegRef {
+    const SegRec* rec;
+    const uint32_t* valid;
+    const uint32_t* starts;
+    const uint32_t* idx;
+    const float* pts;
+    uint64_t seg_off;
+    uint32_t S, nf;
+    int32_t mn[3], mx[3];
+};
+// The voxel map of the tiles' points concatenated in the given order, from their segments:
+// the same map build_map gives for that concatenation. Cells held by one tile keep that
+// tile's records; cells shared by tiles are recomputed from their points.
+int merge_tiles(Map& map, BuildScratch& sc, const std::vector<TileSegRef>& refs, DevBuf& d_refs,
+                const ndt_config& cfg, uint32_t* d_status, cudaStream_t s, float* build_ms);
 
 // One alignment job of a launch.
 struct AlignJob {
@@ -113,7 +156,7 @@ struct AlignOut {
 constexpr int TRACE_REC = 48;
 
 // Largest dense cell index a map build makes (bytes); beyond it the kernels probe the hash.
-constexpr uint64_t DENSE_GRID_MAX_BYTES = 512ull << 20;
+constexpr uint64_t DENSE_GRID_MAX_BYTES = 4096ull << 20;
 
 struct AlignParams {
     MapView map;
@@ -157,8 +200,14 @@ struct AlignParams {
     // stream may only run after it (the host then launches the continuation after the last
     // copy).
     int32_t qresume;
+    // work-queue kernel: a CTA that finds no work for stall_ns with alignments open (and all
+    // input resident) sets ST_QUEUE_STALL and leaves (2 s unless a test shortens it); with
+    // withhold, every chunk starts out claimed (a test hook: no CTA finds work)
+    uint64_t stall_ns;
+    int32_t withhold;
 };
 constexpr unsigned long long QSTARVE_NS = 2000000ull;
+constexpr unsigned long long QSTALL_NS = 2000000000ull;
 
 // Newton-kernel sums per iteration: 34 f32 per-thread accumulators (score, gradient and
 // Hessian terms), reduced in FP64, plus the correspondence count.

@@ -98,51 +98,80 @@ __host__ __device__ constexpr uint32_t mma_idesc_bf16(int m, int n) {
 
 // Fused epilogue of 32 accumulator columns [c0, c0 + 32) of row `row` (one lane = one row):
 // per column, the 32 lanes of a warp write 32 consecutive rows of xt (64 coalesced bytes);
-// the row-major outputs go out as 16-byte vectors.
+// the row-major f32 and bf16 outputs (and the f32 input of the backward mode) move as 16-byte
+// vectors when the columns are full and aligned.
 __device__ __forceinline__ void epilogue_fused(const GemmEpilogue& epi, const uint32_t* r,
                                                float* D, int ldd, int M, int N, int row,
                                                int c0) {
-    const bool in_row = row < M;
-    float v[32];
+    if (row >= M) return;
+    const bool full = c0 + 32 <= N && (N & 7) == 0 && (ldd & 3) == 0;
+    float out[32], v[32];
+    if (full) {
+        if (epi.mode == GEMM_EPI_GELU_BACK) {
+            const float4* z4 = reinterpret_cast<const float4*>(epi.zin + (size_t)row * N + c0);
 #pragma unroll
-    for (int q = 0; q < 32; ++q) {
-        const int n = c0 + q;
-        float a = __uint_as_float(r[q]);
-        float out = a;
-        if (n < N) {
-            if (epi.mode == GEMM_EPI_GELU_BACK) {
-                const float z = in_row ? epi.zin[(size_t)row * N + n] : 0.f;
-                out = a * gelu_tanh_grad(z);
-                v[q] = out;
-            } else {
-                out = a + epi.bias[n];
-                v[q] = epi.mode == GEMM_EPI_BIAS_GELU ? gelu_tanh(out) : out;
+            for (int q = 0; q < 32; q += 4) {
+                const float4 z = z4[q / 4];
+                const float zz[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    out[q + u] = __uint_as_float(r[q + u]) * gelu_tanh_grad(zz[u]);
+                    v[q + u] = out[q + u];
+                }
             }
-            if (in_row) D[(size_t)row * ldd + n] = out;
-            if (epi.xt && in_row) epi.xt[(size_t)n * M + row] = __float2bfloat16(v[q]);
         } else {
-            v[q] = 0.f;
+            const float4* b4 = reinterpret_cast<const float4*>(epi.bias + c0);
+#pragma unroll
+            for (int q = 0; q < 32; q += 4) {
+                const float4 b = b4[q / 4];
+                const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    out[q + u] = __uint_as_float(r[q + u]) + bb[u];
+                    v[q + u] = epi.mode == GEMM_EPI_BIAS_GELU ? gelu_tanh(out[q + u]) : out[q + u];
+                }
+            }
         }
-    }
-    if (epi.x && in_row) {
-        __nv_bfloat16* xr = epi.x + (size_t)row * N + c0;
-        if (c0 + 32 <= N && (N & 7) == 0) {
+        float4* d4 = reinterpret_cast<float4*>(D + (size_t)row * ldd + c0);
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+            d4[q / 4] = make_float4(out[q], out[q + 1], out[q + 2], out[q + 3]);
+        if (epi.x) {
+            uint4* x4 = reinterpret_cast<uint4*>(epi.x + (size_t)row * N + c0);
 #pragma unroll
             for (int q = 0; q < 32; q += 8) {
-                __nv_bfloat162 h0 = __floats2bfloat162_rn(v[q], v[q + 1]);
-                __nv_bfloat162 h1 = __floats2bfloat162_rn(v[q + 2], v[q + 3]);
-                __nv_bfloat162 h2 = __floats2bfloat162_rn(v[q + 4], v[q + 5]);
-                __nv_bfloat162 h3 = __floats2bfloat162_rn(v[q + 6], v[q + 7]);
-                uint4 u;
-                u.x = *reinterpret_cast<uint32_t*>(&h0);
-                u.y = *reinterpret_cast<uint32_t*>(&h1);
-                u.z = *reinterpret_cast<uint32_t*>(&h2);
-                u.w = *reinterpret_cast<uint32_t*>(&h3);
-                *reinterpret_cast<uint4*>(xr + q) = u;
+                __nv_bfloat162 h[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) h[u] = __floats2bfloat162_rn(v[q + 2 * u], v[q + 2 * u + 1]);
+                uint4 w;
+                w.x = *reinterpret_cast<uint32_t*>(&h[0]);
+                w.y = *reinterpret_cast<uint32_t*>(&h[1]);
+                w.z = *reinterpret_cast<uint32_t*>(&h[2]);
+                w.w = *reinterpret_cast<uint32_t*>(&h[3]);
+                x4[q / 8] = w;
             }
-        } else {
-            for (int q = 0; q < 32 && c0 + q < N; ++q) xr[q] = __float2bfloat16(v[q]);
         }
+        if (epi.xt) {
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                epi.xt[(size_t)(c0 + q) * M + row] = __float2bfloat16(v[q]);
+        }
+        return;
+    }
+    for (int q = 0; q < 32 && c0 + q < N; ++q) {
+        const int n = c0 + q;
+        const float a = __uint_as_float(r[q]);
+        float o, x;
+        if (epi.mode == GEMM_EPI_GELU_BACK) {
+            o = a * gelu_tanh_grad(epi.zin[(size_t)row * N + n]);
+            x = o;
+        } else {
+            o = a + epi.bias[n];
+            x = epi.mode == GEMM_EPI_BIAS_GELU ? gelu_tanh(o) : o;
+        }
+        D[(size_t)row * ldd + n] = o;
+        if (epi.x) epi.x[(size_t)row * N + n] = __float2bfloat16(x);
+        if (epi.xt) epi.xt[(size_t)n * M + row] = __float2bfloat16(x);
     }
 }
 

@@ -504,13 +504,6 @@ int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_
 // ---------------------------------------------------------------------------------------
 // Voxel statistics (one thread per segment) and regularisation.
 // ---------------------------------------------------------------------------------------
-struct SegRec {
-    float mean[3];
-    float cov[9];
-    float icov[6];  // c00, c01, c02, c11, c12, c22
-    int32_t coord[3];
-    uint32_t count;
-};
 
 // Cyclic Jacobi for a symmetric 3x3 in f32 (row-major a, eigenvectors in the columns of v).
 // It only has to find the eigenvector directions to f32 accuracy: the eigenvalues and the
@@ -749,73 +742,85 @@ __device__ bool regularize(const double* A, const float* a32, const float* V32, 
     return true;
 }
 
-// Voxel statistics, one thread per segment: FP64 centred two-pass moments over the
-// segment's points in input order (count, mean, covariance / (n - 1)), then the regularised
-// covariance and its inverse (regularize). GB300's FP64 rate is a small fraction of its FP32
-// rate: the eigenvector directions come from an f32 Jacobi, and FP64 is spent only where the
-// outputs depend on it.
+// Statistics of one voxel from its points, visited in input order by each(f) (f called with
+// a pointer to each point's xyz): count, FP64 centred two-pass moments (mean, covariance /
+// (n - 1)), then the regularised covariance and its inverse (regularize). GB300's FP64 rate
+// is a small fraction of its FP32 rate: the eigenvector directions come from an f32 Jacobi,
+// and FP64 is spent only where the outputs depend on it. r.coord is the caller's.
+template <class Each>
+__device__ __forceinline__ bool voxel_stats(Each each, uint32_t cnt, int min_points,
+                                            float ratio, SegRec& r) {
+    r.count = cnt;
+    if ((int)cnt < min_points) return false;
+    double sum[3] = {0.0, 0.0, 0.0};
+    each([&](const float* p) {
+        sum[0] += (double)p[0];
+        sum[1] += (double)p[1];
+        sum[2] += (double)p[2];
+    });
+    const double nn = (double)cnt;
+    const double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
+    // upper triangle xx, xy, xz, yy, yz, zz (the products are symmetric bit for bit)
+    double sq[6] = {0, 0, 0, 0, 0, 0};
+    each([&](const float* p) {
+        const double d0 = (double)p[0] - mean[0], d1 = (double)p[1] - mean[1],
+                     d2 = (double)p[2] - mean[2];
+        sq[0] += d0 * d0;
+        sq[1] += d0 * d1;
+        sq[2] += d0 * d2;
+        sq[3] += d1 * d1;
+        sq[4] += d1 * d2;
+        sq[5] += d2 * d2;
+    });
+    const double nm1 = nn - 1.0;
+    double A[9];
+    A[0] = sq[0] / nm1;
+    A[1] = A[3] = sq[1] / nm1;
+    A[2] = A[6] = sq[2] / nm1;
+    A[4] = sq[3] / nm1;
+    A[5] = A[7] = sq[4] / nm1;
+    A[8] = sq[5] / nm1;
+    float a32[9], V32[9];
+    for (int q = 0; q < 9; ++q) a32[q] = (float)A[q];
+    jacobi3f(a32, V32);
+    if (!regularize(A, a32, V32, ratio, r)) return false;
+    for (int q = 0; q < 3; ++q) r.mean[q] = (float)mean[q];
+    return true;
+}
+
+// Segment sizes as sort keys: segments visited largest first (key 0xFFFF - min(count,
+// 0xFFFF)), so the threads of a warp take segments of nearly equal size (one thread walks
+// one segment; a warp costs its largest segment) and the longest warps start first.
+__global__ void k_seg_size_keys(const uint32_t* __restrict__ starts, uint32_t S, uint32_t nf,
+                                uint64_t* __restrict__ keys, uint32_t* __restrict__ order) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint32_t e = s + 1 < S ? starts[s + 1] : nf;
+    keys[s] = 0xFFFFu - min(e - starts[s], 0xFFFFu);
+    order[s] = s;
+}
+
+// One thread per segment of the sorted keys (order[t]: the t-th segment to visit). Every
+// segment's record gets its cell and count (a tile merge reads them for cells shared between
+// tiles); valid[s] marks the voxels.
 __global__ void __launch_bounds__(128) k_voxel_stats(
     const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
-    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ num_seg, uint32_t nf,
-    float res, int min_points, float ratio, SegRec* __restrict__ rec,
+    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ order, uint32_t S,
+    uint32_t nf, float res, int min_points, float ratio, SegRec* __restrict__ rec,
     uint32_t* __restrict__ valid) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t S = *num_seg;
-    if (s >= nf) return;
-    if (s >= S) {
-        valid[s] = 0;
-        return;
-    }
-    uint32_t b = starts[s];
-    uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
-    uint32_t cnt = e - b;
-    uint32_t ok = 0;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S) return;
+    const uint32_t s = order[t];
+    const uint32_t b = starts[s];
+    const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
     SegRec r;
-    {
-        const float* p0 = pts + 3 * (size_t)sidx[b];
-        cell_of(p0, res, r.coord);
-    }
-    r.count = cnt;
-    if ((int)cnt >= min_points) {
-        double sum[3] = {0.0, 0.0, 0.0};
-        for (uint32_t k = b; k < e; ++k) {
-            const float* p = pts + 3 * (size_t)sidx[k];
-            sum[0] += (double)p[0];
-            sum[1] += (double)p[1];
-            sum[2] += (double)p[2];
-        }
-        const double nn = (double)cnt;
-        const double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
-        // upper triangle xx, xy, xz, yy, yz, zz (the products are symmetric bit for bit)
-        double sq[6] = {0, 0, 0, 0, 0, 0};
-        for (uint32_t k = b; k < e; ++k) {
-            const float* p = pts + 3 * (size_t)sidx[k];
-            const double d0 = (double)p[0] - mean[0], d1 = (double)p[1] - mean[1],
-                         d2 = (double)p[2] - mean[2];
-            sq[0] += d0 * d0;
-            sq[1] += d0 * d1;
-            sq[2] += d0 * d2;
-            sq[3] += d1 * d1;
-            sq[4] += d1 * d2;
-            sq[5] += d2 * d2;
-        }
-        const double nm1 = nn - 1.0;
-        double A[9];
-        A[0] = sq[0] / nm1;
-        A[1] = A[3] = sq[1] / nm1;
-        A[2] = A[6] = sq[2] / nm1;
-        A[4] = sq[3] / nm1;
-        A[5] = A[7] = sq[4] / nm1;
-        A[8] = sq[5] / nm1;
-        float a32[9], V32[9];
-        for (int q = 0; q < 9; ++q) a32[q] = (float)A[q];
-        jacobi3f(a32, V32);
-        ok = regularize(A, a32, V32, ratio, r) ? 1u : 0u;
-        if (ok)
-            for (int q = 0; q < 3; ++q) r.mean[q] = (float)mean[q];
-    }
-    if (ok) rec[s] = r;
-    valid[s] = ok;
+    cell_of(pts + 3 * (size_t)sidx[b], res, r.coord);
+    auto each = [&](auto f) {
+        for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
+    };
+    const bool ok = voxel_stats(each, e - b, min_points, ratio, r);
+    rec[s] = r;
+    valid[s] = ok ? 1u : 0u;
 }
 
 __global__ void k_voxel_compact(const SegRec* __restrict__ rec, const uint32_t* __restrict__ valid,
@@ -882,27 +887,26 @@ __global__ void k_grid_fill(MapView m, float4* __restrict__ grid) {
                             __int_as_float((int32_t)s));
 }
 
-// Neighbourhood masks (layout in MapView::nmask): one thread per cell of the box grown by
-// one cell on every side gathers the occupancy of its 27 neighbours from the dense index.
-__global__ void k_grid_mask(const float4* __restrict__ grid, uint32_t e0, uint32_t e1,
-                            uint32_t e2, uint32_t* __restrict__ nmask) {
-    const uint32_t E1 = e1 + 2u, E2 = e2 + 2u;
-    const uint64_t total = (uint64_t)(e0 + 2u) * E1 * E2;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t mz = (uint32_t)(i % E2);
-        const uint32_t my = (uint32_t)((i / E2) % E1);
-        const uint32_t mx = (uint32_t)(i / ((uint64_t)E2 * E1));
-        uint32_t bits = 0u;
+// Neighbourhood masks (layout in MapView::nmask), scattered from the voxels: the voxel in
+// local cell v is neighbour d = (dx, dy, dz) of cell v - d, so it sets bit
+// 9 (dx + 1) + 3 (dy + 1) + (dz + 1) of that cell's mask, at grown-box position v - d + 1
+// (always inside the grown box). One thread per hash slot; the masks start at zero, and OR
+// is order-free, so the result does not depend on the threads' order. The work goes with
+// the number of voxels, not with the box.
+__global__ void k_grid_mask(MapView m, uint32_t* __restrict__ nmask) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > m.mask) return;
+    const uint32_t key = m.slots[s].x;
+    if (key == EMPTY_KEY) return;
+    const uint32_t vx = key & ((1u << m.bits[0]) - 1u);
+    const uint32_t vy = (key >> m.bits[0]) & ((1u << m.bits[1]) - 1u);
+    const uint32_t vz = key >> (m.bits[0] + m.bits[1]);
+    const uint32_t E1 = m.ext[1] + 2u, E2 = m.ext[2] + 2u;
 #pragma unroll 1
-        for (uint32_t b = 0; b < 27u; ++b) {
-            // neighbour (local) = grown-box cell - 1 + (offset - 1)
-            const uint32_t nx = mx + b / 9u - 2u, ny = my + b / 3u % 3u - 2u, nz = mz + b % 3u - 2u;
-            if (nx >= e0 || ny >= e1 || nz >= e2) continue;  // wrapped negatives are huge
-            const float w = __ldg(&grid[((size_t)nx * e1 + ny) * e2 + nz].w);
-            if (__float_as_int(w) >= 0) bits |= 1u << b;
-        }
-        nmask[i] = bits;
+    for (uint32_t b = 0; b < 27u; ++b) {
+        // grown-box position of cell v - d, plus one: v + 1 - (d + 1) + 1 = v + 2 - (d + 1)
+        const uint32_t gx = vx + 2u - b / 9u, gy = vy + 2u - b / 3u % 3u, gz = vz + 2u - b % 3u;
+        atomicOr(nmask + ((size_t)gx * E1 + gy) * E2 + gz, 1u << b);
     }
 }
 
@@ -912,20 +916,28 @@ static uint32_t bit_width(uint32_t x) {
     return b;
 }
 
-int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
-              uint32_t* d_status, cudaStream_t s, float* build_ms) {
-    if (n == 0) {
-        set_error("Target point cloud is empty");
-        return NDT_ERR_EMPTY_INPUT;
+// Key width of a cell box: bits per axis of (max - min), checked against the key limits.
+static int box_bits(const int32_t* mn, const int32_t* mx, uint32_t* bits) {
+    for (int a = 0; a < 3; ++a) {
+        int64_t range = (int64_t)mx[a] - (int64_t)mn[a];
+        if (range > 0x1FFFFF) {
+            set_error("map extent exceeds 2^21 voxels along an axis");
+            return NDT_ERR_RANGE;
+        }
+        bits[a] = std::max<uint32_t>(1, bit_width((uint32_t)range));
     }
-    if (n >= 0xFFFFFFF0ull) {
-        set_error("target point cloud exceeds 2^32 points");
-        return NDT_ERR_CAPACITY;
+    if (bits[0] + bits[1] + bits[2] > 31) {
+        set_error("map bounding box exceeds 2^31 voxel cells (tile the map)");
+        return NDT_ERR_RANGE;
     }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, s);
+    return 0;
+}
+
+// Stages 1-5 of a build: cells and bounds, Morton keys, sort, segments, per-segment
+// statistics. Leaves in sc: vals (point indices in key order), seg_starts, seg_rec,
+// seg_valid; returns the counts and the cell box in g.
+int build_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+                   cudaStream_t s, SegGeometry& g) {
     int rc = 0;
     if ((rc = dev_reserve(sc.keys_a, n * 8)) || (rc = dev_reserve(sc.vals_a, n * 4)) ||
         (rc = dev_reserve(sc.small, 256)) || (rc = dev_reserve(sc.seg_starts, n * 4 + 4)) ||
@@ -939,51 +951,64 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
     uint32_t* vals = (uint32_t*)sc.vals_a.p;
     int32_t* mm = (int32_t*)sc.small.p;
     uint32_t* nseg = (uint32_t*)((char*)sc.small.p + 64);
-    uint32_t* mprobe = (uint32_t*)((char*)sc.small.p + 128);
 
     if ((rc = morton_codes(d_pts, n, cfg.resolution, keys, vals, mm, s))) return rc;
     int32_t hmm[7];
     cudaMemcpyAsync(hmm, mm, sizeof hmm, cudaMemcpyDeviceToHost, s);
     if ((rc = cuda_fail(cudaStreamSynchronize(s), "map bounds"))) return rc;
-    size_t nf = (size_t)(uint32_t)hmm[6];
-    if (nf == 0) {
+    g.nf = (size_t)(uint32_t)hmm[6];
+    if (g.nf == 0) {
         set_error("Target point cloud is empty");
         return NDT_ERR_EMPTY_INPUT;
     }
-    uint32_t bits[3];
     for (int a = 0; a < 3; ++a) {
-        int64_t range = (int64_t)hmm[3 + a] - (int64_t)hmm[a];
-        if (range > 0x1FFFFF) {
-            set_error("map extent exceeds 2^21 voxels along an axis");
-            return NDT_ERR_RANGE;
-        }
-        bits[a] = std::max<uint32_t>(1, bit_width((uint32_t)range));
+        g.mn[a] = hmm[a];
+        g.mx[a] = hmm[3 + a];
     }
-    if (bits[0] + bits[1] + bits[2] > 31) {
-        set_error("map bounding box exceeds 2^31 voxel cells (tile the map)");
-        return NDT_ERR_RANGE;
-    }
-    uint32_t lv = std::max(bits[0], std::max(bits[1], bits[2]));
-    int end_bit = std::min(64, (int)(3 * lv + 1));
+    uint32_t bits[3];
+    if ((rc = box_bits(g.mn, g.mx, bits))) return rc;
+    const uint32_t lv = std::max(bits[0], std::max(bits[1], bits[2]));
+    const int end_bit = std::min(64, (int)(3 * lv + 1));
     if ((rc = radix_sort_pairs(keys, vals, n, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s))) return rc;
-    if ((rc = detect_segments(keys, nf, nullptr, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p,
+    if ((rc = detect_segments(keys, g.nf, nullptr, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p,
                               sc.tmp.bytes, s)))
         return rc;
-    unsigned g = (unsigned)((nf + 127) / 128);
-    k_voxel_stats<<<g, 128, 0, s>>>(d_pts, vals, (uint32_t*)sc.seg_starts.p, nseg, (uint32_t)nf,
-                                    cfg.resolution, cfg.min_points_per_voxel,
-                                    cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
-                                    (uint32_t*)sc.seg_valid.p);
-    if ((rc = exclusive_scan((uint32_t*)sc.seg_valid.p, (uint32_t*)sc.seg_rank.p, nf, sc.tmp.p,
-                             s)))
+    cudaMemcpyAsync(&g.S, nseg, 4, cudaMemcpyDeviceToHost, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "segments"))) return rc;
+    // visit order of the segments, largest first (the keys' buffer is free again: the
+    // segments are recorded by their starts)
+    uint64_t* skeys = keys;
+    uint32_t* order = (uint32_t*)sc.seg_rank.p;
+    k_seg_size_keys<<<(g.S + 255) / 256, 256, 0, s>>>((const uint32_t*)sc.seg_starts.p, g.S,
+                                                      (uint32_t)g.nf, skeys, order);
+    if ((rc = radix_sort_pairs(skeys, order, g.S, 0, 16, sc.tmp.p, sc.tmp.bytes, s))) return rc;
+    k_voxel_stats<<<(g.S + 127) / 128, 128, 0, s>>>(
+        d_pts, vals, (uint32_t*)sc.seg_starts.p, order, g.S, (uint32_t)g.nf, cfg.resolution,
+        cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
+        (uint32_t*)sc.seg_valid.p);
+    return cuda_fail(cudaStreamSynchronize(s), "voxel statistics");
+}
+
+// Stages 6-7: valid voxels of the S records (in Morton order of their cells) compacted into
+// the map's voxel arrays, hash insert, dense cell index and neighbourhood masks.
+int finish_map(Map& map, BuildScratch& sc, const SegRec* rec, const uint32_t* valid, uint32_t S,
+               const SegGeometry& g, const ndt_config& cfg, uint32_t* d_status, cudaStream_t s) {
+    int rc;
+    if ((rc = dev_reserve(sc.seg_rank, (size_t)S * 4 + 4)) ||
+        (rc = dev_reserve(sc.tmp, std::max(sc.tmp.bytes, scan_temp_bytes(S)))) ||
+        (rc = dev_reserve(sc.small, 256)))
         return rc;
-    uint32_t hs[3];
-    cudaMemcpyAsync(&hs[0], nseg, 4, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&hs[1], (uint32_t*)sc.seg_rank.p + (nf - 1), 4, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&hs[2], (uint32_t*)sc.seg_valid.p + (nf - 1), 4, cudaMemcpyDeviceToHost, s);
-    if ((rc = cuda_fail(cudaStreamSynchronize(s), "voxel statistics"))) return rc;
-    uint32_t S = hs[0];
-    uint32_t V = hs[1] + hs[2];
+    uint32_t* mprobe = (uint32_t*)((char*)sc.small.p + 128);
+    uint32_t* d_S = (uint32_t*)((char*)sc.small.p + 192);
+    uint32_t bits[3];
+    if ((rc = box_bits(g.mn, g.mx, bits))) return rc;
+    if ((rc = exclusive_scan(valid, (uint32_t*)sc.seg_rank.p, S, sc.tmp.p, s))) return rc;
+    uint32_t hs[2];
+    cudaMemcpyAsync(&hs[0], (uint32_t*)sc.seg_rank.p + (S - 1), 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hs[1], valid + (S - 1), 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(d_S, &S, 4, cudaMemcpyHostToDevice, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "voxel compaction"))) return rc;
+    const uint32_t V = hs[0] + hs[1];
     if (V == 0) {
         set_error("No voxels created from target points (too sparse?)");
         return NDT_ERR_NO_VOXELS;
@@ -1003,10 +1028,11 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
         (rc = dev_reserve(map.slots, cap * 16)) || (rc = dev_reserve(map.slot_icov, cap * 32)) ||
         (rc = dev_reserve(map.slot_vidx, cap * 4)))
         return rc;
-    k_voxel_compact<<<g, 128, 0, s>>>((SegRec*)sc.seg_rec.p, (uint32_t*)sc.seg_valid.p,
-                                      (uint32_t*)sc.seg_rank.p, nseg, (int32_t*)map.vox_coord.p,
-                                      (float4*)map.vox_mean.p, (float*)map.vox_cov.p,
-                                      (float*)map.vox_icov.p, (uint32_t*)map.vox_count.p);
+    const unsigned blk = (unsigned)((S + 127) / 128);
+    k_voxel_compact<<<blk, 128, 0, s>>>(rec, valid, (uint32_t*)sc.seg_rank.p, d_S,
+                                        (int32_t*)map.vox_coord.p, (float4*)map.vox_mean.p,
+                                        (float*)map.vox_cov.p, (float*)map.vox_icov.p,
+                                        (uint32_t*)map.vox_count.p);
     cudaMemsetAsync(map.slots.p, 0xFF, cap * 16, s);
     cudaMemsetAsync(mprobe, 0, 4, s);
     MapView v{};
@@ -1016,7 +1042,7 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
     v.mask = (uint32_t)(cap - 1);
     v.max_probe = 0;
     for (int a = 0; a < 3; ++a) {
-        v.min_cell[a] = hmm[a];
+        v.min_cell[a] = g.mn[a];
         v.bits[a] = bits[a];
     }
     v.res = cfg.resolution;
@@ -1035,7 +1061,7 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
     // dense cell index over the bounding box of the map's cells, when it fits the budget
     uint64_t cells = 1;
     for (int a = 0; a < 3; ++a) {
-        v.ext[a] = (uint32_t)((int64_t)hmm[3 + a] - (int64_t)hmm[a] + 1);
+        v.ext[a] = (uint32_t)((int64_t)g.mx[a] - (int64_t)g.mn[a] + 1);
         cells *= v.ext[a];
     }
     v.grid = nullptr;
@@ -1046,39 +1072,247 @@ int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const nd
             (rc = dev_reserve(map.nmask, (size_t)mcells * 4)))
             return rc;
         cudaMemsetAsync(map.grid.p, 0xFF, (size_t)cells * 16, s);
+        cudaMemsetAsync(map.nmask.p, 0, (size_t)mcells * 4, s);
         k_grid_fill<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (float4*)map.grid.p);
-        const unsigned mblocks = (unsigned)std::min<uint64_t>((mcells + 255) / 256, 152ull * 64);
-        k_grid_mask<<<mblocks, 256, 0, s>>>((const float4*)map.grid.p, v.ext[0], v.ext[1],
-                                            v.ext[2], (uint32_t*)map.nmask.p);
+        k_grid_mask<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (uint32_t*)map.nmask.p);
         v.grid = (const float4*)map.grid.p;
         v.nmask = (const uint32_t*)map.nmask.p;
     }
-    cudaEventRecord(e1, s);
     uint32_t hprobe = 0;
     cudaMemcpyAsync(&hprobe, mprobe, 4, cudaMemcpyDeviceToHost, s);
     if ((rc = cuda_fail(cudaStreamSynchronize(s), "hash insert"))) return rc;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (build_ms) *build_ms = ms;
     v.max_probe = hprobe;
     map.view = v;
     ndt_map_info& info = map.info;
-    info.num_points = nf;
+    info.num_points = g.nf;
     info.num_segments = S;
     info.num_voxels = V;
     info.hash_capacity = cap;
     info.max_probe = hprobe;
     for (int a = 0; a < 3; ++a) {
         info.key_bits[a] = bits[a];
-        info.min_coord[a] = hmm[a];
-        info.max_coord[a] = hmm[3 + a];
+        info.min_coord[a] = g.mn[a];
+        info.max_coord[a] = g.mx[a];
     }
-    info.build_ms = ms;
     info.dense_grid_mib =
         v.grid ? (float)(((double)cells * 16.0 + (double)mcells * 4.0) / (1024.0 * 1024.0)) : 0.f;
     map.valid = true;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// Map tiles: segments built once per tile, merged per commit.
+// ---------------------------------------------------------------------------------------
+// Keys of every tile's segments for the merged map: Morton code of the cell relative to the
+// merged box's minimum cell (the key set_target of the concatenated points would give each of
+// its points), value = the segment's index in tile order.
+__global__ void k_merge_keys(const TileSegRef* __restrict__ tiles, int nt, uint64_t total,
+                             int32_t mn0, int32_t mn1, int32_t mn2, uint64_t* __restrict__ keys,
+                             uint32_t* __restrict__ vals) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int t = 0;
+    while (t + 1 < nt && i >= tiles[t + 1].seg_off) ++t;
+    const int32_t* c = tiles[t].rec[i - tiles[t].seg_off].coord;
+    const int32_t mn[3] = {mn0, mn1, mn2};
+    uint32_t q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int64_t d = (int64_t)c[a] - (int64_t)mn[a];
+        q[a] = d > 0x1FFFFF ? 0x1FFFFFu : (uint32_t)d;
+    }
+    keys[i] = morton3(q[0], q[1], q[2]);
+    vals[i] = (uint32_t)i;
+}
+
+// One thread per cell of the merged map (a group of equal keys: the segments of that cell in
+// tile order). A cell held by one tile keeps that tile's record; a cell shared by tiles is
+// recomputed from all its points in tile order, then each tile's input order, which is the
+// order set_target of the concatenated tiles would visit them in.
+__global__ void __launch_bounds__(128) k_merge_groups(
+    const TileSegRef* __restrict__ tiles, int nt, const uint32_t* __restrict__ members,
+    const uint32_t* __restrict__ gstart, const uint32_t* __restrict__ num_groups,
+    uint32_t n_members, int min_points, float ratio, SegRec* __restrict__ grec,
+    uint32_t* __restrict__ gvalid) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t G = *num_groups;
+    if (g >= G) return;
+    const uint32_t m0 = gstart[g], m1 = g + 1 < G ? gstart[g + 1] : n_members;
+    auto locate = [&](uint32_t id, int& t, uint32_t& sl) {
+        t = 0;
+        while (t + 1 < nt && id >= tiles[t + 1].seg_off) ++t;
+        sl = id - (uint32_t)tiles[t].seg_off;
+    };
+    int t;
+    uint32_t sl;
+    locate(members[m0], t, sl);
+    if (m1 - m0 == 1) {
+        grec[g] = tiles[t].rec[sl];
+        gvalid[g] = tiles[t].valid[sl];
+        return;
+    }
+    SegRec r;
+    for (int a = 0; a < 3; ++a) r.coord[a] = tiles[t].rec[sl].coord[a];
+    uint32_t cnt = 0;
+    for (uint32_t m = m0; m < m1; ++m) {
+        locate(members[m], t, sl);
+        cnt += tiles[t].rec[sl].count;
+    }
+    auto each = [&](auto f) {
+        for (uint32_t m = m0; m < m1; ++m) {
+            int tm;
+            uint32_t sm;
+            locate(members[m], tm, sm);
+            const TileSegRef& T = tiles[tm];
+            const uint32_t b = T.starts[sm], e = sm + 1 < T.S ? T.starts[sm + 1] : T.nf;
+            for (uint32_t k = b; k < e; ++k) f(T.pts + 3 * (size_t)T.idx[k]);
+        }
+    };
+    const bool ok = voxel_stats(each, cnt, min_points, ratio, r);
+    grec[g] = r;
+    gvalid[g] = ok ? 1u : 0u;
+}
+
+int merge_tiles(Map& map, BuildScratch& sc, const std::vector<TileSegRef>& refs,
+                DevBuf& d_refs, const ndt_config& cfg, uint32_t* d_status, cudaStream_t s,
+                float* build_ms) {
+    SegGeometry g{};
+    uint64_t total = 0;
+    bool any = false;
+    for (const auto& t : refs) {
+        if (!t.S) continue;
+        for (int a = 0; a < 3; ++a) {
+            g.mn[a] = any ? std::min(g.mn[a], t.mn[a]) : t.mn[a];
+            g.mx[a] = any ? std::max(g.mx[a], t.mx[a]) : t.mx[a];
+        }
+        any = true;
+        g.nf += t.nf;
+        total += t.S;
+    }
+    if (!any) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    if (total >= 0xFFFFFFF0ull) {
+        set_error("too many occupied cells in the tiles");
+        return NDT_ERR_CAPACITY;
+    }
+    uint32_t bits[3];
+    int rc = box_bits(g.mn, g.mx, bits);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    std::vector<TileSegRef> used;
+    for (const auto& t : refs)
+        if (t.S) used.push_back(t);
+    const int nt = (int)used.size();
+    size_t tmp = std::max(radix_sort_temp_bytes(total), detect_segments_temp_bytes(total));
+    if ((rc = dev_reserve(d_refs, used.size() * sizeof(TileSegRef))) ||
+        (rc = dev_reserve(sc.keys_a, total * 8)) || (rc = dev_reserve(sc.vals_a, total * 4)) ||
+        (rc = dev_reserve(sc.small, 256)) || (rc = dev_reserve(sc.seg_starts, total * 4 + 4)) ||
+        (rc = dev_reserve(sc.seg_valid, total * 4 + 4)) ||
+        (rc = dev_reserve(sc.seg_rec, total * sizeof(SegRec))) ||
+        (rc = dev_reserve(sc.tmp, std::max(tmp, scan_temp_bytes(total)))))
+        return rc;
+    cudaMemcpyAsync(d_refs.p, used.data(), used.size() * sizeof(TileSegRef),
+                    cudaMemcpyHostToDevice, s);
+    uint64_t* keys = (uint64_t*)sc.keys_a.p;
+    uint32_t* vals = (uint32_t*)sc.vals_a.p;
+    uint32_t* ngroups = (uint32_t*)((char*)sc.small.p + 64);
+    const TileSegRef* dref = (const TileSegRef*)d_refs.p;
+    k_merge_keys<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(dref, nt, total, g.mn[0],
+                                                                 g.mn[1], g.mn[2], keys, vals);
+    const uint32_t lv = std::max(bits[0], std::max(bits[1], bits[2]));
+    const int end_bit = std::min(64, (int)(3 * lv + 1));
+    if ((rc = radix_sort_pairs(keys, vals, total, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s)) ||
+        (rc = detect_segments(keys, total, nullptr, (uint32_t*)sc.seg_starts.p, ngroups,
+                              sc.tmp.p, sc.tmp.bytes, s)))
+        return rc;
+    k_merge_groups<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        dref, nt, vals, (const uint32_t*)sc.seg_starts.p, ngroups, (uint32_t)total,
+        cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
+        (uint32_t*)sc.seg_valid.p);
+    cudaMemcpyAsync(&g.S, ngroups, 4, cudaMemcpyDeviceToHost, s);
+    if ((rc = cuda_fail(cudaStreamSynchronize(s), "tile merge"))) return rc;
+    rc = finish_map(map, sc, (const SegRec*)sc.seg_rec.p, (const uint32_t*)sc.seg_valid.p, g.S,
+                    g, cfg, d_status, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (build_ms) *build_ms = ms;
+    map.info.build_ms = ms;
+    return 0;
+}
+
+// A tile's segments, kept with the tile: the outputs of build_segments moved into the tile's
+// own buffers (point indices in key order, segment starts, records, validity).
+int build_tile_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+                        cudaStream_t s, TileSegs& out, float* ms_out) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    SegGeometry g{};
+    int rc = build_segments(sc, d_pts, n, cfg, s, g);
+    if (rc == NDT_ERR_EMPTY_INPUT) {  // no finite point: the tile adds no cell
+        out.geo = SegGeometry{};
+        rc = 0;
+    } else if (!rc) {
+        out.geo = g;
+        if ((rc = dev_reserve(out.idx, g.nf * 4)) || (rc = dev_reserve(out.starts, (size_t)g.S * 4)) ||
+            (rc = dev_reserve(out.rec, (size_t)g.S * sizeof(SegRec))) ||
+            (rc = dev_reserve(out.valid, (size_t)g.S * 4)))
+            return rc;
+        cudaMemcpyAsync(out.idx.p, sc.vals_a.p, g.nf * 4, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(out.starts.p, sc.seg_starts.p, (size_t)g.S * 4, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(out.rec.p, sc.seg_rec.p, (size_t)g.S * sizeof(SegRec),
+                        cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(out.valid.p, sc.seg_valid.p, (size_t)g.S * 4, cudaMemcpyDeviceToDevice, s);
+    }
+    cudaEventRecord(e1, s);
+    if (!rc) rc = cuda_fail(cudaEventSynchronize(e1), "tile segments");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms_out) *ms_out = ms;
+    return rc;
+}
+
+int build_map(Map& map, BuildScratch& sc, const float* d_pts, size_t n, const ndt_config& cfg,
+              uint32_t* d_status, cudaStream_t s, float* build_ms) {
+    if (n == 0) {
+        set_error("Target point cloud is empty");
+        return NDT_ERR_EMPTY_INPUT;
+    }
+    if (n >= 0xFFFFFFF0ull) {
+        set_error("target point cloud exceeds 2^32 points");
+        return NDT_ERR_CAPACITY;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    SegGeometry g{};
+    int rc = build_segments(sc, d_pts, n, cfg, s, g);
+    if (!rc)
+        rc = finish_map(map, sc, (const SegRec*)sc.seg_rec.p, (const uint32_t*)sc.seg_valid.p, g.S,
+                        g, cfg, d_status, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (build_ms) *build_ms = ms;
+    map.info.build_ms = ms;
     return 0;
 }
 

@@ -49,7 +49,8 @@ extern "C" {
 /* Cell lookup of the search kernels. Both give the same voxel for a cell (one voxel per
  * cell); they differ in cost. The hash table (the reference's structure, voxel_hash.cu) is
  * always built. The dense index is an array over the map's cell bounding box, 16 bytes per
- * cell {centroid, slot}, built when it takes at most 512 MiB: a lookup is one load. */
+ * cell {centroid, slot}, built when it takes at most 4 GiB (the 2 x 2 km map at 1 m takes
+ * 2.2 GiB): a lookup is one load. */
 #define NDT_CELL_INDEX_AUTO 0       /* dense index when it fits, else the hash */
 #define NDT_CELL_INDEX_HASH 1       /* hash probing only */
 
@@ -182,20 +183,25 @@ int ndt_map_info_get(ndt_ctx* ctx, ndt_map_info* out);
 /* Map tiles streamed in and out (the map module's tile loading and the dual matcher's
  * rebuild-and-swap, src/cuda_ndt_matcher/src/map_module.rs:192-360,
  * src/cuda_ndt_matcher/src/dual_ndt_manager.rs). Tiles (host points, uploaded once) stay in
- * device memory under a caller-chosen id; ndt_tile_put adds or replaces one,
- * ndt_tile_remove drops one. ndt_tiles_commit rebuilds the voxel map from the resident tiles
- * (concatenated on the device in put order) into a standby map, on the context's second
- * stream and a background host thread, while alignment calls keep using the active map.
- * The first alignment (or map query) call after the rebuild has finished switches to the
- * new map. wait = 1 waits for the rebuild and switches before returning. A failed rebuild
+ * device memory under a caller-chosen id; ndt_tile_put adds or replaces one, ndt_tile_remove
+ * drops one. The reference rebuilds its whole map from all points on every change; here the
+ * work per point happens once, when its tile is put: ndt_tile_put sorts the tile's points by
+ * cell and computes every cell's count and FP64 statistics. ndt_tiles_commit then merges the
+ * resident tiles' cells into a standby map (cells held by one tile keep its statistics; a cell
+ * shared by tiles is recomputed from all its points), on the context's second stream and a
+ * background host thread, while alignment calls keep using the active map. The result equals
+ * ndt_set_target of the tiles' points concatenated in put order (a replaced tile keeps its
+ * place). The first alignment (or map query) call after the merge has finished switches to
+ * the new map. wait = 1 waits for the merge and switches before returning. A failed merge
  * leaves the active map in place; ndt_tiles_status reports it. */
 int ndt_tile_put(ndt_ctx* ctx, uint64_t tile_id, const float* xyz, uint64_t num_points);
 int ndt_tile_remove(ndt_ctx* ctx, uint64_t tile_id);
 int ndt_tiles_commit(ndt_ctx* ctx, int32_t wait);
-/* pending: 1 while a rebuild runs; last_rc: result of the last finished rebuild;
- * build_ms: its device time. */
+/* pending: 1 while a merge runs; last_rc: result of the last finished merge; build_ms: its
+ * device time; put_ms: device time of the last ndt_tile_put's cell statistics. Any output
+ * pointer may be NULL. */
 int ndt_tiles_status(ndt_ctx* ctx, uint64_t* num_tiles, uint64_t* num_points, int32_t* pending,
-                     int32_t* last_rc, float* build_ms);
+                     int32_t* last_rc, float* build_ms, float* put_ms);
 /* VoxelGrid accessors (means_flat / inv_covariances_flat, voxel_grid/mod.rs:428-453):
  * valid voxels in ascending coordinate-Morton order; any output pointer may be NULL. */
 int ndt_map_voxels(ndt_ctx* ctx, int32_t* coords, float* means, float* covs, float* icovs,
@@ -382,12 +388,15 @@ int ndt_pnet_debug_grad(ndt_pnet* net, const float* x, const float* targets, uin
 int ndt_pnet_params(ndt_pnet* net, float* params, uint64_t* count, int32_t set);
 /* Learned initial-pose search on the context's target map (also added to the network as
  * map_id): proposals -> one alignment launch for all queries -> NVTL -> selection as in
- * ndt_initial_pose_search; queries whose best NVTL is below nvtl_threshold (2.3) rerun as
- * a plain particle search with `fallback`. used_fallback (optional): 1 per such query. */
+ * ndt_initial_pose_search. With refine (optional, num_particles > 0), a second round draws
+ * refine->num_particles particles around each query's winner (x, y +- xy_range, yaw +-
+ * yaw_range; guided ignored), aligns them in one launch and keeps the better winner. Queries
+ * whose best NVTL is then below nvtl_threshold (2.3) rerun as a plain particle search with
+ * `fallback` (optional). used_fallback (optional): 1 per such query. */
 int ndt_learned_pose_search(ndt_ctx* ctx, ndt_pnet* net, int32_t map_id, const ndt_scan* queries,
-                            uint64_t num_queries, double nvtl_threshold,
-                            const ndt_particle_config* fallback, ndt_pose_estimate* out,
-                            int32_t* used_fallback);
+                            uint64_t num_queries, const ndt_particle_config* refine,
+                            double nvtl_threshold, const ndt_particle_config* fallback,
+                            ndt_pose_estimate* out, int32_t* used_fallback);
 
 /* The network's GEMM: D[m x n] (f32, row-major) = A[m x k] B[n x k]^T with A, B bf16
  * row-major (device), k a multiple of 64; synchronous (checks the kernel's wait limits).
@@ -417,6 +426,14 @@ int ndt_profile_enable(ndt_ctx* ctx, int enable);
 int ndt_debug_trace(ndt_ctx* ctx, int enable);
 int ndt_debug_read(ndt_ctx* ctx, uint64_t index, double* out, int32_t max_records,
                    int32_t* num_records);
+
+/* Test hook for the work-queue kernel's no-progress limit (no counterpart in the reference,
+ * whose host loop synchronises after every kernel). A work-queue CTA that finds no chunk to
+ * claim while alignments are open gives up after limit_ns (default 2 s; 0 restores it) and
+ * the call returns NDT_ERR_DEVICE. With withhold_next = 1, the next work-queue launch starts
+ * with every chunk of every alignment already claimed, so no CTA finds work and the limit
+ * runs out: the error path can be tested without a fault. The context stays usable. */
+int ndt_debug_queue_stall(ndt_ctx* ctx, uint64_t limit_ns, int32_t withhold_next);
 
 const char* ndt_last_error_string(void);
 

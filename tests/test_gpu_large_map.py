@@ -1,6 +1,5 @@
 """Large-map voxel build at its stated size: the 2 x 2 km stress workload of 50M points (5%
-uniform outliers) at 1 m (the cell box exceeds the dense-index budget: hash lookups), 2 m and
-3 m (dense index).
+uniform outliers) at 1 m, 2 m and 3 m.
 
 Per resolution, against the map's own points (numpy, the membership rule of
 VoxelCoord::from_point, src/ndt_cuda/src/voxel_grid/types.rs:206-212, and
@@ -39,7 +38,7 @@ def test_large_map_voxels_full_size(gpu, oracle, big_map, res):
     ctx.set_target(big_map)
     info = ctx.map_info()
     assert info.num_points == N_POINTS
-    assert (info.dense_grid_mib > 0) == (res > 1.0)
+    assert info.dense_grid_mib > 0      # the dense cell index serves every resolution here
     coords, means, covs, icovs, counts = ctx.map_voxels()
     ctx.close()
     key = _key(np.floor(big_map / np.float32(res)))
@@ -95,7 +94,8 @@ def test_large_map_dense_scan_alignment(gpu, big_map):
 
 
 def test_large_map_1m_alignment_matches_oracle(gpu, oracle, big_map):
-    """1 m maps (hash lookups): the library's alignments of dense crop scans against the FP64
+    """1 m maps: the library's alignments of dense crop scans (dense cell index, and hash
+    lookups, bit-identical) against the FP64
     oracle's (graph semantics, the same voxels). A scan that misses the end-to-end bar
     (iterations equal, 1e-4 m, 1e-5 rad) must be one where the oracle parts from itself
     under a 1e-7 start perturbation, and pass the per-iteration check from every oracle
@@ -103,9 +103,17 @@ def test_large_map_1m_alignment_matches_oracle(gpu, oracle, big_map):
     iterations, 0.1 m step clamp, 1 m neighbour radius)."""
     ctx = capi.Context(resolution=1.0)
     ctx.set_target(big_map)
-    assert ctx.map_info().dense_grid_mib == 0
+    assert ctx.map_info().dense_grid_mib > 0
     poses, scans, guesses = _crop_scans(big_map, 4, 100_000, seed=11)
     got = ctx.align_batch(scans, guesses)
+    # the hash lookups give the same neighbours, hence the same results bit for bit
+    hctx = capi.Context(resolution=1.0, cell_index=1)
+    hctx.set_target(big_map)
+    assert hctx.map_info().dense_grid_mib == 0
+    for a, b in zip(got, hctx.align_batch(scans, guesses)):
+        np.testing.assert_array_equal(a["pose"], b["pose"])
+        assert a["iterations"] == b["iterations"] and a["nvtl"] == b["nvtl"]
+    hctx.close()
     # the oracle's grid over the part of the map the scans can reach (cells are absolute,
     # so the voxels there are the full map's)
     sel = np.zeros(len(big_map), bool)

@@ -92,6 +92,12 @@ def test_learned_proposals_gain_over_random_particles(gpu):
             c[5] = rng.uniform(-np.pi, np.pi)
             coarse.append(c)
         learned = ctx.learned_pose_search(net, mid, m.test_scans, coarse)
+        # the refinement round keeps the better of its winner and the proposals' winner
+        refined = ctx.learned_pose_search(
+            net, mid, m.test_scans, coarse,
+            refine=dict(num_particles=8, xy_range=0.5, yaw_range=np.radians(5.0), seed=5))
+        for a, b in zip(refined, learned):
+            assert a["selection_score"] >= b["selection_score"]
         rand = ctx.initial_pose_search(m.test_scans, coarse, num_particles=16, xy_range=5.0,
                                        yaw_range=np.pi, seed=9)
         ok_learned += sum(_success(e["pose"], t) for e, t in zip(learned, m.test_poses))

@@ -227,3 +227,28 @@ def test_queue_streamed_input_serialised(gpu):
         out[blocking] = json.loads(r.stdout.strip().splitlines()[-1])
     assert sum(len(s) for s in out["0"]) > 0
     assert out["0"] == out["1"]
+
+
+def test_queue_stall_limit_reports_and_recovers(gpu):
+    """The work-queue kernel's no-progress limit runs out without a fault: with every chunk
+    of the launch claimed up front (the test hook) no CTA finds work, the call returns
+    NDT_ERR_DEVICE with the stall message after the shortened limit, and the next call on the
+    same context aligns normally."""
+    import time
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=8, scan_points=3000)
+    scans = [seq.scan(k) for k in range(8)]
+    poses = [seq.guess(k) for k in range(8)]
+    ctx = capi.Context(work_queue=2)
+    ctx.set_target(seq.map)
+    want = ctx.align_batch(scans, poses)
+    ctx.debug_queue_stall(1_000_000, withhold_next=True)  # 1 ms
+    t0 = time.perf_counter()
+    with pytest.raises(capi.NdtError) as e:
+        ctx.align_batch(scans, poses)
+    assert time.perf_counter() - t0 < 5.0
+    assert e.value.code == -8 and "no work for 1 ms" in str(e.value)
+    ctx.debug_queue_stall(0)
+    got = ctx.align_batch(scans, poses)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a["pose"], b["pose"])
+        assert a["iterations"] == b["iterations"]
