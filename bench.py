@@ -43,6 +43,15 @@ NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
                      ("k_ndt_queue", 256, 5_000_000, 2): 109.4e6}
 
 
+def _json_default(o):
+    """numpy scalars and arrays in the result line as plain JSON numbers and lists."""
+    if isinstance(o, np.generic):
+        return o.item()
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    raise TypeError(f"{type(o).__name__} is not JSON serialisable")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -674,7 +683,7 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0},
         "reference_gpu_kernels": ref_gpu,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_json_default), flush=True)
 
 
 def reference_gpu_kernels(grid, scans, poses, n=64):
@@ -857,10 +866,14 @@ def run_ours(args):
         cpu = cpu_baseline((seq.map, 2.0), scans, poses, args.cpu_seconds)
     extra = {}
     if rank == 0 and args.extras:
-        extra["init_pose"] = init_pose_bench(5, args.cpu_seconds)
-        extra["queue"] = queue_bench(10)
-        extra["learned_init_pose"] = learned_bench()
-        extra["large_map"] = large_map_bench()
+        for key, fn in (("init_pose", lambda: init_pose_bench(5, args.cpu_seconds)),
+                        ("queue", lambda: queue_bench(10)),
+                        ("learned_init_pose", learned_bench),
+                        ("large_map", large_map_bench)):
+            try:
+                extra[key] = fn()
+            except Exception as e:  # one workload's failure must not lose the headline line
+                extra[key] = {"error": f"{type(e).__name__}: {e}"}
     elif rank == 0 and args.only:
         extra = run_only(args.only, args)
     kname = "k_ndt_queue" if tune["work_queue"] else "k_ndt_align"
@@ -918,7 +931,7 @@ def run_ours(args):
                          "p99_xy_err_m": float(np.percentile(perr, 99))},
         }
         line.update(extra)
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=_json_default), flush=True)
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -957,7 +970,7 @@ def run_only(names, args):
 def main():
     args = parse()
     if args.only and args.impl == "ours" and args.steps == 0:
-        print(json.dumps(run_only(args.only, args)), flush=True)
+        print(json.dumps(run_only(args.only, args), default=_json_default), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

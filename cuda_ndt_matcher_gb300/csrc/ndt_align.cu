@@ -696,6 +696,12 @@ __device__ __forceinline__ int search_point(const MapView& m, const uint32_t* of
 // (they change once per point; keeping them out of registers leaves the search and pair
 // work room without spilling to local memory)
 template <bool CPU_SEM>
+__device__ __forceinline__ void point_pairs(const MapView& m, const float* pv, const float* qh,
+                                            const float* ql, int cnt, const float* fr,
+                                            float d1f, float d2f, float* acc, float* sacc,
+                                            int& ncorr, const uint32_t* nbl, int nbl_stride);
+
+template <bool CPU_SEM>
 __device__ __forceinline__ void point_terms(const MapView& m, const uint32_t* off27,
                                             float px, float py, float pz,
                                             const float* fr, int max_nb, float d1f, float d2f,
@@ -706,6 +712,75 @@ __device__ __forceinline__ void point_terms(const MapView& m, const uint32_t* of
     transform_point(fr, pv, qh, ql);
     const int cnt = search_point(m, off27, qh, ql, max_nb, nbl, nbl_stride);
     if (cnt == 0) return;
+    point_pairs<CPU_SEM>(m, pv, qh, ql, cnt, fr, d1f, d2f, acc, sacc, ncorr, nbl, nbl_stride);
+}
+
+// Neighbour search of the points of a group of NPW lanes, the lanes sharing each point's
+// candidates (the dense index's occupied neighbour cells): for the group's points one after
+// another, lane j of the group tests the point's candidates of rank j, j + NPW, ... among
+// the mask's set bits, the group ORs the accepted bits, and the point's lane lists the first
+// max_nb accepted in ascending bit order (the reference's search order), so every list is
+// the one search_point gives. Each lane passes its own point (bits = 0 when it has none);
+// every lane of the warp takes part. Returns this lane's count.
+template <int NPW>
+__device__ __forceinline__ int search_group(const MapView& m, const uint32_t* off27,
+                                            const float* qh, const float* ql, uint32_t bits,
+                                            uint32_t corner, int max_nb, uint32_t* nbl,
+                                            int nbl_stride, int lane) {
+    const int g0 = lane & ~(NPW - 1), j = lane & (NPW - 1);
+    int my_cnt = 0;
+#pragma unroll 1
+    for (int k = 0; k < NPW; ++k) {
+        const int src = g0 + k;
+        const uint32_t bq = __shfl_sync(0xffffffffu, bits, src);
+        const uint32_t cq = __shfl_sync(0xffffffffu, corner, src);
+        float h[3], l[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            h[a] = __shfl_sync(0xffffffffu, qh[a], src);
+            l[a] = __shfl_sync(0xffffffffu, ql[a], src);
+        }
+        uint32_t rem = bq;
+#pragma unroll
+        for (int t = 0; t < NPW - 1; ++t)
+            if (t < j) rem &= rem - 1u;  // this lane starts at the set bit of rank j
+        uint32_t accm = 0u;
+#pragma unroll 1
+        while (rem != 0u) {
+            const uint32_t b = (uint32_t)(__ffs(rem) - 1);
+            const float4 e = __ldg(m.grid + (cq + off27[b]));
+            const float e0 = (h[0] - e.x) + l[0];
+            const float e1 = (h[1] - e.y) + l[1];
+            const float e2 = (h[2] - e.z) + l[2];
+            if (__float_as_int(e.w) >= 0 && !(fmaf(e0, e0, fmaf(e1, e1, e2 * e2)) > m.r2))
+                accm |= 1u << b;
+#pragma unroll
+            for (int t = 0; t < NPW; ++t) rem &= rem - 1u;  // the next candidate of this lane
+        }
+#pragma unroll
+        for (int o = 1; o < NPW; o <<= 1) accm |= __shfl_xor_sync(0xffffffffu, accm, o);
+        if (lane == src) {
+            // the point's lane lists its accepted voxels in order (slots re-read: L1 hits)
+            int c = 0;
+            uint32_t mm = accm;
+            while (mm != 0u && c < max_nb) {
+                const uint32_t b = (uint32_t)(__ffs(mm) - 1);
+                nbl[c * nbl_stride] = (uint32_t)__float_as_int(
+                    __ldg(reinterpret_cast<const float*>(m.grid + (cq + off27[b])) + 3));
+                mm &= mm - 1u;
+                ++c;
+            }
+            my_cnt = c;
+        }
+    }
+    return my_cnt;
+}
+
+template <bool CPU_SEM>
+__device__ __forceinline__ void point_pairs(const MapView& m, const float* pv, const float* qh,
+                                            const float* ql, int cnt, const float* fr,
+                                            float d1f, float d2f, float* acc, float* sacc,
+                                            int& ncorr, const uint32_t* nbl, int nbl_stride) {
     // ---- pairs: S, G, M aggregated over the listed voxels
     float S = 0.f, G0 = 0.f, G1 = 0.f, G2 = 0.f;
     float M0 = 0.f, M1 = 0.f, M2 = 0.f, M3 = 0.f, M4 = 0.f, M5 = 0.f;

@@ -167,39 +167,58 @@ __global__ void __launch_bounds__(BT) k_radix_hist(const uint64_t* __restrict__ 
     hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-// Each block re-reads its tile in rounds of 256 consecutive keys; a key's destination is
-// base[digit] (scanned histogram) + keys of the same digit in earlier warps of the round +
-// its rank among same-digit lanes of its warp, so the pass is stable.
+// Each block re-reads its tile in rounds of 256 consecutive keys and ranks every key stably
+// by digit (its rank among same-digit lanes of its warp, plus same-digit keys of earlier warps
+// of the round and of earlier rounds). The keys go first to shared memory, in digit order
+// within the tile, and then out to global memory in that order: the keys of one digit leave
+// as one contiguous run at base[digit] (the scanned histogram), so the stores coalesce.
+constexpr int SCATTER_SMEM = TILE * 12;  // keys (8 B) and values (4 B) of one tile
 __global__ void __launch_bounds__(BT) k_radix_scatter(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
     uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, size_t n, int shift,
     uint32_t dmask, const uint32_t* __restrict__ offs, uint32_t nb) {
-    __shared__ uint32_t base[256];
+    extern __shared__ __align__(16) unsigned char sc_smem[];
+    uint64_t* skey = reinterpret_cast<uint64_t*>(sc_smem);
+    uint32_t* sval = reinterpret_cast<uint32_t*>(sc_smem + TILE * 8);
+    __shared__ uint32_t base[256];   // global position of the tile's first key of each digit
+    __shared__ uint32_t loff[256];   // tile-local position of the first key of each digit
+    __shared__ uint32_t run[256];    // keys of each digit placed so far
     __shared__ uint32_t cnt[BT / 32][256];
+    __shared__ uint32_t ws[BT / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t tbase = (size_t)blockIdx.x * TILE;
+    const uint32_t tn = (uint32_t)min((size_t)TILE, n - tbase);
+    // the tile's digit counts -> tile-local digit offsets
+    run[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < tn; i += BT)
+        atomicAdd(&run[(uint32_t)(kin[tbase + i] >> shift) & dmask], 1u);
+    __syncthreads();
+    uint32_t tot;
+    loff[threadIdx.x] = block_exclusive_scan(run[threadIdx.x], ws, &tot);
     base[threadIdx.x] = offs[(size_t)threadIdx.x * nb + blockIdx.x];
+    run[threadIdx.x] = 0;
 #pragma unroll
     for (int w = 0; w < BT / 32; ++w) cnt[w][threadIdx.x] = 0;
     __syncthreads();
-    size_t tbase = (size_t)blockIdx.x * TILE;
     const uint32_t lt = (1u << lane) - 1u;
     for (int r = 0; r < ITEMS; ++r) {
-        size_t i = tbase + (size_t)r * BT + threadIdx.x;
-        bool valid = i < n;
-        uint64_t key = valid ? kin[i] : 0ull;
-        uint32_t val = valid ? vin[i] : 0u;
-        uint32_t d = valid ? ((uint32_t)(key >> shift) & dmask) : 256u;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        uint32_t rank = __popc(peers & lt);
-        int leader = __ffs(peers) - 1;
+        const uint32_t li = (uint32_t)r * BT + threadIdx.x;
+        const bool valid = li < tn;
+        const uint64_t key = valid ? kin[tbase + li] : 0ull;
+        const uint32_t val = valid ? vin[tbase + li] : 0u;
+        const uint32_t d = valid ? ((uint32_t)(key >> shift) & dmask) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt);
+        const int leader = __ffs(peers) - 1;
         if (valid && lane == leader) cnt[warp][d] = __popc(peers);
         __syncthreads();
         if (valid) {
             uint32_t pre = 0;
             for (int w = 0; w < warp; ++w) pre += cnt[w][d];
-            uint32_t pos = base[d] + pre + rank;
-            kout[pos] = key;
-            vout[pos] = val;
+            const uint32_t lp = loff[d] + run[d] + pre + rank;
+            skey[lp] = key;
+            sval[lp] = val;
         }
         __syncthreads();
         uint32_t add = 0;
@@ -208,8 +227,16 @@ __global__ void __launch_bounds__(BT) k_radix_scatter(
             add += cnt[w][threadIdx.x];
             cnt[w][threadIdx.x] = 0;
         }
-        base[threadIdx.x] += add;
+        run[threadIdx.x] += add;
         __syncthreads();
+    }
+    // out in tile-local digit order: consecutive threads write consecutive positions of a run
+    for (uint32_t i = threadIdx.x; i < tn; i += BT) {
+        const uint64_t key = skey[i];
+        const uint32_t d = (uint32_t)(key >> shift) & dmask;
+        const uint32_t pos = base[d] + (i - loff[d]);
+        kout[pos] = key;
+        vout[pos] = sval[i];
     }
 }
 
@@ -240,13 +267,18 @@ int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, in
     uint64_t* kout = kalt;
     uint32_t* vout = valt;
     int passes = 0;
+    // the scatter's tile staging exceeds the default dynamic shared-memory limit (set on the
+    // current device at every call: a host-side attribute, no allocation)
+    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         SCATTER_SMEM);
     for (int shift = begin_bit; shift < end_bit; shift += 8, ++passes) {
         int width = std::min(8, end_bit - shift);
         uint32_t dmask = (1u << width) - 1u;
         k_radix_hist<<<nb, BT, 0, s>>>(kin, n, shift, dmask, hist, nb);
         int rc = exclusive_scan(hist, hist, 256 * (size_t)nb, stemp, s);
         if (rc) return rc;
-        k_radix_scatter<<<nb, BT, 0, s>>>(kin, vin, kout, vout, n, shift, dmask, hist, nb);
+        k_radix_scatter<<<nb, BT, SCATTER_SMEM, s>>>(kin, vin, kout, vout, n, shift, dmask,
+                                                     hist, nb);
         int e = cuda_fail(cudaGetLastError(), "radix scatter launch");
         if (e) return e;
         std::swap(kin, kout);
