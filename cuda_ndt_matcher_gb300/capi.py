@@ -58,7 +58,8 @@ class Config(C.Structure):
                 ("threads_per_cta", C.c_int32), ("hash_capacity_factor", C.c_int32),
                 ("max_registers", C.c_int32), ("cell_index", C.c_int32),
                 ("cuda_graph", C.c_int32), ("use_line_search", C.c_int32),
-                ("work_queue", C.c_int32)]
+                ("work_queue", C.c_int32), ("lanes_per_point", C.c_int32),
+                ("stage_points", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -79,7 +80,8 @@ class TuneResult(C.Structure):
     _fields_ = [("cluster_size", C.c_int32), ("threads_per_cta", C.c_int32),
                 ("kernel_ms", C.c_double), ("aligns_per_s", C.c_double),
                 ("candidates", C.c_int32), ("registers", C.c_int32),
-                ("work_queue", C.c_int32), ("reserved", C.c_int32)]
+                ("work_queue", C.c_int32), ("lanes_per_point", C.c_int32),
+                ("stage_points", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ParticleConfig(C.Structure):
@@ -418,7 +420,8 @@ class Context:
         return {"cluster_size": r.cluster_size, "threads_per_cta": r.threads_per_cta,
                 "kernel_ms": r.kernel_ms, "aligns_per_s": r.aligns_per_s,
                 "candidates": r.candidates, "registers": r.registers,
-                "work_queue": r.work_queue}
+                "work_queue": r.work_queue, "lanes_per_point": r.lanes_per_point,
+                "stage_points": r.stage_points}
 
     def batch_timings(self, n):
         """Start / finish (ms, device clock) of each alignment of the last call."""

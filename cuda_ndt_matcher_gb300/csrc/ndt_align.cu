@@ -2003,7 +2003,7 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
     __syncwarp();
 }
 
-template <int THREADS, bool CPU_SEM, int REGCAP>
+template <int THREADS, bool CPU_SEM, int REGCAP, int NPW>
 __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     k_ndt_queue(const AlignParams P) {
     constexpr int NW = THREADS / 32;
@@ -2020,7 +2020,21 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     const uint32_t B = P.num_jobs;
     uint64_t idle_since = 0;    // thread 0
     uint32_t seen_arrive = 0;   // thread 0: last value of the input counter seen
-    if (tid == 0) s_lw = 0;
+    // the chunk's points, staged by one bulk copy (the TMA engine) into shared memory after
+    // the neighbour lists and accumulators: P.qchunk + 4 points (the copy starts on a 16-byte
+    // boundary, up to 3 points early)
+    __shared__ __align__(8) uint64_t s_stage_bar;
+    float* const stage =
+        reinterpret_cast<float*>(nbl_smem + (size_t)(P.max_nb + NACC - A_HTR) * THREADS);
+    uint32_t stage_phase = 0;
+    if (tid == 0) {
+        s_lw = 0;
+        if (P.qstage) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(&s_stage_bar)));
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+    }
     nbhd_offsets(m, s_off27);  // read after the loop's first barrier
     for (;;) {
         __syncthreads();  // the previous chunk (and controller) is finished with shared memory
@@ -2149,18 +2163,104 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
         const uint32_t csize = (jb.n + nchunks - 1u) / nchunks;  // this iteration's chunk size
         const uint32_t first = min(jb.n, chunk * csize);
         const uint32_t last = min(jb.n, first + csize);
+        // staged points: job-local indices below stage_end come from shared memory (point i
+        // at stage[3 (i - stage_first)]); the rest of the chunk (a ragged tail of less than
+        // 16 bytes, or every point when staging is off) from global memory
+        int64_t stage_first = 0, stage_end = 0;
+        if (P.qstage && last > first) {
+            const uint64_t g0 = (jb.offset + first) & ~3ull;  // 16-byte aligned point index
+            const uint64_t gend = jb.offset + last;
+            const uint32_t bytes = (uint32_t)(((gend - g0) * 12ull) & ~15ull);
+            if (bytes >= 16 && gend - g0 <= (uint64_t)P.qchunk + 4) {
+                const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_stage_bar);
+                if (tid == 0) {
+                    // the CTA's reads of the previous chunk (generic proxy) precede this write
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                                     bar),
+                                 "r"(bytes)
+                                 : "memory");
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                        "[%0], [%1], %2, [%3];" ::"r"((uint32_t)__cvta_generic_to_shared(stage)),
+                        "l"(P.pts + 3 * g0), "r"(bytes), "r"(bar)
+                        : "memory");
+                }
+                // bounded wait (1 s of the global timer); a copy from global memory that does
+                // not land means the device is in trouble: report it and stop this CTA
+                const uint64_t t0 = global_ns();
+                bool done = false;
+                while (!done) {
+                    uint32_t ok;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                        "selp.u32 %0, 1, 0, p;\n\t}"
+                        : "=r"(ok)
+                        : "r"(bar), "r"(stage_phase)
+                        : "memory");
+                    done = ok != 0;
+                    if (!done && global_ns() - t0 > 1000000000ull) break;
+                }
+                if (!__syncthreads_and(done ? 1 : 0)) {
+                    if (tid == 0) atomicOr(P.status, ST_STAGE_TIMEOUT);
+                    return;
+                }
+                stage_phase ^= 1u;
+                stage_first = (int64_t)g0 - (int64_t)jb.offset;
+                stage_end = stage_first + (int64_t)(bytes / 12u);
+            }
+        }
+        auto load_point = [&](uint32_t i, float* pv) {
+            if ((int64_t)i < stage_end) {
+                const float* q = stage + 3 * ((int64_t)i - stage_first);
+                pv[0] = q[0];
+                pv[1] = q[1];
+                pv[2] = q[2];
+            } else {
+                pv[0] = __ldg(pts + 3 * (size_t)i);
+                pv[1] = __ldg(pts + 3 * (size_t)i + 1);
+                pv[2] = __ldg(pts + 3 * (size_t)i + 2);
+            }
+        };
         float acc[NACC];
 #pragma unroll
         for (int i = 0; i < A_HTR; ++i) acc[i] = 0.f;
 #pragma unroll
         for (int k = 0; k < NACC - A_HTR; ++k) sacc[k * THREADS] = 0.f;
         int nc = 0;
-        for (uint32_t i = first + tid; i < last; i += THREADS) {
-            float px = __ldg(pts + 3 * (size_t)i), py = __ldg(pts + 3 * (size_t)i + 1),
-                  pz = __ldg(pts + 3 * (size_t)i + 2);
-            if (!(isfinite(px) && isfinite(py) && isfinite(pz))) continue;
-            point_terms<CPU_SEM>(m, s_off27, px, py, pz, sh.fr, P.max_nb, P.d1f, P.d2f, acc, sacc, nc,
-                                 nbl_smem + tid, THREADS);
+        if (NPW > 1 && m.grid) {
+            // groups of NPW lanes share each point's neighbour search (search_group); every
+            // lane of a warp runs every round, with or without a point of its own
+            for (uint32_t i0 = first; i0 < last; i0 += THREADS) {
+                const uint32_t i = i0 + tid;
+                float pv[3] = {0.f, 0.f, 0.f}, qh[3] = {0.f, 0.f, 0.f}, ql[3] = {0.f, 0.f, 0.f};
+                uint32_t bits = 0u, corner = 0u;
+                if (i < last) {
+                    load_point(i, pv);
+                    if (isfinite(pv[0]) && isfinite(pv[1]) && isfinite(pv[2])) {
+                        transform_point(sh.fr, pv, qh, ql);
+                        int32_t gc[3];
+                        cell_of_sum(m, qh, ql, gc);
+                        bits = nbhd_mask(m, gc, corner);
+                    }
+                }
+                const int cnt = search_group<NPW>(m, s_off27, qh, ql, bits, corner, P.max_nb,
+                                                  nbl_smem + tid, THREADS, lane);
+                __syncwarp();  // the group's list entries are visible to the point's lane
+                if (cnt > 0)
+                    point_pairs<CPU_SEM>(m, pv, qh, ql, cnt, sh.fr, P.d1f, P.d2f, acc, sacc, nc,
+                                         nbl_smem + tid, THREADS);
+                __syncwarp();  // lists are read before the next round rewrites them
+            }
+        } else {
+            for (uint32_t i = first + tid; i < last; i += THREADS) {
+                float pv[3];
+                load_point(i, pv);
+                if (!(isfinite(pv[0]) && isfinite(pv[1]) && isfinite(pv[2]))) continue;
+                point_terms<CPU_SEM>(m, s_off27, pv[0], pv[1], pv[2], sh.fr, P.max_nb, P.d1f,
+                                     P.d2f, acc, sacc, nc, nbl_smem + tid, THREADS);
+            }
         }
 #pragma unroll
         for (int k = 0; k < NACC - A_HTR; ++k) acc[A_HTR + k] = sacc[k * THREADS];
@@ -2210,15 +2310,15 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
     }
 }
 
-template <int T, bool SEM, int CAP>
+template <int T, bool SEM, int CAP, int NPW>
 static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t chunks,
                                   cudaStream_t s) {
-    auto kern = k_ndt_queue<T, SEM, CAP>;
+    auto kern = k_ndt_queue<T, SEM, CAP, NPW>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // persistent grid: every CTA resident (the kernel's CTAs never wait for each other, so
     // residency is a matter of speed only), at most one CTA per chunk of the batch
     static std::mutex mu;
-    static std::map<std::pair<int, size_t>, int> cache;  // (device, smem) -> CTAs
+    static std::map<std::pair<int, size_t>, int> cache;  // (device, smem) -> CTAs, per instance
     int dev = 0;
     cudaGetDevice(&dev);
     int ctas = 0;
@@ -2248,11 +2348,20 @@ static cudaError_t launch_queue_k(const AlignParams& p, size_t smem, uint32_t ch
 }
 
 template <int T, int CAP>
-static int launch_queue_t(const AlignParams& p, uint32_t chunks, cudaStream_t s) {
-    const size_t smem = (size_t)T * (p.max_nb + NACC - A_HTR) * sizeof(uint32_t);
-    const cudaError_t e = p.semantics == NDT_SEMANTICS_CPU
-                              ? launch_queue_k<T, true, CAP>(p, smem, chunks, s)
-                              : launch_queue_k<T, false, CAP>(p, smem, chunks, s);
+static int launch_queue_t(const AlignParams& p, uint32_t chunks, cudaStream_t s, int npw) {
+    // neighbour lists, trailing accumulators, then (staging) the chunk's points
+    const size_t smem = (size_t)T * (p.max_nb + NACC - A_HTR) * sizeof(uint32_t) +
+                        (p.qstage ? ((size_t)p.qchunk + 4) * 12 : 0);
+    cudaError_t e;
+    if (p.semantics == NDT_SEMANTICS_CPU) {
+        e = launch_queue_k<T, true, CAP, 1>(p, smem, chunks, s);
+    } else if (T == 256 && CAP == 64 && npw == 2) {
+        e = launch_queue_k<T, false, CAP, 2>(p, smem, chunks, s);
+    } else if (T == 256 && CAP == 64 && npw == 4) {
+        e = launch_queue_k<T, false, CAP, 4>(p, smem, chunks, s);
+    } else {
+        e = launch_queue_k<T, false, CAP, 1>(p, smem, chunks, s);
+    }
     return cuda_fail(e, "work-queue align launch");
 }
 
@@ -2307,12 +2416,21 @@ int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s) {
             return NDT_ERR_INVALID_ARGUMENT;
         }
         q.qchunk = shape.threads * shape.queue;
+        // staging needs a 16-byte aligned points buffer (the bulk copy's rule)
+        q.qstage = shape.stage > 0 && ((uintptr_t)p.pts & 15u) == 0 ? 1 : 0;
+        const int npw = shape.npw;
+        if (npw > 1 && !(shape.threads == 256 && R != 80 && (npw == 2 || npw == 4) &&
+                         p.semantics != NDT_SEMANTICS_CPU)) {
+            set_error("lanes per point 2 or 4 are built for the graph semantics' 256-thread, "
+                      "64-register work-queue kernel");
+            return NDT_ERR_INVALID_ARGUMENT;
+        }
         switch (shape.threads) {
-            case 128: return launch_queue_t<128, 64>(q, p.qchunks_total, s);
+            case 128: return launch_queue_t<128, 64>(q, p.qchunks_total, s, 1);
             case 256:
-                return R == 80 ? launch_queue_t<256, 80>(q, p.qchunks_total, s)
-                               : launch_queue_t<256, 64>(q, p.qchunks_total, s);
-            case 512: return launch_queue_t<512, 128>(q, p.qchunks_total, s);
+                return R == 80 ? launch_queue_t<256, 80>(q, p.qchunks_total, s, 1)
+                               : launch_queue_t<256, 64>(q, p.qchunks_total, s, npw);
+            case 512: return launch_queue_t<512, 128>(q, p.qchunks_total, s, 1);
             default:
                 set_error("threads per CTA must be 128, 256 or 512");
                 return NDT_ERR_INVALID_ARGUMENT;

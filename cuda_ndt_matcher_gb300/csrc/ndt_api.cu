@@ -420,7 +420,12 @@ static bool config_ok(const ndt_config& c) {
            c.work_queue >= -1 && c.work_queue <= 16 &&
            (c.work_queue <= 0 || (T != 128 || R == 0 || R == 64)) &&
            (c.work_queue <= 0 || (T != 512 || R == 0 || R == 128)) &&
-           (c.work_queue <= 0 || (T != 256 || R == 0 || R == 64 || R == 80));
+           (c.work_queue <= 0 || (T != 256 || R == 0 || R == 64 || R == 80)) &&
+           (c.lanes_per_point == 0 || c.lanes_per_point == 1 ||
+            ((c.lanes_per_point == 2 || c.lanes_per_point == 4) &&
+             c.semantics == NDT_SEMANTICS_GPU_GRAPH && (T == 0 || T == 256) &&
+             (R == 0 || R == 64))) &&
+           (c.stage_points == 0 || c.stage_points == 1);
 }
 
 extern "C" {
@@ -864,6 +869,8 @@ static LaunchShape choose_shape(ndt_ctx* c, uint32_t jobs, uint32_t max_n) {
         sh.threads = c->cfg.threads_per_cta > 0 ? c->cfg.threads_per_cta : 256;
         sh.regcap = c->cfg.max_registers > 0 ? c->cfg.max_registers : (sh.threads == 512 ? 128 : 64);
         sh.queue = c->cfg.work_queue;
+        sh.npw = c->cfg.lanes_per_point > 1 ? c->cfg.lanes_per_point : 1;
+        sh.stage = c->cfg.stage_points > 0 ? 1 : 0;
         return sh;
     }
     auto it = c->tuned.find({log2_bucket(jobs), log2_bucket(max_n)});
@@ -1065,7 +1072,8 @@ static int run_align_enqueue(ndt_ctx* c, const float* d_pts, std::vector<AlignJo
     if (c->cfg.cuda_graph && !c->trace && !stream_in) {
         const std::vector<uint64_t> key = {
             nj, max_n, (uint64_t)shape.cluster, (uint64_t)shape.threads, (uint64_t)shape.regcap,
-            (uint64_t)shape.queue, (uint64_t)(uintptr_t)c->d_qjobs.p,
+            (uint64_t)shape.queue, (uint64_t)shape.npw, (uint64_t)shape.stage,
+            (uint64_t)(uintptr_t)c->d_qjobs.p,
             (uint64_t)(uintptr_t)c->d_qctl.p, (uint64_t)(uintptr_t)c->d_qframe.p,
             (uint64_t)(uintptr_t)c->d_qpart.p, (uint64_t)(uintptr_t)c->d_qoff.p,
             c->map_gen, c->cfg_gen, (uint64_t)(uintptr_t)d_pts, (uint64_t)(uintptr_t)c->d_jobs.p,
@@ -1854,16 +1862,23 @@ int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const 
     const int Ks[4] = {1, 2, 4, 8};
     const int TC[8][2] = {{128, 128}, {128, 80}, {128, 64}, {256, 128},
                           {256, 80},  {256, 64}, {256, 48}, {512, 128}};
-    // work-queue candidates: (threads, registers, points per thread per chunk)
-    const int QC[6][3] = {{256, 64, 2}, {256, 64, 4}, {256, 64, 8},
-                          {256, 80, 4}, {128, 64, 4}, {512, 128, 2}};
+    // work-queue candidates: (threads, registers, points per thread per chunk, lanes sharing
+    // each point's neighbour search, chunk points staged in shared memory)
+    const int QC[14][5] = {{256, 64, 2, 1, 0}, {256, 64, 4, 1, 0}, {256, 64, 8, 1, 0},
+                           {256, 80, 4, 1, 0}, {128, 64, 4, 1, 0}, {512, 128, 2, 1, 0},
+                           {256, 64, 4, 2, 0}, {256, 64, 4, 4, 0}, {256, 64, 8, 4, 0},
+                           {256, 64, 2, 1, 1}, {256, 64, 4, 1, 1}, {256, 64, 8, 1, 1},
+                           {256, 64, 4, 2, 1}, {256, 64, 4, 4, 1}};
+    const bool graph_sem = c->cfg.semantics != NDT_SEMANTICS_CPU;
     const bool ls = c->cfg.use_line_search != 0;
     std::vector<LaunchShape> cands;
     if (c->cfg.work_queue <= 0 || ls)
         for (int K : Ks)
             for (const auto& tc : TC) cands.push_back(LaunchShape{K, tc[0], tc[1], 0});
     if (c->cfg.work_queue >= 0 && !ls)
-        for (const auto& qc : QC) cands.push_back(LaunchShape{1, qc[0], qc[1], qc[2]});
+        for (const auto& qc : QC)
+            if (qc[3] == 1 || graph_sem)
+                cands.push_back(LaunchShape{1, qc[0], qc[1], qc[2], qc[3], qc[4]});
     LaunchShape best{0, 0, 128, 0};
     double best_ms = 1e300;
     int tried = 0;
@@ -1890,6 +1905,8 @@ int ndt_autotune(ndt_ctx* c, const float* d_xyz, const uint64_t* offsets, const 
     out->threads_per_cta = best.threads;
     out->registers = best.regcap;
     out->work_queue = best.queue;
+    out->lanes_per_point = best.queue > 0 ? std::max(1, best.npw) : 0;
+    out->stage_points = best.queue > 0 ? best.stage : 0;
     out->reserved = 0;
     out->kernel_ms = best_ms;
     out->aligns_per_s = best_ms > 0 ? 1000.0 * (double)m / best_ms : 0.0;

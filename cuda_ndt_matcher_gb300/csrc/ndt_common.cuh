@@ -27,6 +27,7 @@ constexpr uint32_t ST_HASH_FULL = 1u << 0;
 constexpr uint32_t ST_PROBE_LIMIT = 1u << 1;
 constexpr uint32_t ST_BAD_INPUT = 1u << 2;
 constexpr uint32_t ST_QUEUE_STALL = 1u << 3;  // work-queue kernel found no progress for 2 s
+constexpr uint32_t ST_STAGE_TIMEOUT = 1u << 4;  // a point-staging bulk copy did not land in 1 s
 
 struct MapView {
     const uint4* slots;

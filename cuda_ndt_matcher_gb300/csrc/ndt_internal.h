@@ -205,6 +205,9 @@ struct AlignParams {
     // withhold, every chunk starts out claimed (a test hook: no CTA finds work)
     uint64_t stall_ns;
     int32_t withhold;
+    // work-queue kernel: each chunk's points staged into shared memory by one bulk copy
+    // (needs the points' buffer 16-byte aligned)
+    int32_t qstage;
 };
 constexpr unsigned long long QSTARVE_NS = 2000000ull;
 constexpr unsigned long long QSTALL_NS = 2000000000ull;
@@ -262,6 +265,8 @@ struct LaunchShape {
     int threads;
     int regcap;  // 128 (default); 80, 64, 48: denser residency for 128/256-thread CTAs
     int queue;   // > 0: work-queue kernel, chunks of `queue` points per thread (cluster 1)
+    int npw;     // work-queue kernel: lanes sharing each point's neighbour search (0, 1: one)
+    int stage;   // work-queue kernel: 1 stages each chunk's points in shared memory (bulk copy)
 };
 
 int launch_align(const AlignParams& p, LaunchShape shape, cudaStream_t s);

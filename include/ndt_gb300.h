@@ -94,6 +94,14 @@ typedef struct ndt_config {
                                       cluster per alignment; 0 autotuned (cluster kernel
                                       until tuned). Line search always uses the cluster
                                       kernel. */
+    int32_t lanes_per_point;       /* work-queue kernel, graph semantics, 256 threads at 64
+                                      registers: 2 or 4 lanes share each point's neighbour
+                                      search (the occupied cells among its 27); 0 or 1: each
+                                      lane searches its own point. The autotuner chooses it. */
+    int32_t stage_points;          /* work-queue kernel: 1 stages each chunk's points in shared
+                                      memory with one bulk copy (the TMA engine) before the
+                                      chunk's work; 0 reads them from global memory. The
+                                      autotuner chooses it. */
 } ndt_config;
 
 /* AlignResult (src/ndt_cuda/src/ndt.rs:219-248) with the pose as a vector. */
@@ -240,7 +248,8 @@ int ndt_align_batch_device(ndt_ctx* ctx, const float* d_xyz, const uint64_t* off
 
 /* Autotuner for the Newton kernel's launch shape: times the cluster kernel at every
  * (cluster size 1, 2, 4, 8) x (threads per CTA, register cap) candidate and the work-queue
- * kernel at its (threads, registers, points per thread per chunk) candidates (unless the
+ * kernel at its (threads, registers, points per thread per chunk, lanes per point's neighbour
+ * search) candidates (unless the
  * configuration fixes the form, or line search is on) on the given device-resident batch
  * (as ndt_align_batch_device takes it), `repeats` timed runs each, and records the fastest
  * for batches of this size class (log2 of the scan count and of the largest scan). Later
@@ -255,6 +264,10 @@ typedef struct ndt_tune_result {
     int32_t registers;             /* register cap of the winning kernel instance */
     int32_t work_queue;            /* points per thread per chunk of the winner if it is the
                                       work-queue kernel, else 0 */
+    int32_t lanes_per_point;       /* lanes sharing each point's neighbour search in the
+                                      winning work-queue kernel (1, 2, 4), else 0 */
+    int32_t stage_points;          /* 1 when the winning work-queue kernel stages its chunks'
+                                      points in shared memory */
     int32_t reserved;
 } ndt_tune_result;
 int ndt_autotune(ndt_ctx* ctx, const float* d_xyz, const uint64_t* offsets,

@@ -144,7 +144,8 @@ def test_queue_autotune_and_forms(gpu):
         ctx.set_target(seq.map)
         r = ctx.autotune(xyz.data_ptr(), offsets, poses, repeats=1)
         assert allowed(r["work_queue"])
-        assert r["candidates"] == {1: 6, -1: 32, 0: 38}[form]
+        assert r["candidates"] == {1: 14, -1: 32, 0: 46}[form]
+        assert (r["lanes_per_point"] in (1, 2, 4)) == (r["work_queue"] > 0)
         res = ctx.align_batch(scans, list(poses))
         assert all(np.isfinite(x["pose"]).all() for x in res)
     # line search keeps the cluster kernel whatever the form says
@@ -252,3 +253,31 @@ def test_queue_stall_limit_reports_and_recovers(gpu):
     for a, b in zip(got, want):
         np.testing.assert_array_equal(a["pose"], b["pose"])
         assert a["iterations"] == b["iterations"]
+
+
+@pytest.mark.parametrize("lanes", [2, 4])
+def test_queue_lanes_per_point(gpu, oracle, single_cases, lanes):
+    """Groups of 2 or 4 lanes sharing each point's neighbour search list the same voxels in
+    the same order as one lane per point: the batch's results equal the one-lane kernel's
+    (same chunks and per-point arithmetic), and single alignments meet the oracle bar."""
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=24, scan_points=0)
+    scans = [seq.scan(k) for k in range(0, 24, 2)]
+    poses = [seq.guess(k) for k in range(0, 24, 2)]
+    one = capi.Context(work_queue=4, threads_per_cta=256, max_registers=64)
+    grp = capi.Context(work_queue=4, threads_per_cta=256, max_registers=64,
+                       lanes_per_point=lanes)
+    for c in (one, grp):
+        c.set_target(seq.map)
+    a = one.align_batch(scans, poses)
+    b = grp.align_batch(scans, poses)
+    for x, y in zip(a, b):
+        assert x["iterations"] == y["iterations"]
+        assert np.abs(x["pose"] - y["pose"]).max() <= 1e-9, np.abs(x["pose"] - y["pose"]).max()
+        assert x["num_correspondences"] == y["num_correspondences"]
+    for i, case in enumerate(single_cases):
+        ctx = capi.Context(work_queue=4, threads_per_cta=256, max_registers=64,
+                           lanes_per_point=lanes)
+        ctx.set_target(case.map_points)
+        got = ctx.align(case.scan, case.guess)
+        want = oracle.Grid(case.map_points, 2.0).align(case.scan, case.guess, semantics="gpu")
+        assert_parity(got, want, f"case {i} lanes={lanes}")
