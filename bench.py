@@ -284,7 +284,7 @@ def _pose_ok(pose, truth):
     return np.linalg.norm(pose[:2] - truth[:2]) < 0.2 and abs(dyaw) < np.radians(1.0)
 
 
-def learned_bench(steps=20000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01):
+def learned_bench(steps=60000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01):
     """Learned initial-pose proposals vs the plain 200-particle search.
 
     Training: n_maps seeded 200x200 m maps of the sequence generator with n_train scans each;

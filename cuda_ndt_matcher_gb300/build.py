@@ -60,9 +60,6 @@ def build_cuda(force=False, verbose=False):
         if force or _newer(obj, [src] + deps_common):
             cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                    "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
-            if s == "voxel_build.cu":
-                # one IEEE rounding per operation: statistics match the CPU evaluation bit for bit
-                cmd.insert(1, "-fmad=false")
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

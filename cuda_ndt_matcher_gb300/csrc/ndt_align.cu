@@ -810,12 +810,14 @@ __device__ __forceinline__ void point_pairs(const MapView& m, const float* pv, c
         G0 = fmaf(w, c0, G0);
         G1 = fmaf(w, c1, G1);
         G2 = fmaf(w, c2, G2);
-        M0 += fmaf(w, ca.x, -wd * c0 * c0);
-        M1 += fmaf(w, ca.y, -wd * c0 * c1);
-        M2 += fmaf(w, ca.z, -wd * c0 * c2);
-        M3 += fmaf(w, ca.w, -wd * c1 * c1);
-        M4 += fmaf(w, cb.x, -wd * c1 * c2);
-        M5 += fmaf(w, cb.y, -wd * c2 * c2);
+        // M += w C - wd c c^T, as two multiply-adds per entry
+        const float u0 = wd * c0, u1 = wd * c1, u2 = wd * c2;
+        M0 = fmaf(-u0, c0, fmaf(w, ca.x, M0));
+        M1 = fmaf(-u0, c1, fmaf(w, ca.y, M1));
+        M2 = fmaf(-u0, c2, fmaf(w, ca.z, M2));
+        M3 = fmaf(-u1, c1, fmaf(w, ca.w, M3));
+        M4 = fmaf(-u1, c2, fmaf(w, cb.x, M4));
+        M5 = fmaf(-u2, c2, fmaf(w, cb.y, M5));
     }
     if (cnt == 0) return;
     ncorr += cnt;

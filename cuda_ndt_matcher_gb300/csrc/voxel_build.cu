@@ -12,19 +12,20 @@
 //                            (replaces cub::DeviceRadixSort, src/cuda_ffi/csrc/radix_sort.cu).
 //   4. segments            : boundary flags + exclusive scan -> segment id / start
 //                            (src/cuda_ffi/csrc/segment_detect.cu:27-146).
-//   5. voxel statistics    : one thread per segment, FP64 two-pass centred moments over the
-//                            segment's points in input order; eigenvector directions by an
-//                            f32 Jacobi, refined in FP64 (orthonormalisation, one or two
-//                            Jacobi sweeps); regularisation to the min-ratio and inverse in
-//                            FP64, f32 outputs
-//                            (Voxel::from_statistics / regularize_covariance,
+//   5. voxel statistics    : one thread per segment (one warp per segment of 48 points or
+//                            more), exact integer moments of the segment's points (the FP64
+//                            running sum's mean bit for bit, the centred covariance from an
+//                            exact numerator), FP64 two-pass moments where the exact bounds
+//                            do not hold; eigenvector directions by an f32 Jacobi, refined
+//                            in FP64; regularisation to the min-ratio and inverse in FP64,
+//                            f32 outputs (Voxel::from_statistics / regularize_covariance,
 //                            src/ndt_cuda/src/voxel_grid/types.rs:54-190).
 //   6. compaction          : valid voxels keep their Morton order.
 //   7. hash insert         : bounded linear probing with atomicCAS, displacement recorded
 //                            (voxel_hash_build_kernel, src/cuda_ffi/csrc/voxel_hash.cu:69-114).
-// This translation unit is compiled with -fmad=false: every FP64/FP32 operation is one IEEE
-// rounding, so the moments (counts, means, unregularised covariances) match a CPU evaluation
-// of the same operation sequence bit for bit.
+// Bit-exact parts (cells, keys, counts, means) use no multiply-add: cells are an f32 division,
+// means an FP64 division of an exact sum (or a running sum of adds), so FMA contraction
+// cannot change them; the regularised covariances, compared in f32 ULPs, use FMAs freely.
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -149,146 +150,201 @@ static int exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, void* tem
 }
 
 // ---------------------------------------------------------------------------------------
-// Stable LSD radix sort of (u64 key, u32 value), 8-bit digits.
+// Stable LSD radix sort of (key, u32 value) pairs, 8-bit digits; keys u64 or, when the
+// significant bits fit, u32 (half the key traffic per pass).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(BT) k_radix_hist(const uint64_t* __restrict__ keys, size_t n,
+// Digit counts of each TILE-key tile: shared-memory atomics into one counter set per warp
+// (keys of one digit then queue only within their warp), summed per digit at the end.
+template <typename K>
+__global__ void __launch_bounds__(BT) k_radix_hist(const K* __restrict__ keys, size_t n,
                                                    int shift, uint32_t dmask,
                                                    uint32_t* __restrict__ hist, uint32_t nb) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    __shared__ uint32_t h[BT / 32][256];
+#pragma unroll
+    for (int w = 0; w < BT / 32; ++w) h[w][threadIdx.x] = 0;
     __syncthreads();
-    size_t base = (size_t)blockIdx.x * TILE;
-#pragma unroll 4
+    uint32_t* const hw = h[threadIdx.x >> 5];
+    const size_t base = (size_t)blockIdx.x * TILE;
+    K kv[ITEMS];
+#pragma unroll
     for (int r = 0; r < ITEMS; ++r) {
-        size_t i = base + (size_t)r * BT + threadIdx.x;
-        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & dmask], 1u);
+        const size_t i = base + (size_t)r * BT + threadIdx.x;
+        kv[r] = i < n ? keys[i] : K(0);
     }
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r)
+        if (base + (size_t)r * BT + threadIdx.x < n)
+            atomicAdd(&hw[(uint32_t)(kv[r] >> shift) & dmask], 1u);
     __syncthreads();
-    hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < BT / 32; ++w) c += h[w][threadIdx.x];
+    hist[(size_t)threadIdx.x * nb + blockIdx.x] = c;
 }
 
-// Each block re-reads its tile in rounds of 256 consecutive keys and ranks every key stably
-// by digit (its rank among same-digit lanes of its warp, plus same-digit keys of earlier warps
-// of the round and of earlier rounds). The keys go first to shared memory, in digit order
-// within the tile, and then out to global memory in that order: the keys of one digit leave
-// as one contiguous run at base[digit] (the scanned histogram), so the stores coalesce.
-constexpr int SCATTER_SMEM = TILE * 12;  // keys (8 B) and values (4 B) of one tile
-__global__ void __launch_bounds__(BT) k_radix_scatter(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-    uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, size_t n, int shift,
-    uint32_t dmask, const uint32_t* __restrict__ offs, uint32_t nb) {
+// Lanes of the warp whose 9-bit value d (an 8-bit digit, or 0x100 for no key) equals this
+// lane's: one ballot per bit, each narrowing the set to the lanes that agree on that bit.
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
+    uint32_t m = 0xffffffffu;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const bool bit = (d >> k) & 1u;
+        const uint32_t b = __ballot_sync(0xffffffffu, bit);
+        m &= bit ? b : ~b;
+    }
+    return m;
+}
+
+// One block per TILE-key tile. Warp w owns the tile's keys [w * 512, (w + 1) * 512), held in
+// registers as 16 rounds of 32. Pass 1: each warp counts its digits into its own counters
+// (same-digit lanes found by digit_peers). Then per digit: the tile-local start (block
+// scan) plus the counts of the earlier warps give each warp's first position. Pass 2: each
+// key goes to shared memory at its warp's running position of its digit plus its rank among
+// the round's same-digit lanes: tile order within each digit, so the sort is stable. Last, the
+// keys leave in that order: the keys of one digit as one contiguous run at base[digit] (the
+// scanned histogram), so the stores coalesce.
+template <typename K>
+__global__ void __launch_bounds__(BT, sizeof(K) == 4 ? 4 : 3) k_radix_scatter(
+    const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
+    uint32_t* __restrict__ vout, size_t n, int shift, uint32_t dmask,
+    const uint32_t* __restrict__ offs, uint32_t nb) {
+    constexpr int NWARP = BT / 32;
+    constexpr int WROUNDS = TILE / BT;  // rounds of 32 keys per warp
     extern __shared__ __align__(16) unsigned char sc_smem[];
-    uint64_t* skey = reinterpret_cast<uint64_t*>(sc_smem);
-    uint32_t* sval = reinterpret_cast<uint32_t*>(sc_smem + TILE * 8);
-    __shared__ uint32_t base[256];   // global position of the tile's first key of each digit
-    __shared__ uint32_t loff[256];   // tile-local position of the first key of each digit
-    __shared__ uint32_t run[256];    // keys of each digit placed so far
-    __shared__ uint32_t cnt[BT / 32][256];
-    __shared__ uint32_t ws[BT / 32];
+    K* skey = reinterpret_cast<K*>(sc_smem);
+    uint32_t* sval = reinterpret_cast<uint32_t*>(sc_smem + TILE * sizeof(K));
+    __shared__ uint32_t wpos[NWARP][256];  // per warp: digit counts, then running positions
+    __shared__ uint32_t base[256];         // global position of the tile's first key of each digit
+    __shared__ uint32_t loff[256];         // tile-local position of the first key of each digit
+    __shared__ uint32_t ws[NWARP];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t tbase = (size_t)blockIdx.x * TILE;
     const uint32_t tn = (uint32_t)min((size_t)TILE, n - tbase);
-    // the tile's digit counts -> tile-local digit offsets
-    run[threadIdx.x] = 0;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < tn; i += BT)
-        atomicAdd(&run[(uint32_t)(kin[tbase + i] >> shift) & dmask], 1u);
-    __syncthreads();
-    uint32_t tot;
-    loff[threadIdx.x] = block_exclusive_scan(run[threadIdx.x], ws, &tot);
-    base[threadIdx.x] = offs[(size_t)threadIdx.x * nb + blockIdx.x];
-    run[threadIdx.x] = 0;
+    const uint32_t wbase = (uint32_t)warp * (WROUNDS * 32);
 #pragma unroll
-    for (int w = 0; w < BT / 32; ++w) cnt[w][threadIdx.x] = 0;
+    for (int w = 0; w < NWARP; ++w) wpos[w][threadIdx.x] = 0;
+    __syncthreads();
+    K key[WROUNDS];
+#pragma unroll
+    for (int r = 0; r < WROUNDS; ++r) {
+        const uint32_t li = wbase + (uint32_t)r * 32 + lane;
+        key[r] = li < tn ? kin[tbase + li] : K(0);
+    }
+#pragma unroll
+    for (int r = 0; r < WROUNDS; ++r) {
+        const uint32_t li = wbase + (uint32_t)r * 32 + lane;
+        const uint32_t d = li < tn ? ((uint32_t)(key[r] >> shift) & dmask) : 0x100u;
+        const uint32_t peers = digit_peers(d);
+        if (d != 0x100u && lane == __ffs(peers) - 1) wpos[warp][d] += (uint32_t)__popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x;  // one thread per digit (BT == 256)
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < NWARP; ++w) {
+            const uint32_t c = wpos[w][d];
+            wpos[w][d] = run;
+            run += c;
+        }
+        uint32_t tot;
+        const uint32_t lo = block_exclusive_scan(run, ws, &tot);
+        loff[d] = lo;
+#pragma unroll
+        for (int w = 0; w < NWARP; ++w) wpos[w][d] += lo;
+        base[d] = offs[(size_t)d * nb + blockIdx.x];
+    }
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
-    for (int r = 0; r < ITEMS; ++r) {
-        const uint32_t li = (uint32_t)r * BT + threadIdx.x;
-        const bool valid = li < tn;
-        const uint64_t key = valid ? kin[tbase + li] : 0ull;
-        const uint32_t val = valid ? vin[tbase + li] : 0u;
-        const uint32_t d = valid ? ((uint32_t)(key >> shift) & dmask) : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
-        const uint32_t rank = __popc(peers & lt);
-        const int leader = __ffs(peers) - 1;
-        if (valid && lane == leader) cnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t pre = 0;
-            for (int w = 0; w < warp; ++w) pre += cnt[w][d];
-            const uint32_t lp = loff[d] + run[d] + pre + rank;
-            skey[lp] = key;
-            sval[lp] = val;
-        }
-        __syncthreads();
-        uint32_t add = 0;
 #pragma unroll
-        for (int w = 0; w < BT / 32; ++w) {
-            add += cnt[w][threadIdx.x];
-            cnt[w][threadIdx.x] = 0;
+    for (int r = 0; r < WROUNDS; ++r) {
+        const uint32_t li = wbase + (uint32_t)r * 32 + lane;
+        const bool valid = li < tn;
+        const uint32_t d = valid ? ((uint32_t)(key[r] >> shift) & dmask) : 0x100u;
+        const uint32_t peers = digit_peers(d);
+        if (valid) {
+            const uint32_t pos = wpos[warp][d] + (uint32_t)__popc(peers & lt);
+            skey[pos] = key[r];
+            sval[pos] = vin[tbase + li];
         }
-        run[threadIdx.x] += add;
-        __syncthreads();
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wpos[warp][d] += (uint32_t)__popc(peers);
+        __syncwarp();
     }
-    // out in tile-local digit order: consecutive threads write consecutive positions of a run
+    __syncthreads();
     for (uint32_t i = threadIdx.x; i < tn; i += BT) {
-        const uint64_t key = skey[i];
-        const uint32_t d = (uint32_t)(key >> shift) & dmask;
+        const K k = skey[i];
+        const uint32_t d = (uint32_t)(k >> shift) & dmask;
         const uint32_t pos = base[d] + (i - loff[d]);
-        kout[pos] = key;
+        kout[pos] = k;
         vout[pos] = sval[i];
     }
 }
 
-size_t radix_sort_temp_bytes(size_t n) {
+template <typename K>
+static size_t radix_temp_bytes(size_t n) {
     size_t nb = ntiles(n);
-    return align_up(n * 8, 256) + align_up(n * 4, 256) + align_up(256 * nb * 4, 256) +
+    return align_up(n * sizeof(K), 256) + align_up(n * 4, 256) + align_up(256 * nb * 4, 256) +
            scan_temp_bytes(256 * nb);
 }
 
-int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
-                     void* temp, size_t temp_bytes, cudaStream_t s) {
+size_t radix_sort_temp_bytes(size_t n) { return radix_temp_bytes<uint64_t>(n); }
+size_t radix_sort_temp_bytes32(size_t n) { return radix_temp_bytes<uint32_t>(n); }
+
+template <typename K>
+static int radix_sort_t(K* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
+                        void* temp, size_t temp_bytes, cudaStream_t s) {
     if (n <= 1 || end_bit <= begin_bit) return 0;
-    if (temp_bytes < radix_sort_temp_bytes(n)) {
+    if (temp_bytes < radix_temp_bytes<K>(n)) {
         set_error("radix sort: temporary storage too small");
         return NDT_ERR_INVALID_ARGUMENT;
     }
     uint32_t nb = ntiles(n);
     char* t = (char*)temp;
-    uint64_t* kalt = (uint64_t*)t;
-    t += align_up(n * 8, 256);
+    K* kalt = (K*)t;
+    t += align_up(n * sizeof(K), 256);
     uint32_t* valt = (uint32_t*)t;
     t += align_up(n * 4, 256);
     uint32_t* hist = (uint32_t*)t;
     t += align_up(256 * (size_t)nb * 4, 256);
     void* stemp = t;
-    uint64_t* kin = keys;
+    K* kin = keys;
     uint32_t* vin = vals;
-    uint64_t* kout = kalt;
+    K* kout = kalt;
     uint32_t* vout = valt;
     int passes = 0;
-    // the scatter's tile staging exceeds the default dynamic shared-memory limit (set on the
-    // current device at every call: a host-side attribute, no allocation)
-    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         SCATTER_SMEM);
+    // the scatter's tile staging may exceed the default dynamic shared-memory limit (set on
+    // the current device at every call: a host-side attribute, no allocation)
+    constexpr int smem = TILE * (int)(sizeof(K) + 4);
+    cudaFuncSetAttribute(k_radix_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     for (int shift = begin_bit; shift < end_bit; shift += 8, ++passes) {
         int width = std::min(8, end_bit - shift);
         uint32_t dmask = (1u << width) - 1u;
-        k_radix_hist<<<nb, BT, 0, s>>>(kin, n, shift, dmask, hist, nb);
+        k_radix_hist<K><<<nb, BT, 0, s>>>(kin, n, shift, dmask, hist, nb);
         int rc = exclusive_scan(hist, hist, 256 * (size_t)nb, stemp, s);
         if (rc) return rc;
-        k_radix_scatter<<<nb, BT, SCATTER_SMEM, s>>>(kin, vin, kout, vout, n, shift, dmask,
-                                                     hist, nb);
+        k_radix_scatter<K><<<nb, BT, smem, s>>>(kin, vin, kout, vout, n, shift, dmask, hist, nb);
         int e = cuda_fail(cudaGetLastError(), "radix scatter launch");
         if (e) return e;
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
     if (passes & 1) {
-        cudaMemcpyAsync(keys, kin, n * 8, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(keys, kin, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(vals, vin, n * 4, cudaMemcpyDeviceToDevice, s);
     }
     return cuda_fail(cudaGetLastError(), "radix sort");
+}
+
+int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
+                     void* temp, size_t temp_bytes, cudaStream_t s) {
+    return radix_sort_t(keys, vals, n, begin_bit, end_bit, temp, temp_bytes, s);
+}
+
+int radix_sort_pairs32(uint32_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
+                       void* temp, size_t temp_bytes, cudaStream_t s) {
+    return radix_sort_t(keys, vals, n, begin_bit, std::min(end_bit, 32), temp, temp_bytes, s);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -401,8 +457,8 @@ namespace ndtgb {
 // ---------------------------------------------------------------------------------------
 // Segments of sorted keys.
 // ---------------------------------------------------------------------------------------
-__global__ void k_seg_flags(const uint64_t* __restrict__ keys, size_t n,
-                            uint32_t* __restrict__ flags) {
+template <typename K>
+__global__ void k_seg_flags(const K* __restrict__ keys, size_t n, uint32_t* __restrict__ flags) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) flags[i] = (i > 0 && keys[i] != keys[i - 1]) ? 1u : 0u;
 }
@@ -423,8 +479,76 @@ size_t detect_segments_temp_bytes(size_t n) {
     return 2 * align_up(n * 4 + 4, 256) + scan_temp_bytes(n);
 }
 
-int detect_segments(const uint64_t* sorted, size_t n, uint32_t* seg_ids, uint32_t* seg_starts,
-                    uint32_t* num_segments, void* temp, size_t temp_bytes, cudaStream_t s) {
+// Segment starts without per-key flags (the map build's form, no segment ids): one block
+// per TILE keys counts the tile's segment starts (key != previous key), the tile counts are
+// scanned, and the blocks write their starts at the scanned offsets in key order.
+template <typename K>
+__global__ void __launch_bounds__(BT) k_seg_count(const K* __restrict__ keys, size_t n,
+                                                  uint32_t* __restrict__ tile_cnt) {
+    __shared__ uint32_t ws[BT / 32];
+    const size_t base = (size_t)blockIdx.x * TILE + (size_t)threadIdx.x * ITEMS;
+    uint32_t c = 0;
+    K prev = base > 0 && base - 1 < n ? keys[base - 1] : K(0);
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const size_t i = base + k;
+        if (i < n) {
+            const K key = keys[i];
+            c += (i == 0 || key != prev) ? 1u : 0u;
+            prev = key;
+        }
+    }
+    uint32_t tot;
+    block_exclusive_scan(c, ws, &tot);
+    if (threadIdx.x == 0) tile_cnt[blockIdx.x] = tot;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(BT) k_seg_write(const K* __restrict__ keys, size_t n,
+                                                  const uint32_t* __restrict__ tile_off,
+                                                  uint32_t* __restrict__ starts,
+                                                  uint32_t* __restrict__ num) {
+    __shared__ uint32_t ws[BT / 32];
+    const size_t base = (size_t)blockIdx.x * TILE + (size_t)threadIdx.x * ITEMS;
+    K kv[ITEMS];
+    uint32_t flags = 0, c = 0;
+    K prev = base > 0 && base - 1 < n ? keys[base - 1] : K(0);
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const size_t i = base + k;
+        kv[k] = i < n ? keys[i] : K(0);
+        const bool f = i < n && (i == 0 || kv[k] != prev);
+        prev = kv[k];
+        flags |= (f ? 1u : 0u) << k;
+        c += f ? 1u : 0u;
+    }
+    uint32_t tot;
+    uint32_t r = tile_off[blockIdx.x] + block_exclusive_scan(c, ws, &tot);
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k)
+        if (flags >> k & 1u) starts[r++] = (uint32_t)(base + k);
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *num = tile_off[blockIdx.x] + tot;
+}
+
+// starts of the runs of equal keys in sorted[0..n), their count in *num_segments;
+// temp >= ntiles(n) * 4 bytes
+template <typename K>
+static int segment_starts(const K* sorted, size_t n, uint32_t* seg_starts,
+                          uint32_t* num_segments, void* temp, cudaStream_t s) {
+    cudaMemsetAsync(num_segments, 0, 4, s);
+    if (n == 0) return cuda_fail(cudaGetLastError(), "segments");
+    const uint32_t nb = ntiles(n);
+    uint32_t* cnt = (uint32_t*)temp;
+    k_seg_count<K><<<nb, BT, 0, s>>>(sorted, n, cnt);
+    k_scan_bsums<<<1, BT, 0, s>>>(cnt, nb);
+    k_seg_write<K><<<nb, BT, 0, s>>>(sorted, n, cnt, seg_starts, num_segments);
+    return cuda_fail(cudaGetLastError(), "segments");
+}
+
+template <typename K>
+static int detect_segments_t(const K* sorted, size_t n, uint32_t* seg_ids, uint32_t* seg_starts,
+                             uint32_t* num_segments, void* temp, size_t temp_bytes,
+                             cudaStream_t s) {
     cudaMemsetAsync(num_segments, 0, 4, s);
     if (n == 0) return cuda_fail(cudaGetLastError(), "segments");
     if (temp_bytes < detect_segments_temp_bytes(n)) {
@@ -442,6 +566,11 @@ int detect_segments(const uint64_t* sorted, size_t n, uint32_t* seg_ids, uint32_
     if (rc) return rc;
     k_seg_finish<<<g, BT, 0, s>>>(flags, ex, n, seg_ids, seg_starts, num_segments);
     return cuda_fail(cudaGetLastError(), "segments");
+}
+
+int detect_segments(const uint64_t* sorted, size_t n, uint32_t* seg_ids, uint32_t* seg_starts,
+                    uint32_t* num_segments, void* temp, size_t temp_bytes, cudaStream_t s) {
+    return detect_segments_t(sorted, n, seg_ids, seg_starts, num_segments, temp, temp_bytes, s);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -499,14 +628,17 @@ __global__ void k_minmax_init(int32_t* mm) {
     else if (threadIdx.x == 6) mm[6] = 0;
 }
 
+// Morton key of each point's cell relative to the minimum cell, all ones for a non-finite
+// point (it sorts last). K = uint32_t when the key's significant bits fit.
+template <typename K>
 __global__ void __launch_bounds__(BT) k_morton(const float* __restrict__ pts, size_t n, float res,
                                                const int32_t* __restrict__ mm,
-                                               uint64_t* __restrict__ codes,
+                                               K* __restrict__ codes,
                                                uint32_t* __restrict__ idx) {
     size_t i = (size_t)blockIdx.x * BT + threadIdx.x;
     if (i >= n) return;
     float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
-    uint64_t code = ~0ull;
+    K code = ~K(0);
     if (finite3(p[0], p[1], p[2])) {
         int32_t c[3];
         cell_of(p, res, c);
@@ -516,20 +648,25 @@ __global__ void __launch_bounds__(BT) k_morton(const float* __restrict__ pts, si
             int64_t d = (int64_t)c[a] - (int64_t)mm[a];
             q[a] = d > 0x1FFFFF ? 0x1FFFFFu : (uint32_t)d;
         }
-        code = morton3(q[0], q[1], q[2]);
+        code = (K)morton3(q[0], q[1], q[2]);
     }
     codes[i] = code;
     idx[i] = (uint32_t)i;
 }
 
-int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_t* idx,
-                 int32_t* mm, cudaStream_t s) {
+// min / max cell and finite count of the points into mm
+static void cell_bounds(const float* pts, size_t n, float res, int32_t* mm, cudaStream_t s) {
     k_minmax_init<<<1, 32, 0, s>>>(mm);
     if (n) {
         unsigned g = (unsigned)std::min<size_t>((n + BT - 1) / BT, 152 * 8);
         k_cells_minmax<<<g, BT, 0, s>>>(pts, n, res, mm);
-        k_morton<<<(unsigned)((n + BT - 1) / BT), BT, 0, s>>>(pts, n, res, mm, codes, idx);
     }
+}
+
+int morton_codes(const float* pts, size_t n, float res, uint64_t* codes, uint32_t* idx,
+                 int32_t* mm, cudaStream_t s) {
+    cell_bounds(pts, n, res, mm, s);
+    if (n) k_morton<uint64_t><<<(unsigned)((n + BT - 1) / BT), BT, 0, s>>>(pts, n, res, mm, codes, idx);
     return cuda_fail(cudaGetLastError(), "morton codes");
 }
 
@@ -774,16 +911,135 @@ __device__ bool regularize(const double* A, const float* a32, const float* V32, 
     return true;
 }
 
-// Statistics of one voxel from its points, visited in input order by each(f) (f called with
-// a pointer to each point's xyz): count, FP64 centred two-pass moments (mean, covariance /
-// (n - 1)), then the regularised covariance and its inverse (regularize). GB300's FP64 rate
-// is a small fraction of its FP32 rate: the eigenvector directions come from an f32 Jacobi,
-// and FP64 is spent only where the outputs depend on it. r.coord is the caller's.
+// ---- Exact moments ------------------------------------------------------------------------
+// Along one axis a voxel's points are f32 values of one sign (one cell) within a binade or two
+// of each other. Take the exponent 2^e0 two binades below the first point's ulp: every point
+// is then p = m 2^e0 with an integer |m| < 2^30, and d = m - m_first stays below 2^26 in
+// magnitude (a cell at least one resolution from zero spans at most 2^24 ulps of its points).
+// So the sums S1_a = sum d_a and S2_ab = sum d_a d_b are exact in int64 for up to 2048 points
+// (|d_a d_b| < 2^52), and a warp's lanes may add their partial sums in any order. From them:
+//   - the sum of the points, (S1 + n m_first) 2^e0, is exact and below 2^53 units; every
+//     partial sum of same-sign multiples of 2^e0 lies below it, so the FP64 running sum in
+//     input order (build_voxel_grid_cpu, src/ndt_cuda/src/voxel_grid/cpu.rs:51-75) is exact
+//     and equal to it, and the mean fl(sum / n) is that running sum's mean bit for bit;
+//   - the centred covariance, cov_ab = (n S2_ab - S1_a S1_b) 2^(e0a + e0b) / (n (n - 1)),
+//     from the exact 128-bit numerator rounded once to FP64 times the FP64 reciprocal of
+//     n (n - 1): within a few roundings of the exact value whatever the order of the points
+//     (a tile merge and a full build of the same cell agree bit for bit).
+// A point that breaks a bound (cells next to zero, subnormal or wide-spread values) sends the
+// voxel to the FP64 two-pass formula.
+struct ExactMoments {
+    int32_t eref[3];    // biased f32 exponent of 2^e0 (e0 = eref - 150)
+    int32_t m0[3];      // the first point's integer m
+    long long s1[3];
+    long long s2[6];    // xx, xy, xz, yy, yz, zz
+    bool ok;
+};
+
+// m of one coordinate with reference exponent eref (ok cleared when it breaks the bounds)
+__device__ __forceinline__ int32_t exact_units(float x, int32_t eref, bool& ok) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    if (ex == 0u) {
+        ok &= (b << 1) == 0u;  // +-0 contributes 0; a subnormal leaves the exact path
+        return 0;
+    }
+    const int32_t sh = (int32_t)ex - eref;
+    ok &= (uint32_t)sh <= 6u;
+    int32_t m = (int32_t)(((b & 0x7FFFFFu) | 0x800000u) << (sh & 7));
+    return (b >> 31) ? -m : m;
+}
+
+__device__ __forceinline__ void exact_begin(ExactMoments& em, const float* p) {
+    em.ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int32_t ex = (int32_t)((__float_as_uint(p[a]) >> 23) & 0xFFu);
+        em.ok &= ex > 2 && ex < 255;
+        em.eref[a] = ex - 2;
+        em.m0[a] = exact_units(p[a], em.eref[a], em.ok);
+        em.s1[a] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) em.s2[k] = 0;
+}
+
+__device__ __forceinline__ void exact_add(ExactMoments& em, const float* p) {
+    int32_t d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        d[a] = exact_units(p[a], em.eref[a], em.ok) - em.m0[a];
+        em.ok &= (uint32_t)(d[a] + (1 << 26)) < (1u << 27);
+        em.s1[a] += d[a];
+    }
+    em.s2[0] += (long long)d[0] * d[0];
+    em.s2[1] += (long long)d[0] * d[1];
+    em.s2[2] += (long long)d[0] * d[2];
+    em.s2[3] += (long long)d[1] * d[1];
+    em.s2[4] += (long long)d[1] * d[2];
+    em.s2[5] += (long long)d[2] * d[2];
+}
+
+// 2^e as an FP64 (normal range)
+__device__ __forceinline__ double pow2d(int e) {
+    return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// A signed 128-bit integer (hi, lo) rounded once to the nearest FP64 (ties to even)
+__device__ __forceinline__ double i128_to_double(long long hi, unsigned long long lo) {
+    const bool neg = hi < 0;
+    unsigned long long uh = (unsigned long long)hi, ul = lo;
+    if (neg) {
+        ul = ~ul + 1ull;
+        uh = ~uh + (ul == 0ull ? 1ull : 0ull);
+    }
+    if (uh == 0ull) {
+        const double v = __ull2double_rn(ul);
+        return neg ? -v : v;
+    }
+    const int lz = __clzll((long long)uh);
+    unsigned long long top = lz ? (uh << lz) | (ul >> (64 - lz)) : uh;
+    const unsigned long long rest = lz ? ul << lz : ul;
+    if (rest != 0ull) top |= 1ull;  // sticky: the discarded bits decide ties and halves
+    const double v = __ull2double_rn(top) * pow2d(64 - lz);
+    return neg ? -v : v;
+}
+
+// mean and covariance from exact sums over n points; s2 as 128-bit (hi, lo) pairs
+__device__ __forceinline__ void exact_finish(const ExactMoments& em, uint32_t n,
+                                             const long long* s2hi,
+                                             const unsigned long long* s2lo, double* mean,
+                                             double* A) {
+    const double nn = (double)n;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const long long tot = em.s1[a] + (long long)n * em.m0[a];
+        mean[a] = ((double)tot * pow2d(em.eref[a] - 150)) / nn;
+    }
+    const double inv_den = 1.0 / (nn * (double)(n - 1u));
+    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        // n S2 (128-bit times a small unsigned) minus S1_a S1_b (64 x 64 -> 128), exact
+        const unsigned long long nl = s2lo[k] * (unsigned long long)n;
+        const long long nh =
+            s2hi[k] * (long long)n + (long long)__umul64hi(s2lo[k], (unsigned long long)n);
+        const long long pa = em.s1[ia[k]], pb = em.s1[ib[k]];
+        const unsigned long long ql = (unsigned long long)pa * (unsigned long long)pb;
+        const long long qh = __mul64hi(pa, pb);
+        const unsigned long long rl = nl - ql;
+        const long long rh = nh - qh - (nl < ql ? 1ll : 0ll);
+        const double v =
+            i128_to_double(rh, rl) * pow2d(em.eref[ia[k]] + em.eref[ib[k]] - 300) * inv_den;
+        A[ia[k] * 3 + ib[k]] = A[ib[k] * 3 + ia[k]] = v;
+    }
+}
+
+// FP64 centred two-pass moments of one voxel's points, visited in input order by each(f) (f
+// called with a pointer to each point's xyz): mean = sum / n, covariance = sum of the centred
+// products / (n - 1). The route for voxels the exact sums cannot take.
 template <class Each>
-__device__ __forceinline__ bool voxel_stats(Each each, uint32_t cnt, int min_points,
-                                            float ratio, SegRec& r) {
-    r.count = cnt;
-    if ((int)cnt < min_points) return false;
+__device__ __noinline__ void moments_two_pass(Each each, uint32_t cnt, double* mean, double* A) {
     double sum[3] = {0.0, 0.0, 0.0};
     each([&](const float* p) {
         sum[0] += (double)p[0];
@@ -791,7 +1047,7 @@ __device__ __forceinline__ bool voxel_stats(Each each, uint32_t cnt, int min_poi
         sum[2] += (double)p[2];
     });
     const double nn = (double)cnt;
-    const double mean[3] = {sum[0] / nn, sum[1] / nn, sum[2] / nn};
+    for (int a = 0; a < 3; ++a) mean[a] = sum[a] / nn;
     // upper triangle xx, xy, xz, yy, yz, zz (the products are symmetric bit for bit)
     double sq[6] = {0, 0, 0, 0, 0, 0};
     each([&](const float* p) {
@@ -805,13 +1061,19 @@ __device__ __forceinline__ bool voxel_stats(Each each, uint32_t cnt, int min_poi
         sq[5] += d2 * d2;
     });
     const double nm1 = nn - 1.0;
-    double A[9];
     A[0] = sq[0] / nm1;
     A[1] = A[3] = sq[1] / nm1;
     A[2] = A[6] = sq[2] / nm1;
     A[4] = sq[3] / nm1;
     A[5] = A[7] = sq[4] / nm1;
     A[8] = sq[5] / nm1;
+}
+
+// Regularised covariance, inverse and mean of a voxel from its FP64 mean and covariance
+// A. GB300's FP64 rate is a small fraction of its FP32 rate: the eigenvector directions come
+// from an f32 Jacobi, and FP64 is spent only where the outputs depend on it (regularize).
+__device__ __forceinline__ bool voxel_finish(const double* mean, const double* A, float ratio,
+                                             SegRec& r) {
     float a32[9], V32[9];
     for (int q = 0; q < 9; ++q) a32[q] = (float)A[q];
     jacobi3f(a32, V32);
@@ -820,11 +1082,45 @@ __device__ __forceinline__ bool voxel_stats(Each each, uint32_t cnt, int min_poi
     return true;
 }
 
+// Largest voxel one thread sums exactly (the int64 bound of the second moments)
+constexpr uint32_t EXACT_THREAD_MAX = 2048;
+
+// Statistics of one voxel by one thread: count, then exact moments when the voxel has at most
+// EXACT_THREAD_MAX points and they stay within the exact bounds, else FP64 two-pass moments;
+// then voxel_finish. each(f) visits the voxel's points in input order; first: its first point.
+// r.coord is the caller's.
+template <class Each>
+__device__ __forceinline__ bool voxel_stats(Each each, const float* first, uint32_t cnt,
+                                            int min_points, float ratio, SegRec& r) {
+    r.count = cnt;
+    if ((int)cnt < min_points) return false;
+    double mean[3], A[9];
+    bool exact = cnt <= EXACT_THREAD_MAX;
+    ExactMoments em;
+    if (exact) {
+        exact_begin(em, first);
+        each([&](const float* p) { exact_add(em, p); });
+        exact = em.ok;
+    }
+    if (exact) {
+        long long hi[6];
+        unsigned long long lo[6];
+        for (int k = 0; k < 6; ++k) {
+            hi[k] = em.s2[k] >> 63;
+            lo[k] = (unsigned long long)em.s2[k];
+        }
+        exact_finish(em, cnt, hi, lo, mean, A);
+    } else {
+        moments_two_pass(each, cnt, mean, A);
+    }
+    return voxel_finish(mean, A, ratio, r);
+}
+
 // Segment sizes as sort keys: segments visited largest first (key 0xFFFF - min(count,
-// 0xFFFF)), so the threads of a warp take segments of nearly equal size (one thread walks
-// one segment; a warp costs its largest segment) and the longest warps start first.
+// 0xFFFF)), so the threads of a warp take segments of nearly equal size and the longest
+// start first.
 __global__ void k_seg_size_keys(const uint32_t* __restrict__ starts, uint32_t S, uint32_t nf,
-                                uint64_t* __restrict__ keys, uint32_t* __restrict__ order) {
+                                uint32_t* __restrict__ keys, uint32_t* __restrict__ order) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
     const uint32_t e = s + 1 < S ? starts[s + 1] : nf;
@@ -832,25 +1128,138 @@ __global__ void k_seg_size_keys(const uint32_t* __restrict__ starts, uint32_t S,
     order[s] = s;
 }
 
-// One thread per segment of the sorted keys (order[t]: the t-th segment to visit). Every
-// segment's record gets its cell and count (a tile merge reads them for cells shared between
-// tiles); valid[s] marks the voxels.
+// Voxels of at least WARP_SEG_MIN points are summed by a whole warp (exact sums of the lanes'
+// strided shares, added over the lanes in 128-bit); up to EXACT_THREAD_MAX points per lane.
+constexpr uint32_t WARP_SEG_MIN = 48;
+
+// 128-bit (hi, lo) sum over the warp's lanes (every lane ends with the total)
+__device__ __forceinline__ void warp_sum128(long long& hi, unsigned long long& lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        const long long oh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const unsigned long long s = lo + ol;
+        hi = hi + oh + (s < lo ? 1ll : 0ll);
+        lo = s;
+    }
+}
+
+// Exact sums of one large segment, as a warp leaves them for the lane that finishes it
+struct SegSums {
+    long long s1[3];
+    long long hi[6];
+    unsigned long long lo[6];
+    int32_t ok;
+    int32_t pad;
+};
+
+// Segments in visit order (order[t], largest first; skey[t] its sorted size key). The first
+// W segments (WARP_SEG_MIN points or more) go to warps in groups of 32: for each segment of
+// its group the warp sums the points exactly (lanes take strided shares, the 128-bit sums
+// are added over the lanes) and lane j keeps segment j's sums; then every lane finishes its
+// own segment (regularisation), the FP64 work spread over the lanes. The rest go one per
+// thread, thread i taking t = W + i. Every segment's record gets its cell and count (a tile
+// merge reads them for cells shared between tiles); valid[s] marks the voxels.
 __global__ void __launch_bounds__(128) k_voxel_stats(
     const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
-    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ order, uint32_t S,
-    uint32_t nf, float res, int min_points, float ratio, SegRec* __restrict__ rec,
-    uint32_t* __restrict__ valid) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ order,
+    const uint32_t* __restrict__ skey, uint32_t S, uint32_t nf, float res, int min_points,
+    float ratio, SegRec* __restrict__ rec, uint32_t* __restrict__ valid) {
+    __shared__ uint32_t sW;
+    __shared__ SegSums stash[4][32];
+    if (threadIdx.x == 0) {
+        // W = number of keys <= 0xFFFF - WARP_SEG_MIN (keys ascend)
+        uint32_t lo = 0, hi = S;
+        const uint32_t lim = 0xFFFFu - WARP_SEG_MIN;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (skey[mid] <= lim) lo = mid + 1;
+            else hi = mid;
+        }
+        sW = lo;
+    }
+    __syncthreads();
+    const uint32_t W = sW;
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    SegSums* const st = stash[wib];
+    for (uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; g0 < W;
+         g0 += warps * 32u) {
+        const uint32_t gn = min(32u, W - g0);
+        for (uint32_t j = 0; j < gn; ++j) {
+            const uint32_t s = order[g0 + j];
+            const uint32_t b = starts[s];
+            const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+            const uint32_t cnt = e - b;
+            if ((int)cnt < min_points) continue;
+            ExactMoments em;
+            exact_begin(em, pts + 3 * (size_t)sidx[b]);
+            for (uint32_t k = b + lane; k < e; k += 32) exact_add(em, pts + 3 * (size_t)sidx[k]);
+            const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= 32u * EXACT_THREAD_MAX;
+            if (exact) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        em.s1[a] += __shfl_xor_sync(0xffffffffu, em.s1[a], o);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    long long h = em.s2[k] >> 63;
+                    unsigned long long l = (unsigned long long)em.s2[k];
+                    warp_sum128(h, l);
+                    if (lane == j) {
+                        st[j].hi[k] = h;
+                        st[j].lo[k] = l;
+                    }
+                }
+                if (lane == j)
+                    for (int a = 0; a < 3; ++a) st[j].s1[a] = em.s1[a];
+            }
+            if (lane == j) st[j].ok = exact ? 1 : 0;
+        }
+        __syncwarp();
+        if (lane < gn) {
+            const uint32_t s = order[g0 + lane];
+            const uint32_t b = starts[s];
+            const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+            const uint32_t cnt = e - b;
+            const float* first = pts + 3 * (size_t)sidx[b];
+            SegRec r;
+            cell_of(first, res, r.coord);
+            r.count = cnt;
+            bool ok = false;
+            if ((int)cnt >= min_points) {
+                double mean[3], A[9];
+                if (st[lane].ok) {
+                    ExactMoments em;
+                    exact_begin(em, first);
+                    for (int a = 0; a < 3; ++a) em.s1[a] = st[lane].s1[a];
+                    exact_finish(em, cnt, st[lane].hi, st[lane].lo, mean, A);
+                } else {
+                    auto each = [&](auto f) {
+                        for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
+                    };
+                    moments_two_pass(each, cnt, mean, A);
+                }
+                ok = voxel_finish(mean, A, ratio, r);
+            }
+            rec[s] = r;
+            valid[s] = ok ? 1u : 0u;
+        }
+        __syncwarp();
+    }
+    const uint32_t t = W + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= S) return;
     const uint32_t s = order[t];
     const uint32_t b = starts[s];
     const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+    const float* first = pts + 3 * (size_t)sidx[b];
     SegRec r;
-    cell_of(pts + 3 * (size_t)sidx[b], res, r.coord);
+    cell_of(first, res, r.coord);
     auto each = [&](auto f) {
         for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
     };
-    const bool ok = voxel_stats(each, e - b, min_points, ratio, r);
+    const bool ok = voxel_stats(each, first, e - b, min_points, ratio, r);
     rec[s] = r;
     valid[s] = ok ? 1u : 0u;
 }
@@ -925,19 +1334,49 @@ __global__ void k_grid_fill(MapView m, float4* __restrict__ grid) {
 // (always inside the grown box). One thread per hash slot; the masks start at zero, and OR
 // is order-free, so the result does not depend on the threads' order. The work goes with
 // the number of voxels, not with the box.
+// A bit is set only where the voxel's centroid can pass the radius test from some point of
+// cell v - d: its distance to that cell's box (the gaps along the axes where d is non-zero)
+// is at most the radius, widened by 1e-5 of it and by 1e-6 cell widths per cell of distance
+// from the origin (the f32 rounding of a point's cell and of the f32 distance test). A
+// cleared bit names a neighbour no point of the cell accepts, so neighbour lists are those of
+// the full 27-cell search, with a fifth or so fewer candidates to test.
 __global__ void k_grid_mask(MapView m, uint32_t* __restrict__ nmask) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s > m.mask) return;
-    const uint32_t key = m.slots[s].x;
+    const uint4 sv = m.slots[s];
+    const uint32_t key = sv.x;
     if (key == EMPTY_KEY) return;
-    const uint32_t vx = key & ((1u << m.bits[0]) - 1u);
-    const uint32_t vy = (key >> m.bits[0]) & ((1u << m.bits[1]) - 1u);
-    const uint32_t vz = key >> (m.bits[0] + m.bits[1]);
+    const uint32_t v[3] = {key & ((1u << m.bits[0]) - 1u),
+                           (key >> m.bits[0]) & ((1u << m.bits[1]) - 1u),
+                           key >> (m.bits[0] + m.bits[1])};
+    const float mu[3] = {__uint_as_float(sv.y), __uint_as_float(sv.z), __uint_as_float(sv.w)};
+    const float res = m.res;
+    float lo[3], hi[3], far = 0.f;  // gaps below / above the voxel's own cell
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float c = (float)((int64_t)v[a] + m.min_cell[a]);
+        lo[a] = fmaxf(mu[a] - c * res, 0.f);           // d_a = +1: the cell below
+        hi[a] = fmaxf((c + 1.f) * res - mu[a], 0.f);   // d_a = -1: the cell above
+        far = fmaxf(far, fabsf(c) + 2.f);
+    }
+    // f32 evaluation: the cell corners and gaps carry at most a few ulps of far * res, well
+    // inside the 1e-6 far * res widening
+    const float lim = res * (1.f + 1e-5f) + 1e-6f * far * res;
+    const float lim2 = lim * lim;
     const uint32_t E1 = m.ext[1] + 2u, E2 = m.ext[2] + 2u;
 #pragma unroll 1
     for (uint32_t b = 0; b < 27u; ++b) {
+        const int dd[3] = {(int)(b / 9u) - 1, (int)(b / 3u % 3u) - 1, (int)(b % 3u) - 1};
+        float g2 = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float gap = dd[a] > 0 ? lo[a] : (dd[a] < 0 ? hi[a] : 0.f);
+            g2 += gap * gap;
+        }
+        if (g2 > lim2) continue;
         // grown-box position of cell v - d, plus one: v + 1 - (d + 1) + 1 = v + 2 - (d + 1)
-        const uint32_t gx = vx + 2u - b / 9u, gy = vy + 2u - b / 3u % 3u, gz = vz + 2u - b % 3u;
+        const uint32_t gx = v[0] + 2u - b / 9u, gy = v[1] + 2u - b / 3u % 3u,
+                       gz = v[2] + 2u - b % 3u;
         atomicOr(nmask + ((size_t)gx * E1 + gy) * E2 + gz, 1u << b);
     }
 }
@@ -979,12 +1418,11 @@ int build_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_con
     size_t tmp = std::max(radix_sort_temp_bytes(n), detect_segments_temp_bytes(n));
     tmp = std::max(tmp, scan_temp_bytes(n));
     if ((rc = dev_reserve(sc.tmp, tmp))) return rc;
-    uint64_t* keys = (uint64_t*)sc.keys_a.p;
     uint32_t* vals = (uint32_t*)sc.vals_a.p;
     int32_t* mm = (int32_t*)sc.small.p;
     uint32_t* nseg = (uint32_t*)((char*)sc.small.p + 64);
 
-    if ((rc = morton_codes(d_pts, n, cfg.resolution, keys, vals, mm, s))) return rc;
+    cell_bounds(d_pts, n, cfg.resolution, mm, s);
     int32_t hmm[7];
     cudaMemcpyAsync(hmm, mm, sizeof hmm, cudaMemcpyDeviceToHost, s);
     if ((rc = cuda_fail(cudaStreamSynchronize(s), "map bounds"))) return rc;
@@ -1001,22 +1439,33 @@ int build_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_con
     if ((rc = box_bits(g.mn, g.mx, bits))) return rc;
     const uint32_t lv = std::max(bits[0], std::max(bits[1], bits[2]));
     const int end_bit = std::min(64, (int)(3 * lv + 1));
-    if ((rc = radix_sort_pairs(keys, vals, n, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s))) return rc;
-    if ((rc = detect_segments(keys, g.nf, nullptr, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p,
-                              sc.tmp.bytes, s)))
-        return rc;
+    const unsigned gp = (unsigned)((n + BT - 1) / BT);
+    if (end_bit <= 32) {
+        // the keys fit 32 bits (the non-finite key, all ones, still sorts last)
+        uint32_t* keys = (uint32_t*)sc.keys_a.p;
+        k_morton<uint32_t><<<gp, BT, 0, s>>>(d_pts, n, cfg.resolution, mm, keys, vals);
+        if ((rc = radix_sort_pairs32(keys, vals, n, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s)) ||
+            (rc = segment_starts(keys, g.nf, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p, s)))
+            return rc;
+    } else {
+        uint64_t* keys = (uint64_t*)sc.keys_a.p;
+        k_morton<uint64_t><<<gp, BT, 0, s>>>(d_pts, n, cfg.resolution, mm, keys, vals);
+        if ((rc = radix_sort_pairs(keys, vals, n, 0, end_bit, sc.tmp.p, sc.tmp.bytes, s)) ||
+            (rc = segment_starts(keys, g.nf, (uint32_t*)sc.seg_starts.p, nseg, sc.tmp.p, s)))
+            return rc;
+    }
     cudaMemcpyAsync(&g.S, nseg, 4, cudaMemcpyDeviceToHost, s);
     if ((rc = cuda_fail(cudaStreamSynchronize(s), "segments"))) return rc;
     // visit order of the segments, largest first (the keys' buffer is free again: the
     // segments are recorded by their starts)
-    uint64_t* skeys = keys;
+    uint32_t* skeys = (uint32_t*)sc.keys_a.p;
     uint32_t* order = (uint32_t*)sc.seg_rank.p;
     k_seg_size_keys<<<(g.S + 255) / 256, 256, 0, s>>>((const uint32_t*)sc.seg_starts.p, g.S,
                                                       (uint32_t)g.nf, skeys, order);
-    if ((rc = radix_sort_pairs(skeys, order, g.S, 0, 16, sc.tmp.p, sc.tmp.bytes, s))) return rc;
+    if ((rc = radix_sort_pairs32(skeys, order, g.S, 0, 16, sc.tmp.p, sc.tmp.bytes, s))) return rc;
     k_voxel_stats<<<(g.S + 127) / 128, 128, 0, s>>>(
-        d_pts, vals, (uint32_t*)sc.seg_starts.p, order, g.S, (uint32_t)g.nf, cfg.resolution,
-        cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
+        d_pts, vals, (uint32_t*)sc.seg_starts.p, order, skeys, g.S, (uint32_t)g.nf,
+        cfg.resolution, cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
         (uint32_t*)sc.seg_valid.p);
     return cuda_fail(cudaStreamSynchronize(s), "voxel statistics");
 }
@@ -1200,7 +1649,9 @@ __global__ void __launch_bounds__(128) k_merge_groups(
             for (uint32_t k = b; k < e; ++k) f(T.pts + 3 * (size_t)T.idx[k]);
         }
     };
-    const bool ok = voxel_stats(each, cnt, min_points, ratio, r);
+    locate(members[m0], t, sl);
+    const float* first = tiles[t].pts + 3 * (size_t)tiles[t].idx[tiles[t].starts[sl]];
+    const bool ok = voxel_stats(each, first, cnt, min_points, ratio, r);
     grec[g] = r;
     gvalid[g] = ok ? 1u : 0u;
 }
