@@ -165,6 +165,31 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def build_bytes(info):
+    """Algorithmic DRAM bytes of one map build as the pipeline runs it (set_target):
+    per point: bounds pass (12 B read), key pass (12 B read, key + index written), one
+    histogram read and one key+value read and write per 8-bit radix pass over the significant
+    key bits (32-bit keys when 3 x max key bits + 1 <= 32, else 64-bit), two key reads for the
+    segment starts, and the statistics' index and point gather (16 B); per segment: its start,
+    size key and visit order, the two 16-bit size-sort passes, its record (88 B) and validity;
+    per voxel: the record read back, the voxel arrays written (104 B), the hash insert's
+    reads (64 B) and slot writes (52 B) and the 27 mask words; per slot: the 16 B clear; the
+    dense index and masks: one clear and one fill of 16 B per cell, one clear of 4 B per mask
+    cell."""
+    n, S, V, cap = (int(info.num_points), int(info.num_segments), int(info.num_voxels),
+                    int(info.hash_capacity))
+    lv = max(int(b) for b in info.key_bits)
+    end_bit = min(64, 3 * lv + 1)
+    kw = 4 if end_bit <= 32 else 8
+    passes = (end_bit + 7) // 8
+    per_point = 12 + 12 + kw + 4 + passes * (kw + 2 * (kw + 4)) + 2 * kw + 16
+    per_seg = 4 + 8 + 2 * 3 * 8 + 88 + 4
+    per_vox = 88 + 104 + 64 + 52 + 27 * 4
+    dense = float(info.dense_grid_mib) * 1024 * 1024  # grid (16 B/cell) + masks (4 B/cell)
+    grid_bytes = 2 * dense * 16 / 20 + dense * 4 / 20
+    return int(per_point * n + per_seg * S + per_vox * V + 16 * cap + grid_bytes)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -493,7 +518,7 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
         ctx.set_target(pts)                # allocations
         ctx.set_target(pts)                # timed rebuild
         info = ctx.map_info()
-        nbytes = 248 * info.num_points + 64 * info.num_voxels + 16 * info.hash_capacity
+        nbytes = build_bytes(info)
         coords, means, covs, icovs, counts = ctx.map_voxels()
         pick = rng.choice(len(coords), 20, replace=False)
         exact, fp32_err, cov_ulp, icov_ulp = True, 0.0, 0.0, 0.0
@@ -862,7 +887,7 @@ def run_ours(args):
     # accuracy of this run against the true poses (diagnostic)
     got = np.array([list(r.pose) for r in res_arr])
     perr = np.linalg.norm(got[:, :2] - truth[:, :2], axis=1)
-    build_bytes = 248 * info.num_points + 64 * info.num_voxels + 16 * info.hash_capacity
+    bbytes = build_bytes(info)
 
     parity = None
     if rank == 0 and args.parity:
@@ -927,10 +952,11 @@ def run_ours(args):
                          "phase_cycles_share": phase_shares(st),
                          "eigen_solves_per_align": st["eigen_solves"] /
                          max(st["alignments"], 1)},
-            "build_roofline": {"bound": "hbm", "achieved": build_bytes / (build_ms / 1e3) / 1e9,
+            "build_roofline": {"bound": "hbm", "achieved": bbytes / (build_ms / 1e3) / 1e9,
                                "peak": pk.get("hbm_gbs"), "unit": "GB/s",
-                               "frac": build_bytes / (build_ms / 1e3) / 1e9 / pk.get("hbm_gbs"),
-                               "build_ms": build_ms, "bytes": int(build_bytes),
+                               "frac": bbytes / (build_ms / 1e3) / 1e9 / pk.get("hbm_gbs"),
+                               "build_ms": build_ms, "bytes": int(bbytes),
+                               "bytes_rule": "bench.build_bytes: the pipeline's passes as run",
                                "peak_source": src},
             "cpu_baseline": cpu,
             "parity": parity,

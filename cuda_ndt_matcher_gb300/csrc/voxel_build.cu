@@ -804,8 +804,9 @@ __device__ __forceinline__ void refine_vector(const double* A, double* v, double
 // ratio * lambda_max are raised to it; cov' = V diag(clamped) V^T when any was, else A;
 // inverse V diag(1 / clamped) V^T. a32 / V32: the f32 Jacobi's eigenvalues (diagonal) and
 // eigenvectors (columns). Which eigenvalues clamp is read from the f32 eigenvalues when they
-// lie clear of the threshold (1e-3 relative, against their 1e-5 error there), and the clamped
-// ones lie at least lambda_max / 100 below the others; then, with FP64 Rayleigh quotients as
+// lie clear of the threshold (1e-4 relative, against their 1e-5 error there), and the clamped
+// ones lie at least lambda_max / 1000 below the others (an f32 direction error of 1e-4 at most,
+// 1e-8 after the first-order refinement); then, with FP64 Rayleigh quotients as
 // the eigenvalues:
 //   - nothing clamps: cov' = A, inverse by the adjugate (A's condition number <= 1 / ratio);
 //   - one clamps: cov' = A + (thr - lambda_c) v_c v_c^T, v_c refined against the other two;
@@ -825,15 +826,15 @@ __device__ bool regularize(const double* A, const float* a32, const float* V32, 
     if (fast) {
         const float thr32 = mx32 * ratio;
         for (int i = 0; i < 3; ++i) {
-            if (e32[i] <= thr32 * 0.999f) {
+            if (e32[i] <= thr32 * 0.9999f) {
                 clamp |= 1 << i;
-            } else if (!(e32[i] >= thr32 * 1.001f)) {
+            } else if (!(e32[i] >= thr32 * 1.0001f)) {
                 fast = false;
             }
         }
         for (int i = 0; i < 3 && fast; ++i)
             for (int j = 0; j < 3; ++j)
-                if ((clamp >> i & 1) && !(clamp >> j & 1) && e32[j] - e32[i] < 0.01f * mx32)
+                if ((clamp >> i & 1) && !(clamp >> j & 1) && e32[j] - e32[i] < 0.001f * mx32)
                     fast = false;
     }
     if (fast) {
@@ -912,72 +913,111 @@ __device__ bool regularize(const double* A, const float* a32, const float* V32, 
 }
 
 // ---- Exact moments ------------------------------------------------------------------------
-// Along one axis a voxel's points are f32 values of one sign (one cell) within a binade or two
-// of each other. Take the exponent 2^e0 two binades below the first point's ulp: every point
-// is then p = m 2^e0 with an integer |m| < 2^30, and d = m - m_first stays below 2^26 in
-// magnitude (a cell at least one resolution from zero spans at most 2^24 ulps of its points).
-// So the sums S1_a = sum d_a and S2_ab = sum d_a d_b are exact in int64 for up to 2048 points
-// (|d_a d_b| < 2^52), and a warp's lanes may add their partial sums in any order. From them:
-//   - the sum of the points, (S1 + n m_first) 2^e0, is exact and below 2^53 units; every
-//     partial sum of same-sign multiples of 2^e0 lies below it, so the FP64 running sum in
-//     input order (build_voxel_grid_cpu, src/ndt_cuda/src/voxel_grid/cpu.rs:51-75) is exact
-//     and equal to it, and the mean fl(sum / n) is that running sum's mean bit for bit;
-//   - the centred covariance, cov_ab = (n S2_ab - S1_a S1_b) 2^(e0a + e0b) / (n (n - 1)),
-//     from the exact 128-bit numerator rounded once to FP64 times the FP64 reciprocal of
-//     n (n - 1): within a few roundings of the exact value whatever the order of the points
-//     (a tile merge and a full build of the same cell agree bit for bit).
-// A point that breaks a bound (cells next to zero, subnormal or wide-spread values) sends the
-// voxel to the FP64 two-pass formula.
+// Per axis, a quantum 2^e0 from the voxel's cell k: its points lie within
+// B = max(|k|, |k + 1|) resolutions of zero, below 2^EB (B < 2^EB with a 1e-3 margin for the
+// f32 cell rule). For a cell at least one resolution from zero every point is at least about
+// B / 2, a multiple of its ulp >= 2^(EB - 26): e0 = EB - 26. A cell next to zero (k = 0 or
+// -1) holds values of any size: e0 = EB - 40. Each point is then m 2^e0 with an integer
+// |m| < 2^40, exact unless it is a value below 2^(e0 + 23) whose low bits fall under the
+// quantum (it is rounded then, by at most 2^-41 of the cell's reach). With d = m - m_first
+// (|d| < 2^41) the sums S1 = sum d (int64) and S2 = sum d d^T (128-bit) are exact for up to
+// 65536 points and independent of the order of the points. From them:
+//   - the mean of an axis whose points were all exact and whose sum (S1 + n m_first) has at
+//     most 53 significant bits above the coarsest power of two dividing every point: every
+//     partial sum of these same-sign values (one cell) is then an FP64 number, so the FP64
+//     running sum in input order (build_voxel_grid_cpu, src/ndt_cuda/src/voxel_grid/cpu.rs:
+//     51-75) never rounds and equals it, and fl(sum / n) is its mean bit for bit. Any other
+//     axis takes that running sum in input order (moments_mean_fp64);
+//   - the centred covariance (n S2 - S1 S1^T) 2^(e0a + e0b) / (n (n - 1)) from the 128-bit
+//     numerator rounded once to FP64 and the FP64 reciprocal of n (n - 1): within a few
+//     roundings of the exact value whatever the order of the points (a tile merge and a full
+//     build of the same cell agree bit for bit).
+// A value beyond the cell's reach or non-finite sends the voxel to the FP64 two-pass formula.
 struct ExactMoments {
-    int32_t eref[3];    // biased f32 exponent of 2^e0 (e0 = eref - 150)
-    int32_t m0[3];      // the first point's integer m
+    int32_t e0[3];            // quantum exponent per axis
+    int32_t tz[3];            // fewest trailing zero bits of a non-zero m (the coarse quantum)
+    long long m0[3];          // the first point in quanta
     long long s1[3];
-    long long s2[6];    // xx, xy, xz, yy, yz, zz
-    bool ok;
+    long long s2h[6];         // xx, xy, xz, yy, yz, zz as 128-bit (hi, lo)
+    unsigned long long s2l[6];
+    bool rep[3];              // every point of the axis an exact multiple of 2^e0
+    bool ok;                  // every point within the cell's reach
 };
 
-// m of one coordinate with reference exponent eref (ok cleared when it breaks the bounds)
-__device__ __forceinline__ int32_t exact_units(float x, int32_t eref, bool& ok) {
+// m of one coordinate in quanta 2^e0 (rounded to nearest; rep cleared when inexact, ok when
+// beyond 2^(e0 + 40))
+__device__ __forceinline__ long long exact_units(float x, int32_t e0, bool& rep, int32_t& tz,
+                                                 bool& ok) {
     const uint32_t b = __float_as_uint(x);
     const uint32_t ex = (b >> 23) & 0xFFu;
-    if (ex == 0u) {
-        ok &= (b << 1) == 0u;  // +-0 contributes 0; a subnormal leaves the exact path
+    if (ex == 0u) {  // +-0 is exact; a subnormal rounds to 0 quanta
+        rep &= (b << 1) == 0u;
         return 0;
     }
-    const int32_t sh = (int32_t)ex - eref;
-    ok &= (uint32_t)sh <= 6u;
-    int32_t m = (int32_t)(((b & 0x7FFFFFu) | 0x800000u) << (sh & 7));
-    return (b >> 31) ? -m : m;
+    ok &= ex != 0xFFu;
+    const int32_t sh = (int32_t)ex - 150 - e0;
+    ok &= sh <= 16;
+    const unsigned long long M = (b & 0x7FFFFFu) | 0x800000u;
+    unsigned long long m;
+    if (sh >= 0) {
+        m = M << (sh & 63);
+    } else if (sh > -25) {
+        const int r = -sh;
+        rep &= (M & ((1ull << r) - 1ull)) == 0ull;
+        m = (M + (1ull << (r - 1))) >> r;
+    } else {
+        rep = false;
+        m = 0;
+    }
+    if (m) tz = min(tz, __ffsll((long long)m) - 1);
+    return (b >> 31) ? -(long long)m : (long long)m;
 }
 
-__device__ __forceinline__ void exact_begin(ExactMoments& em, const float* p) {
+__device__ __forceinline__ void add_prod128(long long& hi, unsigned long long& lo, long long a,
+                                            long long b) {
+    const unsigned long long pl = (unsigned long long)a * (unsigned long long)b;
+    const long long ph = __mul64hi(a, b);
+    const unsigned long long s = lo + pl;
+    hi += ph + (s < lo ? 1ll : 0ll);
+    lo = s;
+}
+
+// quanta of the cell `coord` (the f32 cell index of the voxel) and the first point
+__device__ __forceinline__ void exact_begin(ExactMoments& em, const float* p, const int32_t* coord,
+                                            float res) {
     em.ok = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const int32_t ex = (int32_t)((__float_as_uint(p[a]) >> 23) & 0xFFu);
-        em.ok &= ex > 2 && ex < 255;
-        em.eref[a] = ex - 2;
-        em.m0[a] = exact_units(p[a], em.eref[a], em.ok);
+        const float k = (float)coord[a];
+        const float reach = fmaxf(fabsf(k), fabsf(k + 1.f)) * res * 1.001f;
+        int eb;
+        frexpf(reach, &eb);  // reach < 2^eb
+        em.e0[a] = eb - ((coord[a] == 0 || coord[a] == -1) ? 40 : 26);
+        em.tz[a] = 64;
+        em.rep[a] = true;
         em.s1[a] = 0;
+        em.m0[a] = exact_units(p[a], em.e0[a], em.rep[a], em.tz[a], em.ok);
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) em.s2[k] = 0;
+    for (int k = 0; k < 6; ++k) {
+        em.s2h[k] = 0;
+        em.s2l[k] = 0ull;
+    }
 }
 
 __device__ __forceinline__ void exact_add(ExactMoments& em, const float* p) {
-    int32_t d[3];
+    long long d[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        d[a] = exact_units(p[a], em.eref[a], em.ok) - em.m0[a];
-        em.ok &= (uint32_t)(d[a] + (1 << 26)) < (1u << 27);
+        d[a] = exact_units(p[a], em.e0[a], em.rep[a], em.tz[a], em.ok) - em.m0[a];
         em.s1[a] += d[a];
     }
-    em.s2[0] += (long long)d[0] * d[0];
-    em.s2[1] += (long long)d[0] * d[1];
-    em.s2[2] += (long long)d[0] * d[2];
-    em.s2[3] += (long long)d[1] * d[1];
-    em.s2[4] += (long long)d[1] * d[2];
-    em.s2[5] += (long long)d[2] * d[2];
+    add_prod128(em.s2h[0], em.s2l[0], d[0], d[0]);
+    add_prod128(em.s2h[1], em.s2l[1], d[0], d[1]);
+    add_prod128(em.s2h[2], em.s2l[2], d[0], d[2]);
+    add_prod128(em.s2h[3], em.s2l[3], d[1], d[1]);
+    add_prod128(em.s2h[4], em.s2l[4], d[1], d[2]);
+    add_prod128(em.s2h[5], em.s2l[5], d[2], d[2]);
 }
 
 // 2^e as an FP64 (normal range)
@@ -1005,34 +1045,55 @@ __device__ __forceinline__ double i128_to_double(long long hi, unsigned long lon
     return neg ? -v : v;
 }
 
-// mean and covariance from exact sums over n points; s2 as 128-bit (hi, lo) pairs
-__device__ __forceinline__ void exact_finish(const ExactMoments& em, uint32_t n,
-                                             const long long* s2hi,
-                                             const unsigned long long* s2lo, double* mean,
-                                             double* A) {
+// Mean and covariance from exact sums over n points. Returns a mask of the axes whose mean
+// the exact sums cannot give (bit a set: take the FP64 running sum of axis a).
+__device__ __forceinline__ int exact_finish(const ExactMoments& em, uint32_t n, double* mean,
+                                            double* A) {
     const double nn = (double)n;
+    int redo = 0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const long long tot = em.s1[a] + (long long)n * em.m0[a];
-        mean[a] = ((double)tot * pow2d(em.eref[a] - 150)) / nn;
+        const unsigned long long mag = tot < 0 ? (unsigned long long)(-tot) : (unsigned long long)tot;
+        const int sig = mag ? 64 - __clzll((long long)mag) - min(em.tz[a], 63) : 0;
+        if (em.rep[a] && sig <= 53) {
+            mean[a] = (__ll2double_rn(tot) * pow2d(em.e0[a])) / nn;
+        } else {
+            redo |= 1 << a;
+        }
     }
     const double inv_den = 1.0 / (nn * (double)(n - 1u));
     const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         // n S2 (128-bit times a small unsigned) minus S1_a S1_b (64 x 64 -> 128), exact
-        const unsigned long long nl = s2lo[k] * (unsigned long long)n;
-        const long long nh =
-            s2hi[k] * (long long)n + (long long)__umul64hi(s2lo[k], (unsigned long long)n);
+        const unsigned long long nl = em.s2l[k] * (unsigned long long)n;
+        const long long nh = em.s2h[k] * (long long)n +
+                             (long long)__umul64hi(em.s2l[k], (unsigned long long)n);
         const long long pa = em.s1[ia[k]], pb = em.s1[ib[k]];
         const unsigned long long ql = (unsigned long long)pa * (unsigned long long)pb;
         const long long qh = __mul64hi(pa, pb);
         const unsigned long long rl = nl - ql;
         const long long rh = nh - qh - (nl < ql ? 1ll : 0ll);
         const double v =
-            i128_to_double(rh, rl) * pow2d(em.eref[ia[k]] + em.eref[ib[k]] - 300) * inv_den;
+            i128_to_double(rh, rl) * pow2d(em.e0[ia[k]] + em.e0[ib[k]]) * inv_den;
         A[ia[k] * 3 + ib[k]] = A[ib[k] * 3 + ia[k]] = v;
     }
+    return redo;
+}
+
+// The FP64 running sums of the axes in `axes` (bit mask) over the points in input order, the
+// means fl(sum / n) (build_voxel_grid_cpu's accumulation)
+template <class Each>
+__device__ __noinline__ void moments_mean_fp64(Each each, uint32_t cnt, int axes, double* mean) {
+    double sum[3] = {0.0, 0.0, 0.0};
+    each([&](const float* p) {
+        sum[0] += (double)p[0];
+        sum[1] += (double)p[1];
+        sum[2] += (double)p[2];
+    });
+    for (int a = 0; a < 3; ++a)
+        if (axes >> a & 1) mean[a] = sum[a] / (double)cnt;
 }
 
 // FP64 centred two-pass moments of one voxel's points, visited in input order by each(f) (f
@@ -1082,34 +1143,30 @@ __device__ __forceinline__ bool voxel_finish(const double* mean, const double* A
     return true;
 }
 
-// Largest voxel one thread sums exactly (the int64 bound of the second moments)
-constexpr uint32_t EXACT_THREAD_MAX = 2048;
+// Largest voxel whose sums stay exact (S1 below 2^57, S2 below 2^98 with |d| < 2^41)
+constexpr uint32_t EXACT_MAX_POINTS = 65536;
 
-// Statistics of one voxel by one thread: count, then exact moments when the voxel has at most
-// EXACT_THREAD_MAX points and they stay within the exact bounds, else FP64 two-pass moments;
-// then voxel_finish. each(f) visits the voxel's points in input order; first: its first point.
-// r.coord is the caller's.
+// Statistics of one voxel by one thread: count, then exact moments (FP64 running sums for
+// the axes whose mean they cannot give) when the voxel has at most EXACT_MAX_POINTS points
+// within the exact bounds, else FP64 two-pass moments; then voxel_finish. each(f) visits the
+// voxel's points in input order; first: its first point. r.coord (the voxel's cell) is the
+// caller's.
 template <class Each>
 __device__ __forceinline__ bool voxel_stats(Each each, const float* first, uint32_t cnt,
-                                            int min_points, float ratio, SegRec& r) {
+                                            int min_points, float ratio, float res, SegRec& r) {
     r.count = cnt;
     if ((int)cnt < min_points) return false;
     double mean[3], A[9];
-    bool exact = cnt <= EXACT_THREAD_MAX;
+    bool exact = cnt <= EXACT_MAX_POINTS;
     ExactMoments em;
     if (exact) {
-        exact_begin(em, first);
+        exact_begin(em, first, r.coord, res);
         each([&](const float* p) { exact_add(em, p); });
         exact = em.ok;
     }
     if (exact) {
-        long long hi[6];
-        unsigned long long lo[6];
-        for (int k = 0; k < 6; ++k) {
-            hi[k] = em.s2[k] >> 63;
-            lo[k] = (unsigned long long)em.s2[k];
-        }
-        exact_finish(em, cnt, hi, lo, mean, A);
+        const int redo = exact_finish(em, cnt, mean, A);
+        if (redo) moments_mean_fp64(each, cnt, redo, mean);
     } else {
         moments_two_pass(each, cnt, mean, A);
     }
@@ -1149,8 +1206,8 @@ struct SegSums {
     long long s1[3];
     long long hi[6];
     unsigned long long lo[6];
-    int32_t ok;
-    int32_t pad;
+    int32_t tz[3];
+    int32_t flags;  // bit 0: the exact route holds; bits 1-3: axis a's points all exact
 };
 
 // Segments in visit order (order[t], largest first; skey[t] its sorted size key). The first
@@ -1192,20 +1249,28 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
             const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
             const uint32_t cnt = e - b;
             if ((int)cnt < min_points) continue;
+            const float* first = pts + 3 * (size_t)sidx[b];
+            int32_t coord[3];
+            cell_of(first, res, coord);
             ExactMoments em;
-            exact_begin(em, pts + 3 * (size_t)sidx[b]);
+            exact_begin(em, first, coord, res);
             for (uint32_t k = b + lane; k < e; k += 32) exact_add(em, pts + 3 * (size_t)sidx[k]);
-            const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= 32u * EXACT_THREAD_MAX;
+            const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= EXACT_MAX_POINTS;
+            int flags = exact ? 1 : 0;
             if (exact) {
 #pragma unroll
-                for (int a = 0; a < 3; ++a)
+                for (int a = 0; a < 3; ++a) {
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1)
+                    for (int o = 16; o > 0; o >>= 1) {
                         em.s1[a] += __shfl_xor_sync(0xffffffffu, em.s1[a], o);
+                        em.tz[a] = min(em.tz[a], __shfl_xor_sync(0xffffffffu, em.tz[a], o));
+                    }
+                    if (__all_sync(0xffffffffu, em.rep[a])) flags |= 2 << a;
+                }
 #pragma unroll
                 for (int k = 0; k < 6; ++k) {
-                    long long h = em.s2[k] >> 63;
-                    unsigned long long l = (unsigned long long)em.s2[k];
+                    long long h = em.s2h[k];
+                    unsigned long long l = em.s2l[k];
                     warp_sum128(h, l);
                     if (lane == j) {
                         st[j].hi[k] = h;
@@ -1213,9 +1278,12 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
                     }
                 }
                 if (lane == j)
-                    for (int a = 0; a < 3; ++a) st[j].s1[a] = em.s1[a];
+                    for (int a = 0; a < 3; ++a) {
+                        st[j].s1[a] = em.s1[a];
+                        st[j].tz[a] = em.tz[a];
+                    }
             }
-            if (lane == j) st[j].ok = exact ? 1 : 0;
+            if (lane == j) st[j].flags = flags;
         }
         __syncwarp();
         if (lane < gn) {
@@ -1230,15 +1298,25 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
             bool ok = false;
             if ((int)cnt >= min_points) {
                 double mean[3], A[9];
-                if (st[lane].ok) {
+                auto each = [&](auto f) {
+                    for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
+                };
+                const int flags = st[lane].flags;
+                if (flags & 1) {
                     ExactMoments em;
-                    exact_begin(em, first);
-                    for (int a = 0; a < 3; ++a) em.s1[a] = st[lane].s1[a];
-                    exact_finish(em, cnt, st[lane].hi, st[lane].lo, mean, A);
+                    exact_begin(em, first, r.coord, res);
+                    for (int a = 0; a < 3; ++a) {
+                        em.s1[a] = st[lane].s1[a];
+                        em.tz[a] = st[lane].tz[a];
+                        em.rep[a] = (flags >> (a + 1)) & 1;
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        em.s2h[k] = st[lane].hi[k];
+                        em.s2l[k] = st[lane].lo[k];
+                    }
+                    const int redo = exact_finish(em, cnt, mean, A);
+                    if (redo) moments_mean_fp64(each, cnt, redo, mean);
                 } else {
-                    auto each = [&](auto f) {
-                        for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
-                    };
                     moments_two_pass(each, cnt, mean, A);
                 }
                 ok = voxel_finish(mean, A, ratio, r);
@@ -1259,7 +1337,7 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
     auto each = [&](auto f) {
         for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
     };
-    const bool ok = voxel_stats(each, first, e - b, min_points, ratio, r);
+    const bool ok = voxel_stats(each, first, e - b, min_points, ratio, res, r);
     rec[s] = r;
     valid[s] = ok ? 1u : 0u;
 }
@@ -1289,28 +1367,36 @@ __global__ void k_hash_insert(const int32_t* __restrict__ coord, const float4* _
                               uint4* __restrict__ slots, float4* __restrict__ slot_icov,
                               int32_t* __restrict__ slot_vidx, uint32_t* __restrict__ max_probe,
                               uint32_t* __restrict__ status) {
-    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
-    int32_t gx = coord[3 * v], gy = coord[3 * v + 1], gz = coord[3 * v + 2];
-    uint32_t key, s;
-    cell_slot(m, gx, gy, gz, key, s);  // every voxel lies inside the map's bounding box
-    for (uint32_t j = 0; j <= m.mask; ++j) {
-        uint32_t old = atomicCAS(&slots[s].x, EMPTY_KEY, key);
-        if (old == EMPTY_KEY) {
-            float4 mu = mean4[v];
-            slots[s].y = __float_as_uint(mu.x);
-            slots[s].z = __float_as_uint(mu.y);
-            slots[s].w = __float_as_uint(mu.z);
-            const float* c = icov + 9 * (size_t)v;
-            slot_icov[2 * (size_t)s] = make_float4(c[0], c[1], c[2], c[4]);
-            slot_icov[2 * (size_t)s + 1] = make_float4(c[5], c[8], 0.f, 0.f);
-            slot_vidx[s] = (int32_t)v;
-            atomicMax(max_probe, j);
-            return;
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t disp = 0;  // this voxel's displacement from its home slot
+    if (v < nv) {
+        const int32_t gx = coord[3 * v], gy = coord[3 * v + 1], gz = coord[3 * v + 2];
+        uint32_t key, s;
+        cell_slot(m, gx, gy, gz, key, s);  // every voxel lies inside the map's bounding box
+        bool placed = false;
+        for (uint32_t j = 0; j <= m.mask; ++j) {
+            const uint32_t old = atomicCAS(&slots[s].x, EMPTY_KEY, key);
+            if (old == EMPTY_KEY) {
+                const float4 mu = mean4[v];
+                slots[s].y = __float_as_uint(mu.x);
+                slots[s].z = __float_as_uint(mu.y);
+                slots[s].w = __float_as_uint(mu.z);
+                const float* c = icov + 9 * (size_t)v;
+                slot_icov[2 * (size_t)s] = make_float4(c[0], c[1], c[2], c[4]);
+                slot_icov[2 * (size_t)s + 1] = make_float4(c[5], c[8], 0.f, 0.f);
+                slot_vidx[s] = (int32_t)v;
+                disp = j;
+                placed = true;
+                break;
+            }
+            s = (s + 1) & m.mask;
         }
-        s = (s + 1) & m.mask;
+        if (!placed) atomicOr(status, ST_HASH_FULL);
     }
-    atomicOr(status, ST_HASH_FULL);
+    // the largest displacement: one atomic per warp that has a displaced voxel (3M threads on
+    // one counter would queue at its L2 slice)
+    disp = __reduce_max_sync(0xffffffffu, disp);
+    if ((threadIdx.x & 31u) == 0 && disp) atomicMax(max_probe, disp);
 }
 
 // Dense cell index: every occupied hash slot writes {centroid, slot} into the entry of its
@@ -1613,7 +1699,7 @@ __global__ void k_merge_keys(const TileSegRef* __restrict__ tiles, int nt, uint6
 __global__ void __launch_bounds__(128) k_merge_groups(
     const TileSegRef* __restrict__ tiles, int nt, const uint32_t* __restrict__ members,
     const uint32_t* __restrict__ gstart, const uint32_t* __restrict__ num_groups,
-    uint32_t n_members, int min_points, float ratio, SegRec* __restrict__ grec,
+    uint32_t n_members, int min_points, float ratio, float res, SegRec* __restrict__ grec,
     uint32_t* __restrict__ gvalid) {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t G = *num_groups;
@@ -1651,7 +1737,7 @@ __global__ void __launch_bounds__(128) k_merge_groups(
     };
     locate(members[m0], t, sl);
     const float* first = tiles[t].pts + 3 * (size_t)tiles[t].idx[tiles[t].starts[sl]];
-    const bool ok = voxel_stats(each, first, cnt, min_points, ratio, r);
+    const bool ok = voxel_stats(each, first, cnt, min_points, ratio, res, r);
     grec[g] = r;
     gvalid[g] = ok ? 1u : 0u;
 }
@@ -1715,7 +1801,7 @@ int merge_tiles(Map& map, BuildScratch& sc, const std::vector<TileSegRef>& refs,
         return rc;
     k_merge_groups<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
         dref, nt, vals, (const uint32_t*)sc.seg_starts.p, ngroups, (uint32_t)total,
-        cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
+        cfg.min_points_per_voxel, cfg.eigenvalue_ratio, cfg.resolution, (SegRec*)sc.seg_rec.p,
         (uint32_t*)sc.seg_valid.p);
     cudaMemcpyAsync(&g.S, ngroups, 4, cudaMemcpyDeviceToHost, s);
     if ((rc = cuda_fail(cudaStreamSynchronize(s), "tile merge"))) return rc;
