@@ -309,12 +309,12 @@ def _pose_ok(pose, truth):
     return np.linalg.norm(pose[:2] - truth[:2]) < 0.2 and abs(dyaw) < np.radians(1.0)
 
 
-def learned_bench(steps=60000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01):
+def learned_bench(steps=15000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01, **net_cfg):
     """Learned initial-pose proposals vs the plain 200-particle search.
 
     Training: n_maps seeded 200x200 m maps of the sequence generator with n_train scans each;
     labels are plain NDT's converged poses; perturbations x, y U(+-5 m), yaw uniform, drawn on
-    the device (steps x 256 samples). Evaluation: n_test held-out scans per map, coarse poses
+    the device (steps x train_batch samples, 1024 per step by default). Evaluation: n_test held-out scans per map, coarse poses
     x, y U(+-5 m) with an unknown heading. Plain = 200 particles over the same range;
     learned = 16 proposals refined by NDT; refine8 = then 8 particles (x, y +- 0.5 m, yaw +-
     5 deg) around each query's winner, aligned as a second round; fallback = the plain
@@ -328,7 +328,7 @@ def learned_bench(steps=60000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
     from cuda_ndt_matcher_gb300 import capi, synth
     t0 = time.perf_counter()
     maps = synth.proposal_maps(seed=100, n_maps=n_maps, n_train=n_train, n_test=n_test)
-    net = capi.PNet(seed=7)
+    net = capi.PNet(seed=7, **net_cfg)
     ctx = capi.Context(cuda_graph=1)
     mids = []
     for m in maps:
@@ -348,7 +348,7 @@ def learned_bench(steps=60000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
     cfg = net.cfg
     dims = [cfg.input_dim] + [cfg.hidden] * cfg.hidden_layers + [4 * cfg.proposals]
     pairs = list(zip(dims[:-1], dims[1:]))
-    flops_step = 2 * cfg.batch * (2 * sum(i * o for i, o in pairs) + sum(i * o for i, o in pairs[1:]))
+    flops_step = 2 * cfg.train_batch * (2 * sum(i * o for i, o in pairs) + sum(i * o for i, o in pairs[1:]))
     rng = np.random.default_rng(99)
     names = ("plain_200", "learned_16", "learned_16_refine8", "learned_16_refine8_fallback",
              "learned_16_refine8_fallback29")
@@ -399,7 +399,8 @@ def learned_bench(steps=60000, n_maps=50, n_train=400, n_test=200, nvtl_tol=0.01
         n += len(m.test_poses)
     res = {"metric": "init-pose est/s, learned vs plain", "queries": n,
            "training": {"maps": len(maps), "scans": sum(len(m.train_scans) for m in maps),
-                        "steps": steps, "samples": steps * cfg.batch, "seconds": train_s,
+                        "steps": steps, "batch": cfg.train_batch, "samples": steps * cfg.train_batch,
+                        "seconds": train_s,
                         "device_ms": nst["train_ms"], "prep_seconds": prep,
                         "final_loss": float(loss.mean()),
                         "roofline": {"bound": "tensor", "kernel": "k_gemm_bf16_tn (training step)",

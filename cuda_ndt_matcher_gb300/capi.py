@@ -101,7 +101,8 @@ class PoseEstimate(C.Structure):
 class PNetConfig(C.Structure):
     _fields_ = [("input_dim", C.c_int32), ("hidden", C.c_int32), ("hidden_layers", C.c_int32),
                 ("proposals", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_float),
-                ("xy_range", C.c_float), ("yaw_weight", C.c_float), ("seed", C.c_uint64)]
+                ("xy_range", C.c_float), ("yaw_weight", C.c_float), ("seed", C.c_uint64),
+                ("train_batch", C.c_int32), ("reserved", C.c_int32)]
 
 
 class PNetStats(C.Structure):

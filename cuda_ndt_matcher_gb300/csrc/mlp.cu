@@ -26,6 +26,7 @@
 //   L = e_j* + CE(softmax(logits), j*) + 0.05 mean_{j != j*} e_j,   averaged over the batch.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -171,27 +172,56 @@ struct AdamTable {
     uint64_t start[2 * PN_MAX_LAYERS + 1];
     int tensors;
 };
+// Four consecutive elements per thread (every tensor's size and start is a multiple of 4):
+// 16-byte loads and stores of the f32 state, 8-byte stores of the bf16 copy. The bias
+// corrections are formed once per block.
 __global__ void k_adam_all(const AdamTable t, const uint64_t* __restrict__ step_ctr, float lr,
                            float b1, float b2, float eps) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ float s_c[2];
+    if (threadIdx.x == 0) {
+        const float step = (float)*step_ctr;
+        s_c[0] = lr / (1.f - powf(b1, step));  // lr / (1 - b1^t)
+        s_c[1] = 1.f / (1.f - powf(b2, step));  // 1 / (1 - b2^t)
+    }
+    __syncthreads();
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4ull;
     if (i >= t.start[t.tensors]) return;
     int k = 0;
     while (i >= t.start[k + 1]) ++k;
     const size_t j = (size_t)(i - t.start[k]);
-    const float step = (float)*step_ctr;
-    const float c1 = 1.f - powf(b1, step), c2 = 1.f - powf(b2, step);
-    const float gi = t.g[k][j];
-    const float mi = b1 * t.m[k][j] + (1.f - b1) * gi;
-    const float vi = b2 * t.v[k][j] + (1.f - b2) * gi * gi;
-    t.m[k][j] = mi;
-    t.v[k][j] = vi;
-    const float wi = t.w[k][j] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    t.w[k][j] = wi;
+    const float lc1 = s_c[0], ic2 = s_c[1];
+    const float4 g4 = *reinterpret_cast<const float4*>(t.g[k] + j);
+    float4 m4 = *reinterpret_cast<const float4*>(t.m[k] + j);
+    float4 v4 = *reinterpret_cast<const float4*>(t.v[k] + j);
+    float4 w4 = *reinterpret_cast<const float4*>(t.w[k] + j);
+    float* const gm[4] = {&m4.x, &m4.y, &m4.z, &m4.w};
+    float* const gv[4] = {&v4.x, &v4.y, &v4.z, &v4.w};
+    float* const gw[4] = {&w4.x, &w4.y, &w4.z, &w4.w};
+    const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float mi = b1 * *gm[q] + (1.f - b1) * gg[q];
+        const float vi = b2 * *gv[q] + (1.f - b2) * gg[q] * gg[q];
+        *gm[q] = mi;
+        *gv[q] = vi;
+        *gw[q] -= lc1 * mi / (sqrtf(vi * ic2) + eps);
+    }
+    *reinterpret_cast<float4*>(t.m[k] + j) = m4;
+    *reinterpret_cast<float4*>(t.v[k] + j) = v4;
+    *reinterpret_cast<float4*>(t.w[k] + j) = w4;
     if (t.wb[k]) {
-        const __nv_bfloat16 h = __float2bfloat16(wi);
-        t.wb[k][j] = h;
-        const int C = t.cols[k];
-        if (t.wbt[k]) t.wbt[k][(size_t)(j % C) * t.rows[k] + j / C] = h;
+        const __nv_bfloat162 h01 = __floats2bfloat162_rn(w4.x, w4.y);
+        const __nv_bfloat162 h23 = __floats2bfloat162_rn(w4.z, w4.w);
+        __nv_bfloat162* wb2 = reinterpret_cast<__nv_bfloat162*>(t.wb[k] + j);
+        wb2[0] = h01;
+        wb2[1] = h23;
+        if (t.wbt[k]) {
+            const int C = t.cols[k];
+            const __nv_bfloat16 hs[4] = {h01.x, h01.y, h23.x, h23.y};
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                t.wbt[k][(size_t)((j + q) % C) * t.rows[k] + (j + q) / C] = hs[q];
+        }
     }
 }
 
@@ -596,7 +626,7 @@ static int pn_adam(ndt_pnet* p) {
         ++k;
     }
     t.tensors = k;
-    k_adam_all<<<blocks(t.start[k]), 256, 0, p->stream>>>(
+    k_adam_all<<<blocks((t.start[k] + 3) / 4), 256, 0, p->stream>>>(
         t, (const uint64_t*)p->step_ctr.p, p->cfg.learning_rate, 0.9f, 0.999f, 1e-8f);
     return cuda_fail(cudaGetLastError(), "proposal update");
 }
@@ -640,6 +670,7 @@ int ndt_pnet_config_default(ndt_pnet_config* c) {
     c->hidden_layers = 4;
     c->proposals = 16;
     c->batch = 256;
+    c->train_batch = 1024;
     c->learning_rate = 3e-4f;
     c->xy_range = 5.0f;
     c->yaw_weight = 8.0f;
@@ -658,12 +689,13 @@ int ndt_pnet_create(const ndt_pnet_config* cfg, int32_t device, ndt_pnet** out) 
     const int no = c.proposals * PN_OUT_PER;
     if (c.input_dim <= 0 || c.input_dim % 64 || c.hidden <= 0 || c.hidden % 64 ||
         c.hidden_layers < 1 || c.hidden_layers + 1 > PN_MAX_LAYERS || c.proposals < 1 ||
-        no % 64 || c.batch < 1 || c.batch % 64 ||
+        no % 64 || c.batch < 1 || c.batch % 64 || c.train_batch < 0 || c.train_batch % 64 ||
         !(c.learning_rate > 0.f)) {
-        set_error("proposal network: input_dim, hidden, 4 * proposals and batch must be "
-                  "positive multiples of 64");
+        set_error("proposal network: input_dim, hidden, 4 * proposals, batch and train_batch "
+                  "must be positive multiples of 64");
         return NDT_ERR_INVALID_ARGUMENT;
     }
+    if (c.train_batch == 0) c.train_batch = c.batch;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device) {
         set_error("no CUDA device available");
@@ -716,7 +748,7 @@ int ndt_pnet_create(const ndt_pnet_config* cfg, int32_t device, ndt_pnet** out) 
                                                      (__nv_bfloat16*)L.wbt.p);
         rc = cuda_fail(cudaStreamSynchronize(p->stream), "proposal network init");
     }
-    if (!rc) rc = pn_reserve_batch(p, c.batch);
+    if (!rc) rc = pn_reserve_batch(p, std::max(c.batch, c.train_batch));
     if (rc) {
         ndt_pnet_destroy(p);
         return rc;
@@ -835,7 +867,7 @@ int ndt_pnet_train(ndt_pnet* p, uint64_t steps, float* loss_out) {
     cudaSetDevice(p->device);
     int rc = pn_upload_data(p);
     if (rc) return rc;
-    const int B = p->cfg.batch;
+    const int B = p->cfg.train_batch;
     cudaStream_t s = p->stream;
     cudaEventRecord(p->ev0, s);
     for (uint64_t it = 0; it < steps; ++it) {

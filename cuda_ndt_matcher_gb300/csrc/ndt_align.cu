@@ -785,6 +785,12 @@ __device__ __forceinline__ void point_pairs(const MapView& m, const float* pv, c
     float S = 0.f, G0 = 0.f, G1 = 0.f, G2 = 0.f;
     float M0 = 0.f, M1 = 0.f, M2 = 0.f, M3 = 0.f, M4 = 0.f, M5 = 0.f;
     const float d1d2 = d1f * d2f;
+    // e = exp(-d2 sq / 2) as 2^(k2 sq) with k2 = -d2 log2(e) / 2 carried as two floats (the
+    // constant -log2(e) / 2 split into two floats, then an exact product split: k2h + k2l), so the
+    // argument is as accurate as the product d2 sq itself: two operations and the base-2
+    // exponential per pair
+    const float k2h = d2f * -0.72134751081466674805f;
+    const float k2l = fmaf(d2f, -0.72134751081466674805f, -k2h) + d2f * -9.6298151675000554e-09f;
 #pragma unroll 1
     for (int j = 0; j < cnt; ++j) {
         const uint32_t s = nbl[j * nbl_stride];
@@ -799,7 +805,7 @@ __device__ __forceinline__ void point_pairs(const MapView& m, const float* pv, c
         const float c1 = fmaf(ca.y, x0, fmaf(ca.w, x1, cb.x * x2));
         const float c2 = fmaf(ca.z, x0, fmaf(cb.x, x1, cb.y * x2));
         const float sq = fmaf(x0, c0, fmaf(x1, c1, x2 * c2));
-        const float e = expf(-0.5f * d2f * sq);
+        const float e = exp2f(fmaf(k2h, sq, k2l * sq));
         if (CPU_SEM) {
             const float wn = d2f * e;  // compute_derivative_single: zero unless d2*e in [0,1]
             if (!(wn >= 0.f && wn <= 1.f)) continue;

@@ -355,12 +355,15 @@ typedef struct ndt_pnet_config {
     int32_t hidden;                /* 512 */
     int32_t hidden_layers;         /* 4 */
     int32_t proposals;             /* 16 */
-    int32_t batch;                 /* 256: training batch, inference chunk */
+    int32_t batch;                 /* 256: inference chunk (queries per network launch) */
     float learning_rate;           /* Adam, 3e-4 */
     float xy_range;                /* training perturbation of x, y (m): 5 */
     float yaw_weight;              /* loss weight of the yaw error (its scale pi / yaw_weight
                                       against 4 m for x, y): 8 */
     uint64_t seed;                 /* weight initialisation and training samples */
+    int32_t train_batch;           /* samples per training step, a multiple of 64 (0: batch);
+                                      default 1024 */
+    int32_t reserved;
 } ndt_pnet_config;
 
 typedef struct ndt_pnet ndt_pnet;
