@@ -40,7 +40,7 @@ FLOP_PER_PAIR = 65
 # DRAM bytes (read + write) of one Newton-kernel launch of the default workload (256 scans,
 # 5M-point map, seed 2), from one ncu capture of this bench per kernel form
 NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
-                     ("k_ndt_queue", 256, 5_000_000, 2): 109.4e6}
+                     ("k_ndt_queue", 256, 5_000_000, 2): 117.0e6}
 
 
 def _json_default(o):
@@ -64,7 +64,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--only", default="",
                     help="comma-separated extra workloads to run instead of all of them "
-                         "(init_pose, queue, learned, large_map); with --steps 0 only those")
+                         "(init_pose, queue, learned, large_map, large_build, tiles); with "
+                         "--steps 0 only those")
     ap.add_argument("--parity", type=int, default=1,
                     help="after timing, check 64 scans of the timed batch against the FP64 "
                          "oracle and the reference's own kernels")
@@ -576,6 +577,30 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
     return out
 
 
+def large_build_bench(n_points=50_000_000, repeats=3):
+    """The large map's builds alone: the 50M-point 2 x 2 km map set as the target at 1, 2 and
+    3 m, one untimed build (allocations) then `repeats` builds, CUDA-event time of each; bytes
+    by build_bytes."""
+    from cuda_ndt_matcher_gb300 import capi, synth
+    pts = synth.large_map(seed=7, extent=2000.0, n_points=n_points)
+    out = {}
+    for res in (1.0, 2.0, 3.0):
+        ctx = capi.Context(resolution=res)
+        ctx.set_target(pts)
+        ms = []
+        for _ in range(repeats):
+            ctx.set_target(pts)
+            ms.append(float(ctx.map_info().build_ms))
+        info = ctx.map_info()
+        b = build_bytes(info)
+        out[f"{res:g}m"] = {"voxels": int(info.num_voxels), "segments": int(info.num_segments),
+                            "build_ms": min(ms), "bytes": b,
+                            "build_gbs": b / (min(ms) / 1e3) / 1e9,
+                            "build_hbm_frac": b / (min(ms) / 1e3) / 1e9 / peaks()[0]["hbm_gbs"]}
+        ctx.close()
+    return out
+
+
 def parity_sample(seq_map, scans, poses, results, n=64):
     """Checker run after the timed regions: the first n scans of the timed batch, as the last
     timed step aligned them, against the FP64 oracle (graph semantics, the same inputs) and
@@ -975,7 +1000,7 @@ def run_ours(args):
 
 def run_only(names, args):
     """The named extra workloads alone (comma-separated: init_pose, queue, learned,
-    large_map, tiles)."""
+    large_map, large_build, tiles)."""
     out = {}
     for nm in names.split(","):
         if nm == "init_pose":
@@ -986,6 +1011,8 @@ def run_only(names, args):
             out["learned_init_pose"] = learned_bench()
         elif nm == "large_map":
             out["large_map"] = large_map_bench()
+        elif nm == "large_build":
+            out["large_build"] = large_build_bench()
         elif nm == "tiles":
             from cuda_ndt_matcher_gb300 import synth
             pts = synth.large_map(seed=7, extent=2000.0, n_points=50_000_000)
