@@ -38,6 +38,7 @@ def test_struct_layouts():
     assert C.sizeof(capi.Result) == 6 * 8 + 3 * 8 + 36 * 8 + 6 * 4
     assert C.sizeof(capi.Config) == 96
     assert C.sizeof(capi.TuneResult) == 48
+    assert C.sizeof(capi.PNetConfig) == 48
     assert C.sizeof(capi.Scan) == 8 + 8 + 48
     assert C.sizeof(capi.ParticleConfig) == 4 + 4 + 4 * 8 + 8
     assert C.sizeof(capi.PoseEstimate) == 12 * 8 + 3 * 8 + 4 * 4
