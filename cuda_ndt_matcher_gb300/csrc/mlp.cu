@@ -97,16 +97,32 @@ struct ColsumTable {
     int start[PN_MAX_LAYERS + 1];
     int layers;
 };
-__global__ void k_colsum_all(const ColsumTable t, int B) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= t.start[t.layers]) return;
-    int l = 0;
-    while (c >= t.start[l + 1]) ++l;
-    const int n = c - t.start[l], N = t.n[l];
-    const float* G = t.g[l];
+// One block of 32 x 32 threads per 32 columns: lane x takes column c0 + x, row group y the
+// rows y, y + 32, ... (coalesced 128-byte rows), then the 32 row-group sums of a column are
+// added in a fixed order (deterministic).
+constexpr int PN_CS_ROWS = 32;
+__global__ void __launch_bounds__(32 * PN_CS_ROWS) k_colsum_all(const ColsumTable t, int B) {
+    __shared__ float part[PN_CS_ROWS][33];
+    const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
+    const int c = blockIdx.x * 32 + x;
     float s = 0.f;
-    for (int b = 0; b < B; ++b) s += G[(size_t)b * N + n];
-    t.out[l][n] = s;
+    int l = 0, n = 0;
+    const bool ok = c < t.start[t.layers];
+    if (ok) {
+        while (c >= t.start[l + 1]) ++l;
+        n = c - t.start[l];
+        const int N = t.n[l];
+        const float* G = t.g[l] + n;
+#pragma unroll 4
+        for (int b = y; b < B; b += PN_CS_ROWS) s += G[(size_t)b * N];
+    }
+    part[y][x] = s;
+    __syncthreads();
+    if (y == 0 && ok) {
+        float tot = 0.f;
+        for (int r = 0; r < PN_CS_ROWS; ++r) tot += part[r][x];
+        t.out[l][n] = tot;
+    }
 }
 
 // loss and output gradient, one thread per sample; O [B x P*4] (biased), T [B x 3]
@@ -582,7 +598,7 @@ static int pn_backward(ndt_pnet* p, int B) {
         ct.n[l] = p->L[l].out;
         ct.start[l + 1] = ct.start[l] + p->L[l].out;
     }
-    k_colsum_all<<<blocks(ct.start[nl]), 256, 0, s>>>(ct, B);
+    k_colsum_all<<<(unsigned)((ct.start[nl] + 31) / 32), 32 * PN_CS_ROWS, 0, s>>>(ct, B);
     return cuda_fail(cudaGetLastError(), "proposal backward");
 }
 
