@@ -67,7 +67,6 @@ struct BuildScratch {
 
 // Temporary-storage sizing of the sort / scan primitives (two-phase convention).
 size_t radix_sort_temp_bytes(size_t n);
-size_t radix_sort_temp_bytes32(size_t n);
 size_t scan_temp_bytes(size_t n);
 int radix_sort_pairs(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
                      void* temp, size_t temp_bytes, cudaStream_t s);

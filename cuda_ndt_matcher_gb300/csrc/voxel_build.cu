@@ -290,7 +290,6 @@ static size_t radix_temp_bytes(size_t n) {
 }
 
 size_t radix_sort_temp_bytes(size_t n) { return radix_temp_bytes<uint64_t>(n); }
-size_t radix_sort_temp_bytes32(size_t n) { return radix_temp_bytes<uint32_t>(n); }
 
 template <typename K>
 static int radix_sort_t(K* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
@@ -1186,7 +1185,7 @@ __global__ void k_seg_size_keys(const uint32_t* __restrict__ starts, uint32_t S,
 }
 
 // Voxels of at least WARP_SEG_MIN points are summed by a whole warp (exact sums of the lanes'
-// strided shares, added over the lanes in 128-bit); up to EXACT_THREAD_MAX points per lane.
+// strided shares, added over the lanes in 128-bit), up to EXACT_MAX_POINTS points.
 constexpr uint32_t WARP_SEG_MIN = 48;
 
 // 128-bit (hi, lo) sum over the warp's lanes (every lane ends with the total)
@@ -1199,6 +1198,29 @@ __device__ __forceinline__ void warp_sum128(long long& hi, unsigned long long& l
         hi = hi + oh + (s < lo ? 1ll : 0ll);
         lo = s;
     }
+}
+
+// f(point) for the points sidx[k], k = b, b + step, ... < e, in that order, with the loads of
+// four points issued together (the gathers are random reads of the map: four in flight per
+// thread instead of one)
+template <class F>
+__device__ __forceinline__ void visit_points(const float* __restrict__ pts,
+                                             const uint32_t* __restrict__ sidx, uint32_t b,
+                                             uint32_t e, uint32_t step, F f) {
+    uint32_t k = b;
+    for (; k + 3 * step < e; k += 4 * step) {
+        float v[4][3];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float* q = pts + 3 * (size_t)sidx[k + j * step];
+            v[j][0] = q[0];
+            v[j][1] = q[1];
+            v[j][2] = q[2];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) f(v[j]);
+    }
+    for (; k < e; k += step) f(pts + 3 * (size_t)sidx[k]);
 }
 
 // Exact sums of one large segment, as a warp leaves them for the lane that finishes it
@@ -1254,7 +1276,7 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
             cell_of(first, res, coord);
             ExactMoments em;
             exact_begin(em, first, coord, res);
-            for (uint32_t k = b + lane; k < e; k += 32) exact_add(em, pts + 3 * (size_t)sidx[k]);
+            visit_points(pts, sidx, b + lane, e, 32u, [&](const float* p) { exact_add(em, p); });
             const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= EXACT_MAX_POINTS;
             int flags = exact ? 1 : 0;
             if (exact) {
@@ -1334,9 +1356,7 @@ __global__ void __launch_bounds__(128) k_voxel_stats(
     const float* first = pts + 3 * (size_t)sidx[b];
     SegRec r;
     cell_of(first, res, r.coord);
-    auto each = [&](auto f) {
-        for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
-    };
+    auto each = [&](auto f) { visit_points(pts, sidx, b, e, 1u, f); };
     const bool ok = voxel_stats(each, first, e - b, min_points, ratio, res, r);
     rec[s] = r;
     valid[s] = ok ? 1u : 0u;
