@@ -1,7 +1,7 @@
 """GPU voxel-map build vs the oracle, through the C ABI: Morton codes, radix sort order,
-segments, voxel membership/counts/means bit-exact; covariances / inverse covariances
-bit-exact against the oracle's centred FP64 restatement (identical operation sequence)
-and within a few f32 ulp of the reference's uncentred formula."""
+segments, voxel membership/counts/means bit-exact; covariances / inverse covariances within
+2 / 4 f32 ULP of the oracle's centred FP64 restatement and within 1e-4 relative of the
+reference's uncentred formula."""
 import ctypes as C
 import json
 import os
@@ -174,6 +174,47 @@ def test_map_build_matches_oracle(gpu, oracle, name):
     assert rel < 1e-4, rel
     info = ctx.map_info()
     assert info.num_voxels == g.n and info.hash_capacity == g.capacity
+
+
+def _route_map():
+    """Voxels that take every route of the statistics kernel: cells far from the origin (exact
+    sums), cells next to zero with values over many binades, +-0 and subnormals (exact
+    covariance, FP64 running sum for the mean), one warp-summed voxel of 3,000 points, one of
+    70,000 (beyond the exact sums' bound: FP64 two-pass), and many small ones."""
+    rng = np.random.default_rng(5)
+    parts = []
+    far = np.column_stack([rng.integers(-800, 800, (300, 2)), rng.integers(-40, 40, 300)])
+    for c in far:                                       # far cells, 6-60 points
+        n = int(rng.integers(6, 60))
+        parts.append(c * 2.0 + rng.uniform(0, 2, (n, 3)))
+    for _ in range(200):                                # next to zero on z, ground-like
+        n = int(rng.integers(6, 40))
+        xy = rng.integers(-50, 50, 2) * 2.0 + rng.uniform(0, 2, (n, 2))
+        z = rng.normal(0, 0.03, n) * 10.0 ** rng.integers(-6, 1, n)
+        parts.append(np.column_stack([xy, z]))
+    tiny = np.zeros((12, 3))
+    tiny[:, :2] = [10.5, 20.5]
+    tiny[:, 2] = [0.0, -0.0, 1e-40, -1e-41, 1e-38, 3e-39, 1e-30, 1e-20, 0.5, 1.5, 1e-7, 0.25]
+    parts.append(tiny)                                  # zeros and subnormals
+    parts.append(np.array([300.0, 300.0, 4.0]) + rng.uniform(0, 2, (3000, 3)))
+    parts.append(np.array([-300.0, 100.0, 6.0]) + rng.uniform(0, 2, (70000, 3)))
+    pts = np.concatenate(parts).astype(np.float32)
+    return np.ascontiguousarray(pts[rng.permutation(len(pts))])
+
+
+def test_voxel_routes_match_oracle(gpu, oracle):
+    pts = _route_map()
+    ctx = capi.Context()
+    ctx.set_target(pts)
+    coords, means, covs, icovs, counts = ctx.map_voxels()
+    g = oracle.Grid(pts, 2.0, centered=True)
+    assert np.array_equal(coords, g.coords) and np.array_equal(counts, g.counts)
+    assert np.array_equal(means, g.means)
+    assert counts.max() == 70000 and (counts == 3000).any()
+    cu, iu = matrix_ulps(covs, g.covs), matrix_ulps(icovs, g.icovs)
+    print(f"routes: {len(coords)} voxels, covariance max {cu.max():.1f} f32 ULP, inverse max "
+          f"{iu.max():.1f} f32 ULP")
+    assert cu.max() <= 2 and iu.max() <= 4, (cu.max(), iu.max())
 
 
 @pytest.mark.parametrize("cell_index", [0, 1])   # dense cell index / hash probing
