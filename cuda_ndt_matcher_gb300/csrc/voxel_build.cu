@@ -1223,7 +1223,7 @@ __device__ __forceinline__ void visit_points(const float* __restrict__ pts,
     for (; k < e; k += step) f(pts + 3 * (size_t)sidx[k]);
 }
 
-// Exact sums of one large segment, as a warp leaves them for the lane that finishes it
+// Exact sums of one large segment, as a warp leaves them for the thread that finishes it
 struct SegSums {
     long long s1[3];
     long long hi[6];
@@ -1232,132 +1232,131 @@ struct SegSums {
     int32_t flags;  // bit 0: the exact route holds; bits 1-3: axis a's points all exact
 };
 
-// Segments in visit order (order[t], largest first; skey[t] its sorted size key). The first
-// W segments (WARP_SEG_MIN points or more) go to warps in groups of 32: for each segment of
-// its group the warp sums the points exactly (lanes take strided shares, the 128-bit sums
-// are added over the lanes) and lane j keeps segment j's sums; then every lane finishes its
-// own segment (regularisation), the FP64 work spread over the lanes. The rest go one per
-// thread, thread i taking t = W + i. Every segment's record gets its cell and count (a tile
-// merge reads them for cells shared between tiles); valid[s] marks the voxels.
-__global__ void __launch_bounds__(128) k_voxel_stats(
+// Number of visit-order segments with at least WARP_SEG_MIN points (sorted size keys ascend)
+__device__ __forceinline__ uint32_t large_segments(const uint32_t* __restrict__ skey, uint32_t S) {
+    uint32_t lo = 0, hi = S;
+    const uint32_t lim = 0xFFFFu - WARP_SEG_MIN;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (skey[mid] <= lim) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Exact sums of the large segments (the first W in visit order, order[t], largest first),
+// one warp per segment at a time (lanes take strided shares, the 128-bit sums are added over
+// the lanes), into sums[t]. k_voxel_stats finishes them one per thread.
+__global__ void __launch_bounds__(128) k_segment_sums(
     const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
     const uint32_t* __restrict__ starts, const uint32_t* __restrict__ order,
     const uint32_t* __restrict__ skey, uint32_t S, uint32_t nf, float res, int min_points,
-    float ratio, SegRec* __restrict__ rec, uint32_t* __restrict__ valid) {
+    SegSums* __restrict__ sums) {
     __shared__ uint32_t sW;
-    __shared__ SegSums stash[4][32];
-    if (threadIdx.x == 0) {
-        // W = number of keys <= 0xFFFF - WARP_SEG_MIN (keys ascend)
-        uint32_t lo = 0, hi = S;
-        const uint32_t lim = 0xFFFFu - WARP_SEG_MIN;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (skey[mid] <= lim) lo = mid + 1;
-            else hi = mid;
-        }
-        sW = lo;
-    }
+    if (threadIdx.x == 0) sW = large_segments(skey, S);
     __syncthreads();
     const uint32_t W = sW;
-    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    SegSums* const st = stash[wib];
-    for (uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; g0 < W;
-         g0 += warps * 32u) {
-        const uint32_t gn = min(32u, W - g0);
-        for (uint32_t j = 0; j < gn; ++j) {
-            const uint32_t s = order[g0 + j];
-            const uint32_t b = starts[s];
-            const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
-            const uint32_t cnt = e - b;
-            if ((int)cnt < min_points) continue;
-            const float* first = pts + 3 * (size_t)sidx[b];
-            int32_t coord[3];
-            cell_of(first, res, coord);
-            ExactMoments em;
-            exact_begin(em, first, coord, res);
-            visit_points(pts, sidx, b + lane, e, 32u, [&](const float* p) { exact_add(em, p); });
-            const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= EXACT_MAX_POINTS;
-            int flags = exact ? 1 : 0;
-            if (exact) {
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < W; t += warps) {
+        const uint32_t s = order[t];
+        const uint32_t b = starts[s];
+        const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+        const uint32_t cnt = e - b;
+        if ((int)cnt < min_points) continue;
+        const float* first = pts + 3 * (size_t)sidx[b];
+        int32_t coord[3];
+        cell_of(first, res, coord);
+        ExactMoments em;
+        exact_begin(em, first, coord, res);
+        visit_points(pts, sidx, b + lane, e, 32u, [&](const float* p) { exact_add(em, p); });
+        const bool exact = __all_sync(0xffffffffu, em.ok) && cnt <= EXACT_MAX_POINTS;
+        int flags = exact ? 1 : 0;
+        SegSums& o = sums[t];
+        if (exact) {
 #pragma unroll
+            for (int a = 0; a < 3; ++a) {
+#pragma unroll
+                for (int k = 16; k > 0; k >>= 1) {
+                    em.s1[a] += __shfl_xor_sync(0xffffffffu, em.s1[a], k);
+                    em.tz[a] = min(em.tz[a], __shfl_xor_sync(0xffffffffu, em.tz[a], k));
+                }
+                if (__all_sync(0xffffffffu, em.rep[a])) flags |= 2 << a;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                long long h = em.s2h[k];
+                unsigned long long l = em.s2l[k];
+                warp_sum128(h, l);
+                if (lane == 0) {
+                    o.hi[k] = h;
+                    o.lo[k] = l;
+                }
+            }
+            if (lane == 0)
                 for (int a = 0; a < 3; ++a) {
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        em.s1[a] += __shfl_xor_sync(0xffffffffu, em.s1[a], o);
-                        em.tz[a] = min(em.tz[a], __shfl_xor_sync(0xffffffffu, em.tz[a], o));
-                    }
-                    if (__all_sync(0xffffffffu, em.rep[a])) flags |= 2 << a;
+                    o.s1[a] = em.s1[a];
+                    o.tz[a] = em.tz[a];
                 }
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    long long h = em.s2h[k];
-                    unsigned long long l = em.s2l[k];
-                    warp_sum128(h, l);
-                    if (lane == j) {
-                        st[j].hi[k] = h;
-                        st[j].lo[k] = l;
-                    }
-                }
-                if (lane == j)
-                    for (int a = 0; a < 3; ++a) {
-                        st[j].s1[a] = em.s1[a];
-                        st[j].tz[a] = em.tz[a];
-                    }
-            }
-            if (lane == j) st[j].flags = flags;
         }
-        __syncwarp();
-        if (lane < gn) {
-            const uint32_t s = order[g0 + lane];
-            const uint32_t b = starts[s];
-            const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
-            const uint32_t cnt = e - b;
-            const float* first = pts + 3 * (size_t)sidx[b];
-            SegRec r;
-            cell_of(first, res, r.coord);
-            r.count = cnt;
-            bool ok = false;
-            if ((int)cnt >= min_points) {
-                double mean[3], A[9];
-                auto each = [&](auto f) {
-                    for (uint32_t k = b; k < e; ++k) f(pts + 3 * (size_t)sidx[k]);
-                };
-                const int flags = st[lane].flags;
-                if (flags & 1) {
-                    ExactMoments em;
-                    exact_begin(em, first, r.coord, res);
-                    for (int a = 0; a < 3; ++a) {
-                        em.s1[a] = st[lane].s1[a];
-                        em.tz[a] = st[lane].tz[a];
-                        em.rep[a] = (flags >> (a + 1)) & 1;
-                    }
-                    for (int k = 0; k < 6; ++k) {
-                        em.s2h[k] = st[lane].hi[k];
-                        em.s2l[k] = st[lane].lo[k];
-                    }
-                    const int redo = exact_finish(em, cnt, mean, A);
-                    if (redo) moments_mean_fp64(each, cnt, redo, mean);
-                } else {
-                    moments_two_pass(each, cnt, mean, A);
-                }
-                ok = voxel_finish(mean, A, ratio, r);
-            }
-            rec[s] = r;
-            valid[s] = ok ? 1u : 0u;
-        }
-        __syncwarp();
+        if (lane == 0) o.flags = flags;
     }
-    const uint32_t t = W + blockIdx.x * blockDim.x + threadIdx.x;
+}
+
+// One thread per segment in visit order (order[t], largest first; skey[t] its sorted size
+// key). The first W (WARP_SEG_MIN points or more) are finished from their sums in sums[t]
+// (k_segment_sums); the others are summed here. Every segment's record gets its cell and
+// count (a tile merge reads them for cells shared between tiles); valid[s] marks the voxels.
+__global__ void __launch_bounds__(128) k_voxel_stats(
+    const float* __restrict__ pts, const uint32_t* __restrict__ sidx,
+    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ order,
+    const uint32_t* __restrict__ skey, const SegSums* __restrict__ sums, uint32_t S,
+    uint32_t nf, float res, int min_points, float ratio, SegRec* __restrict__ rec,
+    uint32_t* __restrict__ valid) {
+    __shared__ uint32_t sW;
+    if (threadIdx.x == 0) sW = large_segments(skey, S);
+    __syncthreads();
+    const uint32_t W = sW;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= S) return;
     const uint32_t s = order[t];
     const uint32_t b = starts[s];
     const uint32_t e = (s + 1 < S) ? starts[s + 1] : nf;
+    const uint32_t cnt = e - b;
     const float* first = pts + 3 * (size_t)sidx[b];
     SegRec r;
     cell_of(first, res, r.coord);
     auto each = [&](auto f) { visit_points(pts, sidx, b, e, 1u, f); };
-    const bool ok = voxel_stats(each, first, e - b, min_points, ratio, res, r);
+    bool ok;
+    if (t < W) {
+        r.count = cnt;
+        ok = false;
+        if ((int)cnt >= min_points) {
+            double mean[3], A[9];
+            const SegSums& ss = sums[t];
+            const int flags = ss.flags;
+            if (flags & 1) {
+                ExactMoments em;
+                exact_begin(em, first, r.coord, res);
+                for (int a = 0; a < 3; ++a) {
+                    em.s1[a] = ss.s1[a];
+                    em.tz[a] = ss.tz[a];
+                    em.rep[a] = (flags >> (a + 1)) & 1;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    em.s2h[k] = ss.hi[k];
+                    em.s2l[k] = ss.lo[k];
+                }
+                const int redo = exact_finish(em, cnt, mean, A);
+                if (redo) moments_mean_fp64(each, cnt, redo, mean);
+            } else {
+                moments_two_pass(each, cnt, mean, A);
+            }
+            ok = voxel_finish(mean, A, ratio, r);
+        }
+    } else {
+        ok = voxel_stats(each, first, cnt, min_points, ratio, res, r);
+    }
     rec[s] = r;
     valid[s] = ok ? 1u : 0u;
 }
@@ -1569,8 +1568,16 @@ int build_segments(BuildScratch& sc, const float* d_pts, size_t n, const ndt_con
     k_seg_size_keys<<<(g.S + 255) / 256, 256, 0, s>>>((const uint32_t*)sc.seg_starts.p, g.S,
                                                       (uint32_t)g.nf, skeys, order);
     if ((rc = radix_sort_pairs32(skeys, order, g.S, 0, 16, sc.tmp.p, sc.tmp.bytes, s))) return rc;
+    // the large segments' sums into the sort's temporary storage (free again): at most
+    // nf / WARP_SEG_MIN segments of SegSums, well inside its 12 bytes per point
+    SegSums* sums = (SegSums*)sc.tmp.p;
+    const uint32_t wmax = (uint32_t)std::min<size_t>(g.S, g.nf / WARP_SEG_MIN + 1);
+    const unsigned gs = (unsigned)std::min<uint32_t>((wmax + 3) / 4, 152u * 64u);
+    k_segment_sums<<<gs, 128, 0, s>>>(d_pts, vals, (uint32_t*)sc.seg_starts.p, order, skeys,
+                                      g.S, (uint32_t)g.nf, cfg.resolution,
+                                      cfg.min_points_per_voxel, sums);
     k_voxel_stats<<<(g.S + 127) / 128, 128, 0, s>>>(
-        d_pts, vals, (uint32_t*)sc.seg_starts.p, order, skeys, g.S, (uint32_t)g.nf,
+        d_pts, vals, (uint32_t*)sc.seg_starts.p, order, skeys, sums, g.S, (uint32_t)g.nf,
         cfg.resolution, cfg.min_points_per_voxel, cfg.eigenvalue_ratio, (SegRec*)sc.seg_rec.p,
         (uint32_t*)sc.seg_valid.p);
     return cuda_fail(cudaStreamSynchronize(s), "voxel statistics");
