@@ -1980,10 +1980,11 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
             __stcg(&q->max_osc, sh.max_osc);
             __stcg(&q->n_eigen, sh.n_eigen);
             __stcg(&q->have_w, sh.solve.have_w);
+            // every chunk of this iteration has reported: nothing else touches the counter
+            // until the claim word below opens the next iteration
+            P.qjobs[job].done = 0u;
         }
     }
-    __threadfence();
-    __syncwarp();
     if (lane == 0) {
         const unsigned long long c3 = clock64();
         if (t) t[46] = (double)(c3 - c2);  // step + next frame + state store
@@ -1998,14 +1999,17 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
             o.n_eigen = sh.n_eigen;
             o.t_start = __ldcg(&q->t_start);
             o.t_end = global_ns();
-            __threadfence();
+        }
+    }
+    // one release fence for every lane's stores (state, frame, outputs), then the claim word
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) {
+        if (done) {
             atomicExch(&P.qjobs[job].gen_claim, qword(QDONE, 0u));
             atomicAdd(P.qcount, 1u);
         } else {
-            const uint32_t nch = queue_chunks(P, jb.n, it + 1u);
-            P.qjobs[job].done = 0u;
-            __threadfence();
-            atomicExch(&P.qjobs[job].gen_claim, qword(it + 1u, nch));
+            atomicExch(&P.qjobs[job].gen_claim, qword(it + 1u, queue_chunks(P, jb.n, it + 1u)));
         }
     }
     __syncwarp();
