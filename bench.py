@@ -489,8 +489,8 @@ def tile_stream_bench(pts, scans, guesses, events=40):
 def large_map_bench(n_points=50_000_000, n_scans=16):
     """Large-map stress: 50M points over 2 x 2 km (sequence generator densities, 5% uniform
     outliers) built at 1, 2 and 3 m. Per resolution:
-    - build time (CUDA events around the build) and GB/s of the canonical build bytes
-      (248 N + 64 V + 16 cap);
+    - build time (CUDA events around the build) and GB/s of the pipeline's bytes
+      (build_bytes);
     - hash load factor;
     - 20 sampled voxels against the oracle's build of exactly that cell's points: coordinates,
       counts and FP64 means bit for bit, covariance and inverse in f32 ULP of the matrix scale;

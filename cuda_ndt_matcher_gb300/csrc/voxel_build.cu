@@ -1,19 +1,23 @@
 // voxel_build.cu — GPU voxel-map build for sm_103a (the `set_target` hot path).
 //
-// Pipeline (one CUDA stream, no host work between kernels except the two size reads that
-// size the allocations):
+// Pipeline (one CUDA stream, no host work between kernels except the size reads that pick
+// the key width and size the allocations):
 //   1. cells + bounds      : cell = floor(p / res) per finite point (f32 IEEE division, the
 //                            membership rule of VoxelCoord::from_point,
 //                            src/ndt_cuda/src/voxel_grid/types.rs:206-212); min/max cell.
 //   2. Morton keys         : key = morton(cell - min cell), 21 bits per axis
 //                            (src/ndt_cuda/src/voxel_grid/gpu/morton.rs:45-95 layout); the
 //                            non-finite points get key ~0 and sort last.
-//   3. LSD radix sort      : stable, 8-bit digits, only the significant key bits
-//                            (replaces cub::DeviceRadixSort, src/cuda_ffi/csrc/radix_sort.cu).
-//   4. segments            : boundary flags + exclusive scan -> segment id / start
-//                            (src/cuda_ffi/csrc/segment_detect.cu:27-146).
-//   5. voxel statistics    : one thread per segment (one warp per segment of 48 points or
-//                            more), exact integer moments of the segment's points (the FP64
+//   3. LSD radix sort      : stable, 8-bit digits, only the significant key bits, 32-bit
+//                            keys when they fit (replaces cub::DeviceRadixSort,
+//                            src/cuda_ffi/csrc/radix_sort.cu).
+//   4. segments            : per-tile counts of key changes, scanned, then the starts
+//                            (src/cuda_ffi/csrc/segment_detect.cu:27-146; the API's
+//                            ndt_detect_segments keeps flags + scan for the segment ids).
+//   5. voxel statistics    : segments visited largest first; segments of 48 points or more
+//                            summed by a warp each (k_segment_sums), the rest by a thread
+//                            each, every voxel finished by a thread (k_voxel_stats); exact
+//                            integer moments of the segment's points (the FP64
 //                            running sum's mean bit for bit, the centred covariance from an
 //                            exact numerator), FP64 two-pass moments where the exact bounds
 //                            do not hold; eigenvector directions by an f32 Jacobi, refined
