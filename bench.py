@@ -186,8 +186,12 @@ def build_bytes(info):
     per_point = 12 + 12 + kw + 4 + passes * (kw + 2 * (kw + 4)) + 2 * kw + 16
     per_seg = 4 + 8 + 2 * 3 * 8 + 88 + 4
     per_vox = 88 + 104 + 64 + 52 + 27 * 4
-    dense = float(info.dense_grid_mib) * 1024 * 1024  # grid (16 B/cell) + masks (4 B/cell)
-    grid_bytes = 2 * dense * 16 / 20 + dense * 4 / 20
+    # dense index: the grid (16 B per cell of the box: filled, then written) and the
+    # neighbourhood masks (4 B per mask, masks_per_cell per cell of the grown box: filled)
+    dense = float(info.dense_grid_mib) * 1024 * 1024
+    cells = float(np.prod([int(info.max_coord[a]) - int(info.min_coord[a]) + 1
+                           for a in range(3)])) if dense > 0 else 0.0
+    grid_bytes = 2 * 16 * cells + max(dense - 16 * cells, 0.0)
     return int(per_point * n + per_seg * S + per_vox * V + 16 * cap + grid_bytes)
 
 
@@ -559,7 +563,8 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
             "build_hbm_frac": nbytes / (info.build_ms / 1e3) / 1e9 / peaks()[0]["hbm_gbs"],
             "hash_capacity": int(info.hash_capacity),
             "hash_load": info.num_voxels / info.hash_capacity, "max_probe": int(info.max_probe),
-            "cell_index": (f"dense grid {info.dense_grid_mib:.0f} MiB"
+            "cell_index": (f"dense grid {info.dense_grid_mib:.0f} MiB, "
+                           f"{info.masks_per_cell} mask(s) per cell"
                            if info.dense_grid_mib > 0 else "hash"),
             "sampled_voxels_membership_counts_means_bitexact_vs_oracle": exact,
             "sampled_cov_max_f32_ulp": cov_ulp, "sampled_icov_max_f32_ulp": icov_ulp,
@@ -945,7 +950,8 @@ def run_ours(args):
             "config": {"workload": "sequence: 5M-pt 400x400 m map, 20k-pt 128-ring scans, "
                                    "batched alignment", "batch": B, "scan_points": 20000,
                        "map_points": args.map_points, "map_voxels": int(info.num_voxels),
-                       "cell_index": (f"dense grid {info.dense_grid_mib:.1f} MiB"
+                       "cell_index": (f"dense grid {info.dense_grid_mib:.1f} MiB, "
+                                      f"{info.masks_per_cell} neighbourhood mask(s) per cell"
                                       if info.dense_grid_mib > 0 else "hash"),
                        "semantics": "graph kernels K1-K5", "l2": "flushed (256 MB write) "
                        "between steps",

@@ -116,7 +116,8 @@ class MapInfo(C.Structure):
                 ("num_voxels", C.c_uint64), ("hash_capacity", C.c_uint64),
                 ("max_probe", C.c_uint32), ("key_bits", C.c_uint32 * 3),
                 ("min_coord", C.c_int32 * 3), ("max_coord", C.c_int32 * 3),
-                ("build_ms", C.c_float), ("dense_grid_mib", C.c_float)]
+                ("build_ms", C.c_float), ("dense_grid_mib", C.c_float),
+                ("masks_per_cell", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Stats(C.Structure):

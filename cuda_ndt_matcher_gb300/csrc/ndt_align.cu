@@ -615,15 +615,16 @@ __device__ __forceinline__ int search_point(const MapView& m, const uint32_t* of
                                             const float* qh, const float* ql, int max_nb,
                                             uint32_t* nbl, int nbl_stride) {
     int32_t gc[3];
-    cell_of_sum(m, qh, ql, gc);
+    const uint32_t oct = cell_oct_of_sum(m, qh, ql, gc);
     int cnt = 0;
     if (m.grid) {
-        // dense cell index: the cell's neighbourhood mask names the occupied cells among the
-        // 27, in search order; their {centroid, slot} entries are loaded NB_BATCH at a time
-        // (independent loads in flight together), then tested in order
+        // dense cell index: the neighbourhood mask of the point's cell (octant) names the
+        // occupied cells among the 27 that it can accept, in search order; their
+        // {centroid, slot} entries are loaded NB_BATCH at a time (independent loads in flight
+        // together), then tested in order
         constexpr int NB_BATCH = 4;
         uint32_t corner;
-        uint32_t bits = nbhd_mask(m, gc, corner);
+        uint32_t bits = nbhd_mask(m, gc, oct, corner);
 #pragma unroll 1
         while (bits != 0u && cnt < max_nb) {
             float4 e[NB_BATCH];
@@ -2299,8 +2300,8 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * REGCAP))
                     if (isfinite(pv[0]) && isfinite(pv[1]) && isfinite(pv[2])) {
                         transform_point(sh.fr, pv, qh, ql);
                         int32_t gc[3];
-                        cell_of_sum(m, qh, ql, gc);
-                        bits = nbhd_mask(m, gc, corner);
+                        const uint32_t oct = cell_oct_of_sum(m, qh, ql, gc);
+                        bits = nbhd_mask(m, gc, oct, corner);
                     }
                 }
                 const int cnt = search_group<NPW>(m, s_off27, qh, ql, bits, corner, P.max_nb,

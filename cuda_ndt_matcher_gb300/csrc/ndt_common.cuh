@@ -47,11 +47,15 @@ struct MapView {
     // slot -1 for an empty cell
     const float4* grid;
     uint32_t ext[3];
-    // neighbourhood masks over the dense index's box grown by one cell on every side:
-    // nmask[((ux + 1) * (ext[1] + 2) + uy + 1) * (ext[2] + 2) + uz + 1] has bit
+    // neighbourhood masks over the dense index's box grown by one cell on every side, 2^msh
+    // of them per cell: msh = 0, one mask per cell; msh = 3, one per octant of the cell
+    // (octant o: bit 2 of o set for the upper half along x, bit 1 along y, bit 0 along z).
+    // nmask[((((ux + 1) * (ext[1] + 2) + uy + 1) * (ext[2] + 2) + uz + 1) << msh) + o] has bit
     // 9 (dx + 1) + 3 (dy + 1) + (dz + 1) set when local cell (ux + dx, uy + dy, uz + dz) holds
-    // a voxel; ascending bits are the reference's 27-cell search order (dx outer, dz inner)
+    // a voxel whose centroid a point of that cell (octant) can accept; ascending bits are the
+    // reference's 27-cell search order (dx outer, dz inner)
     const uint32_t* nmask;
+    uint32_t msh;
 };
 
 // Column (ux, uy) of local cells lies inside the dense index. Local coordinates are unsigned
@@ -60,12 +64,13 @@ __device__ __forceinline__ bool grid_in(const MapView& m, uint32_t ux, uint32_t 
     return ux < m.ext[0] && uy < m.ext[1];
 }
 
-// Occupied neighbours of cell gc (dense index only): the neighbourhood mask (0 when gc lies
-// more than one cell outside the box), and in `corner` the dense-index position of cell
+// Occupied neighbours of cell gc (dense index only) that a point in octant `oct` of it
+// (cell_oct_of_sum) can accept: the neighbourhood mask (0 when gc lies more than one cell
+// outside the box), and in `corner` the dense-index position of cell
 // gc - (1, 1, 1), from which nbhd_index finds each neighbour. Positions are computed modulo
 // 2^32: the corner of a cell in the outer ring lies outside the box, but every neighbour
 // whose bit is set lies inside it, so its position comes out exact.
-__device__ __forceinline__ uint32_t nbhd_mask(const MapView& m, const int32_t* gc,
+__device__ __forceinline__ uint32_t nbhd_mask(const MapView& m, const int32_t* gc, uint32_t oct,
                                               uint32_t& corner) {
     const uint32_t mx = (uint32_t)gc[0] - (uint32_t)m.min_cell[0] + 1u;
     const uint32_t my = (uint32_t)gc[1] - (uint32_t)m.min_cell[1] + 1u;
@@ -73,7 +78,8 @@ __device__ __forceinline__ uint32_t nbhd_mask(const MapView& m, const int32_t* g
     const uint32_t E1 = m.ext[1] + 2u, E2 = m.ext[2] + 2u;
     corner = ((mx - 2u) * m.ext[1] + (my - 2u)) * m.ext[2] + (mz - 2u);
     if (mx >= m.ext[0] + 2u || my >= E1 || mz >= E2) return 0u;
-    return __ldg(m.nmask + ((size_t)mx * E1 + my) * E2 + mz);
+    const size_t cell = ((size_t)mx * E1 + my) * E2 + mz;
+    return __ldg(m.nmask + (cell << m.msh) + (oct & ((1u << m.msh) - 1u)));
 }
 
 // Dense-index position of neighbour b (bit b of the mask) of the cell whose corner is given.
@@ -196,6 +202,24 @@ __device__ __forceinline__ void cell_of_sum(const MapView& m, const float* qh, c
         if (m.exact_inv && f == fl && ql[i] < 0.f) fl -= 1.f;
         gc[i] = (int32_t)fl;
     }
+}
+
+// cell_of_sum, and the point's octant in that cell: bit 2 (x), 1 (y), 0 (z) set when the
+// point lies in the upper half along that axis (f - floor(f) >= 1/2, exact in f32). A point
+// within rounding of a half-cell face may land in either octant; the octant masks are widened
+// by more than that rounding, so either octant's mask lists every neighbour the point accepts.
+__device__ __forceinline__ uint32_t cell_oct_of_sum(const MapView& m, const float* qh,
+                                                    const float* ql, int32_t* gc) {
+    uint32_t oct = 0u;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float f = __fmul_rn(qh[i], m.inv_res);
+        float fl = floorf(f);
+        if (m.exact_inv && f == fl && ql[i] < 0.f) fl -= 1.f;
+        gc[i] = (int32_t)fl;
+        oct = (oct << 1) | (f - fl >= 0.5f ? 1u : 0u);
+    }
+    return oct;
 }
 
 // Offsets in the reference's fixed order (ndt_graph_kernels.cu:29-39): dx outer, dz inner.

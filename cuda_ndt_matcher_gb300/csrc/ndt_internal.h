@@ -159,6 +159,9 @@ constexpr int TRACE_REC = 48;
 
 // Largest dense cell index a map build makes (bytes); beyond it the kernels probe the hash.
 constexpr uint64_t DENSE_GRID_MAX_BYTES = 4096ull << 20;
+// octant neighbourhood masks (32 B per cell of the grown box) up to this size, else one
+// mask per cell (4 B): the octant masks cost eight times the scatter of one mask per cell
+constexpr uint64_t OCTANT_MASK_MAX_BYTES = 256ull << 20;
 
 struct AlignParams {
     MapView map;

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
         transform_comp(Th, Tl, px, py, pz, qh, ql);
         const float qx = qh[0], qy = qh[1], qz = qh[2];
         int32_t gc[3];
-        cell_of_sum(m, qh, ql, gc);
+        const uint32_t oct = cell_oct_of_sum(m, qh, ql, gc);
         const int32_t gx = gc[0], gy = gc[1], gz = gc[2];
         float best = -INFINITY, sum = 0.f;
         int cnt = 0;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(ST) k_score(MapView m, const float* __restrict
         };
         if (m.grid) {  // occupied neighbours only, in the same order, from the mask
             uint32_t corner;
-            uint32_t bits = nbhd_mask(m, gc, corner);
+            uint32_t bits = nbhd_mask(m, gc, oct, corner);
 #pragma unroll 1
             while (bits != 0u) {
                 const uint32_t b = (uint32_t)(__ffs(bits) - 1);

@@ -137,6 +137,10 @@ typedef struct ndt_map_info {
     int32_t max_coord[3];
     float build_ms;                /* device time of the last set_target build */
     float dense_grid_mib;          /* size of the dense cell index, 0 when the hash serves */
+    uint32_t masks_per_cell;       /* neighbourhood masks per cell of the dense index: 1, or 8
+                                      (one per octant) while they take at most 256 MiB; 0 when
+                                      the hash serves */
+    uint32_t reserved;
 } ndt_map_info;
 
 /* Counters accumulated by a context since creation or the last ndt_stats_reset. */

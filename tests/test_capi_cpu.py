@@ -43,6 +43,7 @@ def test_struct_layouts():
     assert C.sizeof(capi.ParticleConfig) == 4 + 4 + 4 * 8 + 8
     assert C.sizeof(capi.PoseEstimate) == 12 * 8 + 3 * 8 + 4 * 4
     assert C.sizeof(capi.Stats) == 19 * 8
+    assert C.sizeof(capi.MapInfo) == 4 * 8 + 4 + 3 * 12 + 2 * 4 + 2 * 4
     assert C.sizeof(capi.PNetStats) == 5 * 8
 
 

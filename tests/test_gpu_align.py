@@ -223,3 +223,50 @@ def test_reference_scenarios(gpu):
     assert m2.evaluate_nvtl(synth.voxelize_pcd(mp, 1.0), np.eye(4)) > 0
     res = m.align_parallel_scans([(scan, matcher.translation(100, 100, 0))] * 3)
     assert len(res) == 3 and all(abs(x.pose[0, 3] - 100) < 2 for x in res)
+
+
+def test_octant_masks_equal_hash_search(gpu):
+    """The dense index's octant neighbourhood masks drop only voxels that no point of the
+    octant can accept, so every search lists what the hash-probing search lists: aligned
+    batches (both Newton kernels, both semantics) and scores of points on and one f32 step
+    beside the cells' faces and half-faces are equal bit for bit with the two cell indexes."""
+    seq = synth.Sequence(seed=4, n_map=1_000_000, n_scans=24, scan_points=0)
+    scans = [seq.scan(k) for k in range(0, 24, 3)]
+    rng = np.random.default_rng(3)
+    poses = []
+    for k in range(0, 24, 3):
+        p = seq.guess(k)
+        p[:2] += rng.uniform(-1.0, 1.0, 2)  # longer trajectories through more cells
+        poses.append(p)
+    forms = ({}, {"work_queue": 8, "threads_per_cta": 256, "max_registers": 64},
+             {"semantics": 1})
+    for form in forms:
+        dense = capi.Context(cell_index=0, **form)
+        hashed = capi.Context(cell_index=1, **form)
+        for c in (dense, hashed):
+            c.set_target(seq.map)
+        assert dense.map_info().masks_per_cell == 8
+        assert hashed.map_info().masks_per_cell == 0
+        a = dense.align_batch(scans, poses)
+        b = hashed.align_batch(scans, poses)
+        for i, (x, y) in enumerate(zip(a, b)):
+            assert x["iterations"] == y["iterations"], (form, i)
+            assert np.array_equal(x["pose"], y["pose"]), (form, i)
+            assert x["num_correspondences"] == y["num_correspondences"], (form, i)
+            assert x["score"] == y["score"] and x["nvtl"] == y["nvtl"], (form, i)
+    # points on the faces and half-faces of the voxels' cells and one f32 step either side
+    coords, means, _, _, _ = dense.map_voxels()
+    pick = rng.choice(len(coords), 4000, replace=False)
+    res = np.float32(2.0)
+    pts = []
+    for frac in (0.0, 0.5):
+        for axis in range(3):
+            p = means[pick, :3].astype(np.float32).copy()
+            p[:, axis] = ((coords[pick, axis] + frac) * res).astype(np.float32)
+            pts += [p, np.nextafter(p, np.float32(np.inf)), np.nextafter(p, np.float32(-np.inf))]
+    pts = np.concatenate(pts)
+    T = [np.hstack([np.eye(3), np.zeros((3, 1))]),
+         np.hstack([np.eye(3), np.array([[0.5], [-0.25], [0.125]])])]
+    nd, td = dense.eval_batch(pts, T)
+    nh, th = hashed.eval_batch(pts, T)
+    assert np.array_equal(nd, nh) and np.array_equal(td, th), (nd, nh, td, th)
