@@ -135,6 +135,14 @@ __device__ const uint32_t FRAME_TERMS[90] = {
 // null the B_kl entries are skipped (a line-search candidate needs the gradient only).
 __device__ __noinline__ void make_frame_warp(const double* pose, bool small, float* fr,
                                              double* trig, double* Ad, double* Bd, int lane) {
+    // each lane's term words first: their loads overlap the sines and cosines
+    const int nterms = Bd ? 90 : 36;
+    uint32_t words[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int e = lane + 32 * k;
+        words[k] = e < nterms ? __ldg(FRAME_TERMS + e) : 0u;
+    }
     if (lane < 3) {
         double s, c;
         sincos(pose[3 + lane], &s, &c);
@@ -153,9 +161,12 @@ __device__ __noinline__ void make_frame_warp(const double* pose, bool small, flo
         trig[14] = 1.0;
     }
     __syncwarp();
-    const int nterms = Bd ? 90 : 36;
-    for (int e = lane; e < nterms; e += 32) {
-        const uint32_t w = __ldg(FRAME_TERMS + e);
+    // a lane's (up to) three terms are independent: unrolled, their FP64 chains overlap
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int e = lane + 32 * k;
+        if (e >= nterms) break;
+        const uint32_t w = words[k];
         const double* f = e < 9 ? trig : trig + 8;
         const double t0 = f[w & 7u] * f[(w >> 3) & 7u] * f[(w >> 6) & 7u];
         const double t1 = f[(w >> 9) & 7u] * f[(w >> 12) & 7u] * f[(w >> 15) & 7u];
@@ -1930,6 +1941,7 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
                                            uint32_t it, int lane) {
     const unsigned long long c0 = clock64();
     QCtl* q = P.qctl + job;
+    const AlignJob jb = P.jobs[job];  // loaded with the state, used after the solve
     uint64_t cnt[2] = {0, 0};  // lane 0: point-iterations and correspondences so far
     {  // the state: every load in flight at once (one L2 round trip), then into shared memory
         const double* qd = reinterpret_cast<const double*>(q);
@@ -1968,7 +1980,6 @@ __device__ __noinline__ void queue_control(const AlignParams& P, AlignShared& sh
     __syncwarp();
     solve_warp<CPU_SEM>(sh.H, sh.g, sh.solve, lane);
     const unsigned long long c2 = clock64();
-    const AlignJob jb = P.jobs[job];
     int done = 0;
     double* t = nullptr;
     if (lane == 0) {
