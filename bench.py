@@ -40,7 +40,7 @@ FLOP_PER_PAIR = 65
 # DRAM bytes (read + write) of one Newton-kernel launch of the default workload (256 scans,
 # 5M-point map, seed 2), from one ncu capture of this bench per kernel form
 NCU_ALIGN_TRAFFIC = {("k_ndt_align", 256, 5_000_000, 2): 73.3e6,
-                     ("k_ndt_queue", 256, 5_000_000, 2): 117.0e6}
+                     ("k_ndt_queue", 256, 5_000_000, 2): 126.5e6}
 
 
 def _json_default(o):

@@ -1450,6 +1450,7 @@ __global__ void k_grid_fill(MapView m, float4* __restrict__ grid) {
 // names a neighbour no point there accepts, so neighbour lists are those of the full 27-cell
 // search. On the 5M-point 400 m map at 2 m a scan point tests 16.3 candidates with one mask
 // per cell and 9.0 with octant masks, of which it accepts 5.45.
+template <bool OCT>
 __global__ void k_grid_mask(MapView m, uint32_t* __restrict__ nmask) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s > m.mask) return;
@@ -1470,7 +1471,7 @@ __global__ void k_grid_mask(MapView m, uint32_t* __restrict__ nmask) {
         const float lo = fmaxf(mu[a] - c * res, 0.f);          // above the voxel's cell floor
         const float hi = fmaxf((c + 1.f) * res - mu[a], 0.f);  // below its ceiling
         far = fmaxf(far, fabsf(c) + 2.f);
-        if (m.msh == 0) {
+        if constexpr (!OCT) {
             gap[a][2][0] = gap[a][2][1] = lo;  // d_a = +1: the cell below the voxel's
             gap[a][0][0] = gap[a][0][1] = hi;  // d_a = -1: the cell above
             gap[a][1][0] = gap[a][1][1] = 0.f;
@@ -1488,28 +1489,41 @@ __global__ void k_grid_mask(MapView m, uint32_t* __restrict__ nmask) {
     const float lim = res * (1.f + 1e-5f) + 1e-6f * far * res;
     const float lim2 = lim * lim;
     const uint32_t E1 = m.ext[1] + 2u, E2 = m.ext[2] + 2u;
-    const uint32_t nsub = 1u << m.msh;
-    // every loop unrolled, so the gap table stays in registers
+    if constexpr (!OCT) {  // one mask per cell (m.msh = 0): a rolled loop over the 27 neighbours
+#pragma unroll 1
+        for (uint32_t b = 0; b < 27u; ++b) {
+            const uint32_t dx = b / 9u, dy = b / 3u % 3u, dz = b % 3u;
+            const float gx = dx == 2u ? gap[0][2][0] : (dx == 0u ? gap[0][0][0] : 0.f);
+            const float gy = dy == 2u ? gap[1][2][0] : (dy == 0u ? gap[1][0][0] : 0.f);
+            const float gz = dz == 2u ? gap[2][2][0] : (dz == 0u ? gap[2][0][0] : 0.f);
+            if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) > lim2) continue;
+            atomicOr(nmask + ((size_t)(v[0] + 2u - dx) * E1 + (v[1] + 2u - dy)) * E2 +
+                         (v[2] + 2u - dz),
+                     1u << b);
+        }
+    } else {
+        // octant masks (m.msh = 3): every loop unrolled, so the gap table stays in registers
 #pragma unroll
-    for (uint32_t dx = 0; dx < 3u; ++dx)  // d + 1 per axis
+        for (uint32_t dx = 0; dx < 3u; ++dx)  // d + 1 per axis
 #pragma unroll
-        for (uint32_t dy = 0; dy < 3u; ++dy)
+            for (uint32_t dy = 0; dy < 3u; ++dy)
 #pragma unroll
-            for (uint32_t dz = 0; dz < 3u; ++dz) {
-                const uint32_t b = dx * 9u + dy * 3u + dz;
-                // grown-box position of cell v - d, plus one: v + 2 - (d + 1)
-                uint32_t* w = nmask + ((((size_t)(v[0] + 2u - dx) * E1 + (v[1] + 2u - dy)) * E2 +
-                                        (v[2] + 2u - dz))
-                                       << m.msh);
+                for (uint32_t dz = 0; dz < 3u; ++dz) {
+                    const uint32_t b = dx * 9u + dy * 3u + dz;
+                    // grown-box position of cell v - d, plus one: v + 2 - (d + 1)
+                    uint32_t* w = nmask + ((((size_t)(v[0] + 2u - dx) * E1 + (v[1] + 2u - dy)) *
+                                                E2 +
+                                            (v[2] + 2u - dz))
+                                           << 3);
 #pragma unroll
-                for (uint32_t o = 0; o < 8u; ++o) {
-                    if (o >= nsub) break;
-                    const float gx = gap[0][dx][(o >> 2) & 1u], gy = gap[1][dy][(o >> 1) & 1u],
-                                gz = gap[2][dz][o & 1u];
-                    if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) > lim2) continue;
-                    atomicOr(w + o, 1u << b);
+                    for (uint32_t o = 0; o < 8u; ++o) {
+                        const float gx = gap[0][dx][(o >> 2) & 1u],
+                                    gy = gap[1][dy][(o >> 1) & 1u], gz = gap[2][dz][o & 1u];
+                        if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) > lim2) continue;
+                        atomicOr(w + o, 1u << b);
+                    }
                 }
-            }
+    }
 }
 
 static uint32_t bit_width(uint32_t x) {
@@ -1699,7 +1713,10 @@ int finish_map(Map& map, BuildScratch& sc, const SegRec* rec, const uint32_t* va
         cudaMemsetAsync(map.grid.p, 0xFF, (size_t)cells * 16, s);
         cudaMemsetAsync(map.nmask.p, 0, (size_t)mwords * 4, s);
         k_grid_fill<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (float4*)map.grid.p);
-        k_grid_mask<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (uint32_t*)map.nmask.p);
+        if (v.msh)
+            k_grid_mask<true><<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (uint32_t*)map.nmask.p);
+        else
+            k_grid_mask<false><<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(v, (uint32_t*)map.nmask.p);
         v.grid = (const float4*)map.grid.p;
         v.nmask = (const uint32_t*)map.nmask.p;
     }
