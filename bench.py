@@ -174,9 +174,10 @@ def build_bytes(info):
     segment starts, and the statistics' index and point gather (16 B); per segment: its start,
     size key and visit order, the two 16-bit size-sort passes, its record (88 B) and validity;
     per voxel: the record read back, the voxel arrays written (104 B), the hash insert's
-    reads (64 B) and slot writes (52 B) and the 27 mask words; per slot: the 16 B clear; the
-    dense index and masks: one clear and one fill of 16 B per cell, one clear of 4 B per mask
-    cell."""
+    reads (64 B) and slot writes (52 B); per slot: the 16 B clear; the dense index: one clear
+    and one fill of 16 B per cell; the neighbourhood masks (4 B each, one or eight per cell of
+    the grown box): one clear, and one write-back of the words the voxels' atomic ORs set in
+    L2."""
     n, S, V, cap = (int(info.num_points), int(info.num_segments), int(info.num_voxels),
                     int(info.hash_capacity))
     lv = max(int(b) for b in info.key_bits)
@@ -185,13 +186,13 @@ def build_bytes(info):
     passes = (end_bit + 7) // 8
     per_point = 12 + 12 + kw + 4 + passes * (kw + 2 * (kw + 4)) + 2 * kw + 16
     per_seg = 4 + 8 + 2 * 3 * 8 + 88 + 4
-    per_vox = 88 + 104 + 64 + 52 + 27 * 4
-    # dense index: the grid (16 B per cell of the box: filled, then written) and the
-    # neighbourhood masks (4 B per mask, masks_per_cell per cell of the grown box: filled)
+    per_vox = 88 + 104 + 64 + 52
+    # dense index: the grid (16 B per cell of the box: cleared, then filled) and the
+    # neighbourhood masks (the rest of dense_grid_mib: cleared, then written back)
     dense = float(info.dense_grid_mib) * 1024 * 1024
     cells = float(np.prod([int(info.max_coord[a]) - int(info.min_coord[a]) + 1
                            for a in range(3)])) if dense > 0 else 0.0
-    grid_bytes = 2 * 16 * cells + max(dense - 16 * cells, 0.0)
+    grid_bytes = 2 * 16 * cells + 2 * max(dense - 16 * cells, 0.0)
     return int(per_point * n + per_seg * S + per_vox * V + 16 * cap + grid_bytes)
 
 
