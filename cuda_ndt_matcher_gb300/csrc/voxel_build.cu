@@ -27,6 +27,10 @@
 //   6. compaction          : valid voxels keep their Morton order.
 //   7. hash insert         : bounded linear probing with atomicCAS, displacement recorded
 //                            (voxel_hash_build_kernel, src/cuda_ffi/csrc/voxel_hash.cu:69-114).
+//   8. dense cell index    : when it fits, {centroid, slot} per cell of the map's box, and
+//                            the neighbourhood masks (one per octant of each cell while they
+//                            fit their budget, else one per cell) that list the neighbours a
+//                            point there can accept.
 // Bit-exact parts (cells, keys, counts, means) use no multiply-add: cells are an f32 division,
 // means an FP64 division of an exact sum (or a running sum of adds), so FMA contraction
 // cannot change them; the regularised covariances, compared in f32 ULPs, use FMAs freely.
