@@ -579,7 +579,27 @@ def large_map_bench(n_points=50_000_000, n_scans=16):
             max(st["point_iterations"], 1),
             "dense_scan_e2e_aligns_per_s": len(scans) / wall,
             "dense_scan_median_err_m": float(np.median(err))}
+        if res == 2.0:
+            res_2m = res_al
         ctx.close()
+    # the 2 m map with a neighbourhood mask per octant of each cell (NDT_CELL_INDEX_OCTANT;
+    # the automatic choice keeps one mask per cell at this size): build and the same scans
+    ctx = capi.Context(resolution=2.0, cuda_graph=1, cell_index=2)
+    ctx.set_target(pts)
+    ctx.set_target(pts)
+    info = ctx.map_info()
+    ctx.stats_reset()                      # timed as the resolutions above
+    res_oct = ctx.align_batch(scans, guesses)
+    st = ctx.stats()
+    out["2m_octant_masks"] = {
+        "build_ms": float(info.build_ms),
+        "cell_index": f"dense grid {info.dense_grid_mib:.0f} MiB, {info.masks_per_cell} "
+                      f"mask(s) per cell",
+        "dense_scan_aligns_per_s": len(scans) / (st["align_kernel_ms"] / 1e3),
+        "same_results_as_2m": bool(all(np.array_equal(a["pose"], b["pose"]) and
+                                       a["iterations"] == b["iterations"]
+                                       for a, b in zip(res_oct, res_2m)))}
+    ctx.close()
     return out
 
 

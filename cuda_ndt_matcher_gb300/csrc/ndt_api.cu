@@ -414,7 +414,8 @@ static bool config_ok(const ndt_config& c) {
            (K == 0 || K == 1 || K == 2 || K == 4 || K == 8) &&
            (T == 0 || T == 128 || T == 256 || T == 512) &&
            (R == 0 || R == 48 || R == 64 || R == 80 || R == 128) &&
-           (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH) &&
+           (c.cell_index == NDT_CELL_INDEX_AUTO || c.cell_index == NDT_CELL_INDEX_HASH ||
+            c.cell_index == NDT_CELL_INDEX_OCTANT) &&
            (c.cuda_graph == 0 || c.cuda_graph == 1) &&
            (c.use_line_search == 0 || c.use_line_search == 1) &&
            c.work_queue >= -1 && c.work_queue <= 16 &&

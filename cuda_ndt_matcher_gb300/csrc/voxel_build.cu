@@ -1707,9 +1707,13 @@ int finish_map(Map& map, BuildScratch& sc, const SegRec* rec, const uint32_t* va
     v.msh = 0;
     const uint64_t mcells = (uint64_t)(v.ext[0] + 2) * (v.ext[1] + 2) * (v.ext[2] + 2);
     uint64_t mwords = 0;
-    if (cfg.cell_index == NDT_CELL_INDEX_AUTO && cells * 16 <= DENSE_GRID_MAX_BYTES) {
-        // octant masks (eight words per cell of the grown box) while they fit their budget
-        v.msh = mcells * 32 <= OCTANT_MASK_MAX_BYTES ? 3u : 0u;
+    if (cfg.cell_index != NDT_CELL_INDEX_HASH && cells * 16 <= DENSE_GRID_MAX_BYTES) {
+        // octant masks (eight words per cell of the grown box) while they fit their budget,
+        // or (NDT_CELL_INDEX_OCTANT) while grid and masks fit the dense index's
+        const bool oct = cfg.cell_index == NDT_CELL_INDEX_OCTANT
+                             ? cells * 16 + mcells * 32 <= DENSE_GRID_MAX_BYTES
+                             : mcells * 32 <= OCTANT_MASK_MAX_BYTES;
+        v.msh = oct ? 3u : 0u;
         mwords = mcells << v.msh;
         if ((rc = dev_reserve(map.grid, (size_t)cells * 16)) ||
             (rc = dev_reserve(map.nmask, (size_t)mwords * 4)))

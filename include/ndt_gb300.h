@@ -53,6 +53,11 @@ extern "C" {
  * 2.2 GiB): a lookup is one load. */
 #define NDT_CELL_INDEX_AUTO 0       /* dense index when it fits, else the hash */
 #define NDT_CELL_INDEX_HASH 1       /* hash probing only */
+#define NDT_CELL_INDEX_OCTANT 2     /* dense index with a neighbourhood mask per octant of each
+                                       cell whenever grid and masks fit the dense budget: AUTO
+                                       keeps one mask per cell beyond 256 MiB of masks; this
+                                       trades build time and memory on large maps for faster
+                                       searches (same results bit for bit) */
 
 #define NDT_STATUS_CONVERGED 0
 #define NDT_STATUS_MAX_ITERATIONS 1

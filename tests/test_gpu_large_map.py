@@ -85,12 +85,23 @@ def _crop_scans(big_map, n, n_points, seed):
 
 
 def test_large_map_dense_scan_alignment(gpu, big_map):
+    """Dense crop scans on the 2 m map: accurate against the truth; the same results bit for
+    bit with one neighbourhood mask per cell (the automatic choice at this size) and with
+    octant masks (NDT_CELL_INDEX_OCTANT)."""
     ctx = capi.Context(resolution=2.0)
     ctx.set_target(big_map)
+    assert ctx.map_info().masks_per_cell == 1
     poses, scans, guesses = _crop_scans(big_map, 8, 100_000, seed=3)
     res = ctx.align_batch(scans, guesses)
     err = [np.linalg.norm(r["pose"][:2] - p[:2]) for r, p in zip(res, poses)]
     assert np.median(err) < 0.1, err
+    octx = capi.Context(resolution=2.0, cell_index=2)
+    octx.set_target(big_map)
+    assert octx.map_info().masks_per_cell == 8
+    for a, b in zip(res, octx.align_batch(scans, guesses)):
+        np.testing.assert_array_equal(a["pose"], b["pose"])
+        assert a["iterations"] == b["iterations"] and a["nvtl"] == b["nvtl"]
+    octx.close()
 
 
 def test_large_map_1m_alignment_matches_oracle(gpu, oracle, big_map):
